@@ -1,0 +1,290 @@
+"""GB300-native Dual Marching Cubes, drop-in for the reference's ``dmc`` API.
+
+The reference (vcg-thin-meshgen/Framework, DMC_CUDA/DMC_CUDA/include/dmc.hpp)
+exposes ``dmc::setup_device_luts()``, ``dmc::run_dmc(vertices, triangles,
+grid, xyz_min, xyz_max, iso_value, num_smooth)`` and
+``dmc::cleanup_device_luts()``.  This module mirrors those three calls on top
+of the C ABI in include/dmc_gb300.h (library ``libdmc_gb300.so``, built from
+framework_gb300/csrc by ``framework_gb300.build``), plus an object API with
+device-memory, batched and serving entry points.
+
+All extraction runs in the CUDA library; there is no CPU fallback.  Importing
+works without a GPU, but every call that extracts fails loudly when the
+library or a CUDA device is missing.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+__all__ = ["DMCError", "Extractor", "Mesh", "setup_device_luts", "run_dmc", "cleanup_device_luts",
+           "load_library", "STATUS"]
+
+STATUS = {
+    0: "DMC_OK", 1: "DMC_ERR_INVALID_ARG", 2: "DMC_ERR_OOM", 3: "DMC_ERR_OUTPUT_OVERFLOW",
+    4: "DMC_ERR_TIMEOUT", 5: "DMC_ERR_CUDA", 6: "DMC_ERR_UNSUPPORTED", 7: "DMC_ERR_DEVICE_CHECK",
+}
+DTYPE = {"float32": 0, "uint16": 1}
+ALGO = {"auto": 0, "simple": 1, "brick": 2}
+
+# exported symbols of the C ABI (include/dmc_gb300.h)
+ABI_SYMBOLS = [
+    "dmc_version", "dmc_tables_sha256", "dmc_status_string", "dmc_create", "dmc_destroy",
+    "dmc_set_algo", "dmc_run", "dmc_mesh_free", "dmc_extract_device", "dmc_get_stats",
+]
+
+
+class DMCError(RuntimeError):
+    def __init__(self, status, what=""):
+        self.status = int(status)
+        super().__init__("%s%s" % (STATUS.get(self.status, "status %d" % self.status),
+                                   (": " + what) if what else ""))
+
+
+class _Volume(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("dtype", ctypes.c_int), ("dims", ctypes.c_uint32 * 3)]
+
+
+class _Mesh(ctypes.Structure):
+    _fields_ = [("vertices", ctypes.POINTER(ctypes.c_float)), ("quads", ctypes.POINTER(ctypes.c_uint32)),
+                ("triangles", ctypes.POINTER(ctypes.c_uint32)), ("n_vertices", ctypes.c_uint64),
+                ("n_quads", ctypes.c_uint64), ("n_triangles", ctypes.c_uint64)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("n_vertices", ctypes.c_uint64), ("n_quads", ctypes.c_uint64),
+                ("n_active_cells", ctypes.c_uint64), ("n_lut2_cells", ctypes.c_uint64),
+                ("n_dropped_quads", ctypes.c_uint64), ("device_ms", ctypes.c_float), ("algo", ctypes.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def library_path():
+    return _build.LIB
+
+
+def load_library(build_if_missing=True):
+    """Load libdmc_gb300.so (building it first if needed) and declare the ABI."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path) or not _build.up_to_date():
+        if not build_if_missing:
+            raise DMCError(5, "CUDA library %s is missing; run framework_gb300.build" % path)
+        _build.build()
+    L = ctypes.CDLL(path)
+    P = ctypes.POINTER
+    L.dmc_version.restype = ctypes.c_char_p
+    L.dmc_tables_sha256.restype = ctypes.c_char_p
+    L.dmc_status_string.restype = ctypes.c_char_p
+    L.dmc_status_string.argtypes = [ctypes.c_int]
+    L.dmc_create.argtypes = [P(ctypes.c_void_p), ctypes.c_int]
+    L.dmc_destroy.argtypes = [ctypes.c_void_p]
+    L.dmc_set_algo.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.dmc_run.argtypes = [ctypes.c_void_p, P(_Volume), P(ctypes.c_float), P(ctypes.c_float), ctypes.c_float,
+                          ctypes.c_uint32, ctypes.c_int, P(_Mesh)]
+    L.dmc_mesh_free.argtypes = [P(_Mesh)]
+    L.dmc_mesh_free.restype = None
+    L.dmc_extract_device.argtypes = [ctypes.c_void_p, P(_Volume), P(ctypes.c_float), P(ctypes.c_float), ctypes.c_float,
+                                     ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p,
+                                     ctypes.c_uint64, ctypes.c_void_p, P(ctypes.c_uint64), P(ctypes.c_uint64),
+                                     ctypes.c_void_p]
+    L.dmc_get_stats.argtypes = [ctypes.c_void_p, P(Stats)]
+    for name in ABI_SYMBOLS:
+        if name not in ("dmc_version", "dmc_tables_sha256", "dmc_status_string", "dmc_mesh_free"):
+            getattr(L, name).restype = ctypes.c_int
+    _lib = L
+    return L
+
+
+def _f3(v):
+    return (ctypes.c_float * 3)(*[float(x) for x in v])
+
+
+def _check(status, what=""):
+    if status != 0:
+        raise DMCError(status, what)
+
+
+class Mesh:
+    """Extraction result in host memory: vertices (V,3) float32, quads (Q,4)
+    uint32 and, when requested, triangles (2Q,3) uint32 in the reference's
+    split (q0,q1,q2), (q2,q3,q0)."""
+
+    def __init__(self, vertices, quads, triangles=None, stats=None):
+        self.vertices = vertices
+        self.quads = quads
+        self.triangles = triangles
+        self.stats = stats or {}
+
+    def __repr__(self):
+        return "Mesh(V=%d, Q=%d)" % (len(self.vertices), len(self.quads))
+
+
+def _volume_struct(data_ptr, dtype, dims):
+    v = _Volume()
+    v.data = data_ptr
+    v.dtype = dtype
+    v.dims[0], v.dims[1], v.dims[2] = [int(d) for d in dims]
+    return v
+
+
+def _host_volume(volume):
+    arr = np.ascontiguousarray(volume)
+    if arr.ndim != 3:
+        raise DMCError(1, "volume must be a 3-D array indexed [z, y, x]")
+    if arr.dtype == np.float32:
+        dt = 0
+    elif arr.dtype == np.uint16:
+        dt = 1
+    else:
+        raise DMCError(1, "volume dtype must be float32 or uint16, got %s" % arr.dtype)
+    nz, ny, nx = arr.shape
+    return arr, _volume_struct(arr.ctypes.data, dt, (nx, ny, nz))
+
+
+def _default_extent(dims_xyz, xyz_min, xyz_max):
+    if xyz_min is None:
+        xyz_min = (0.0, 0.0, 0.0)
+    if xyz_max is None:
+        xyz_max = tuple(float(d - 1) for d in dims_xyz)
+    return xyz_min, xyz_max
+
+
+class Extractor:
+    """One extraction context on one CUDA device (``dmc_create``)."""
+
+    def __init__(self, device=0, algo="auto"):
+        self._lib = load_library()
+        h = ctypes.c_void_p()
+        _check(self._lib.dmc_create(ctypes.byref(h), int(device)), "dmc_create(device=%d)" % device)
+        self._h = h
+        self.device = int(device)
+        self.set_algo(algo)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.dmc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_algo(self, algo):
+        _check(self._lib.dmc_set_algo(self._h, ALGO[algo] if isinstance(algo, str) else int(algo)))
+
+    def stats(self):
+        s = Stats()
+        _check(self._lib.dmc_get_stats(self._h, ctypes.byref(s)))
+        return s.as_dict()
+
+    def run(self, volume, xyz_min=None, xyz_max=None, iso=0.0, num_smooth=0, triangles=True):
+        """Host-memory extraction (``dmc_run``): numpy [z,y,x] float32/uint16 in, Mesh out."""
+        arr, vol = _host_volume(volume)
+        mn, mx = _default_extent(vol.dims, xyz_min, xyz_max)
+        m = _Mesh()
+        _check(self._lib.dmc_run(self._h, ctypes.byref(vol), _f3(mn), _f3(mx), ctypes.c_float(iso),
+                                 int(num_smooth), 1 if triangles else 0, ctypes.byref(m)), "dmc_run")
+        try:
+            V, Q = int(m.n_vertices), int(m.n_quads)
+            verts = np.ctypeslib.as_array(m.vertices, shape=(3 * V,)).reshape(V, 3).copy() if V else np.zeros((0, 3), np.float32)
+            quads = np.ctypeslib.as_array(m.quads, shape=(4 * Q,)).reshape(Q, 4).copy() if Q else np.zeros((0, 4), np.uint32)
+            tris = None
+            if triangles:
+                tris = np.ctypeslib.as_array(m.triangles, shape=(6 * Q,)).reshape(2 * Q, 3).copy() if Q else np.zeros((0, 3), np.uint32)
+        finally:
+            self._lib.dmc_mesh_free(ctypes.byref(m))
+        return Mesh(verts, quads, tris, self.stats())
+
+    def extract_device(self, volume, xyz_min=None, xyz_max=None, iso=0.0, vertices=None, quads=None,
+                       triangles=None, stream=None, dims=None, dtype=None):
+        """Device-memory extraction (``dmc_extract_device``).
+
+        ``volume`` is a CUDA tensor [z,y,x] (float32, or int16 holding uint16
+        bit patterns) or a raw device pointer with ``dims``/``dtype``.  Output
+        buffers are CUDA tensors (float32 [V,3], int32/uint32 [Q,4]); returns
+        (n_vertices, n_quads).  Raises DMCError(OUTPUT_OVERFLOW) carrying the
+        needed counts in ``.counts`` when the buffers are too small."""
+        if isinstance(volume, int):
+            ptr, dims_xyz, dt = volume, dims, DTYPE[dtype]
+        else:
+            t = volume
+            if not t.is_cuda or not t.is_contiguous() or t.dim() != 3:
+                raise DMCError(1, "volume must be a contiguous 3-D CUDA tensor")
+            name = str(t.dtype).replace("torch.", "")
+            dt = {"float32": 0, "int16": 1, "uint16": 1}.get(name)
+            if dt is None:
+                raise DMCError(1, "volume tensor dtype must be float32 or (u)int16")
+            ptr = t.data_ptr()
+            dims_xyz = (t.shape[2], t.shape[1], t.shape[0])
+        vol = _volume_struct(ptr, dt, dims_xyz)
+        mn, mx = _default_extent(vol.dims, xyz_min, xyz_max)
+        vptr = vertices.data_ptr() if vertices is not None else None
+        vcap = vertices.numel() // 3 if vertices is not None else 0
+        qptr = quads.data_ptr() if quads is not None else None
+        qcap = quads.numel() // 4 if quads is not None else 0
+        tptr = triangles.data_ptr() if triangles is not None else None
+        if triangles is not None:
+            qcap = min(qcap, triangles.numel() // 6)
+        nv, nq = ctypes.c_uint64(), ctypes.c_uint64()
+        st = stream if stream is not None else None
+        if st is not None and hasattr(st, "cuda_stream"):
+            st = st.cuda_stream
+        rc = self._lib.dmc_extract_device(self._h, ctypes.byref(vol), _f3(mn), _f3(mx), ctypes.c_float(iso), 0,
+                                          vptr, vcap, qptr, qcap, tptr, ctypes.byref(nv), ctypes.byref(nq), st)
+        if rc != 0:
+            e = DMCError(rc, "dmc_extract_device")
+            e.counts = (int(nv.value), int(nq.value))
+            raise e
+        return int(nv.value), int(nq.value)
+
+
+# ---------------------------------------------------------------------------
+# reference-shaped module API (dmc.hpp:40-57)
+
+_default = None
+
+
+def setup_device_luts(device=0):
+    """``dmc::setup_device_luts()``: create the process-wide default context."""
+    global _default
+    if _default is None:
+        _default = Extractor(device)
+    return _default
+
+
+def cleanup_device_luts():
+    """``dmc::cleanup_device_luts()``: release the default context."""
+    global _default
+    if _default is not None:
+        _default.close()
+        _default = None
+
+
+def run_dmc(scalar_grid, xyz_min, xyz_max, iso_value, num_smooth=0):
+    """``dmc::run_dmc``: returns (vertices float32 (V,3), triangles uint32 (T,3)).
+
+    ``scalar_grid`` is indexed [z, y, x] (utils::Array3D layout)."""
+    ctx = setup_device_luts()
+    m = ctx.run(scalar_grid, xyz_min, xyz_max, iso_value, num_smooth=num_smooth, triangles=True)
+    return m.vertices, m.triangles

@@ -1,0 +1,292 @@
+// C ABI entry points (include/dmc_gb300.h): context, table upload, host and
+// device forms of the extraction.
+#include <stdlib.h>
+#include <string.h>
+#include <new>
+#include "dmc_internal.h"
+
+namespace dmc {
+
+static thread_local cudaError_t g_last_cuda = cudaSuccess;
+void set_last_cuda_error(cudaError_t e) { g_last_cuda = e; }
+
+dmc_status ctx_reserve_scratch(Ctx *ctx, size_t bytes)
+{
+    if (bytes <= ctx->scratch_bytes) return DMC_OK;
+    if (ctx->scratch) { cudaFree(ctx->scratch); ctx->scratch = nullptr; ctx->scratch_bytes = 0; }
+    size_t want = bytes + bytes / 8;   // headroom: fewer re-allocations across calls
+    CUDA_TRY(cudaMalloc(&ctx->scratch, want));
+    ctx->scratch_bytes = want;
+    return DMC_OK;
+}
+
+static dmc_status reserve(void **p, size_t *have, size_t bytes)
+{
+    if (bytes <= *have) return DMC_OK;
+    if (*p) { cudaFree(*p); *p = nullptr; *have = 0; }
+    size_t want = bytes + bytes / 8 + 256;
+    CUDA_TRY(cudaMalloc(p, want));
+    *have = want;
+    return DMC_OK;
+}
+
+dmc_status upload_tables(Ctx *ctx)
+{
+    DeviceTables h;
+    memcpy(h.edge_lut[0], DMC_EDGE_LUT1, sizeof(h.edge_lut[0]));
+    memcpy(h.edge_lut[1], DMC_EDGE_LUT2, sizeof(h.edge_lut[1]));
+    memcpy(h.nvert[0], DMC_NVERT_LUT1, sizeof(h.nvert[0]));
+    memcpy(h.nvert[1], DMC_NVERT_LUT2, sizeof(h.nvert[1]));
+    memcpy(h.amb_face, DMC_AMBIGUOUS_FACE, sizeof(h.amb_face));
+    memset(h.face_dir, 0, sizeof(h.face_dir));
+    memcpy(h.face_dir, DMC_FACE_DIR, 6);
+    CUDA_TRY(cudaMalloc(&ctx->d_tab, sizeof(DeviceTables)));
+    CUDA_TRY(cudaMemcpy(ctx->d_tab, &h, sizeof(DeviceTables), cudaMemcpyHostToDevice));
+    return DMC_OK;
+}
+
+struct OutBufs {
+    void *v = nullptr, *q = nullptr, *t = nullptr;
+    size_t vb = 0, qb = 0, tb = 0;
+};
+
+}  // namespace dmc
+
+using namespace dmc;
+
+struct dmc_ctx {
+    Ctx c;
+    OutBufs out;
+};
+
+static bool valid_volume(const dmc_volume *vol)
+{
+    if (!vol || !vol->data) return false;
+    if (vol->dtype != DMC_F32 && vol->dtype != DMC_U16) return false;
+    return true;
+}
+
+static dmc_status make_args(const dmc_volume *vol, const float mn[3], const float mx[3], float iso, ExtractArgs &a)
+{
+    if (!valid_volume(vol) || !mn || !mx) return DMC_ERR_INVALID_ARG;
+    memset(&a, 0, sizeof(a));
+    a.vol = vol->data;
+    a.dtype = vol->dtype;
+    a.pts = make_uint3(vol->dims[0], vol->dims[1], vol->dims[2]);
+    uint3 c;
+    c.x = vol->dims[0] > 0 ? vol->dims[0] - 1 : 0;
+    c.y = vol->dims[1] > 0 ? vol->dims[1] - 1 : 0;
+    c.z = vol->dims[2] > 0 ? vol->dims[2] - 1 : 0;
+    a.cells = c;
+    a.n_cells = (uint64_t)c.x * c.y * c.z;
+    // 32-bit cell indices inside the kernels' per-axis math; the totals are 64-bit
+    if (a.n_cells >= (1ull << 40)) return DMC_ERR_UNSUPPORTED;
+    a.iso = iso;
+    a.mn = make_float3(mn[0], mn[1], mn[2]);
+    // utils.hpp / dmc.cu:2149: xyz_range = xyz_max - xyz_min
+    a.rng = make_float3(mx[0] - mn[0], mx[1] - mn[1], mx[2] - mn[2]);
+    return DMC_OK;
+}
+
+static uint64_t volume_bytes(const dmc_volume *vol)
+{
+    return (uint64_t)vol->dims[0] * vol->dims[1] * vol->dims[2] * (vol->dtype == DMC_U16 ? 2 : 4);
+}
+
+// Runs the selected path.  On return *a.n_vertices/*a.n_quads hold the totals.
+static dmc_status run_path(dmc_ctx *ctx, ExtractArgs &a, cudaStream_t st)
+{
+    Ctx *c = &ctx->c;
+    int algo = c->algo;
+    if (algo == DMC_ALGO_AUTO) algo = brick_supports(a) ? DMC_ALGO_BRICK : DMC_ALGO_SIMPLE;
+    if (algo == DMC_ALGO_BRICK && !brick_supports(a)) return DMC_ERR_UNSUPPORTED;
+    c->stats.algo = algo;
+    return algo == DMC_ALGO_BRICK ? brick_run(c, a, st) : simple_run(c, a, st);
+}
+
+static dmc_status finish(dmc_ctx *ctx, cudaStream_t st)
+{
+    Ctx *c = &ctx->c;
+    CUDA_TRY(cudaEventRecord(c->ev1, st));
+    CUDA_TRY(cudaMemcpyAsync(c->h_ctl, c->d_ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    c->stats.device_ms = ms;
+    uint32_t err = c->h_ctl->err;
+    if (err & DEV_ERR_TIMEOUT) return DMC_ERR_TIMEOUT;
+    if (err & DEV_ERR_OVERFLOW) return DMC_ERR_OUTPUT_OVERFLOW;
+    if (err & DEV_ERR_BOUNDS) return DMC_ERR_DEVICE_CHECK;
+    return DMC_OK;
+}
+
+extern "C" {
+
+const char *dmc_version(void) { return "gb300-dmc 0.1.0 (sm_103a)"; }
+
+const char *dmc_tables_sha256(void) { return DMC_TABLES_SHA256; }
+
+const char *dmc_status_string(dmc_status s)
+{
+    switch (s) {
+    case DMC_OK: return "ok";
+    case DMC_ERR_INVALID_ARG: return "invalid argument";
+    case DMC_ERR_OOM: return "out of device memory";
+    case DMC_ERR_OUTPUT_OVERFLOW: return "output buffers too small or more than 2^32-1 vertices/quads";
+    case DMC_ERR_TIMEOUT: return "a bounded device-side wait timed out";
+    case DMC_ERR_CUDA: return "CUDA error";
+    case DMC_ERR_UNSUPPORTED: return "unsupported input for the selected path";
+    case DMC_ERR_DEVICE_CHECK: return "device-side bounds check failed";
+    }
+    return "unknown status";
+}
+
+dmc_status dmc_create(dmc_ctx **out, int device)
+{
+    if (!out) return DMC_ERR_INVALID_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return DMC_ERR_INVALID_ARG;
+    dmc_ctx *ctx = new (std::nothrow) dmc_ctx();
+    if (!ctx) return DMC_ERR_OOM;
+    Ctx *c = &ctx->c;
+    c->device = device;
+    dmc_status s = DMC_OK;
+    do {
+        if (cudaSetDevice(device) != cudaSuccess) { s = DMC_ERR_CUDA; break; }
+        cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+        if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { s = DMC_ERR_CUDA; break; }
+        if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) { s = DMC_ERR_CUDA; break; }
+        if (cudaMalloc(&c->d_ctl, sizeof(DevCtl)) != cudaSuccess) { s = DMC_ERR_OOM; break; }
+        if (cudaMallocHost(&c->h_ctl, sizeof(DevCtl)) != cudaSuccess) { s = DMC_ERR_OOM; break; }
+        s = upload_tables(c);
+    } while (0);
+    if (s != DMC_OK) { dmc_destroy(ctx); return s; }
+    *out = ctx;
+    return DMC_OK;
+}
+
+dmc_status dmc_destroy(dmc_ctx *ctx)
+{
+    if (!ctx) return DMC_ERR_INVALID_ARG;
+    Ctx *c = &ctx->c;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    cudaFree(c->scratch); cudaFree(c->d_ctl); cudaFree(c->d_tab); cudaFree(c->d_vol);
+    cudaFree(ctx->out.v); cudaFree(ctx->out.q); cudaFree(ctx->out.t);
+    if (c->h_ctl) cudaFreeHost(c->h_ctl);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete ctx;
+    return DMC_OK;
+}
+
+dmc_status dmc_set_algo(dmc_ctx *ctx, dmc_algo algo)
+{
+    if (!ctx || algo < DMC_ALGO_AUTO || algo > DMC_ALGO_BRICK) return DMC_ERR_INVALID_ARG;
+    ctx->c.algo = algo;
+    return DMC_OK;
+}
+
+dmc_status dmc_get_stats(const dmc_ctx *ctx, dmc_stats *stats)
+{
+    if (!ctx || !stats) return DMC_ERR_INVALID_ARG;
+    *stats = ctx->c.stats;
+    return DMC_OK;
+}
+
+void dmc_mesh_free(dmc_mesh *m)
+{
+    if (!m) return;
+    free(m->vertices); free(m->quads); free(m->triangles);
+    memset(m, 0, sizeof(*m));
+}
+
+dmc_status dmc_extract_device(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min[3], const float xyz_max[3],
+                              float iso, uint32_t num_smooth, float *d_vertices, uint64_t vertex_capacity,
+                              uint32_t *d_quads, uint64_t quad_capacity, uint32_t *d_triangles,
+                              uint64_t *n_vertices, uint64_t *n_quads, void *stream)
+{
+    if (!ctx || !n_vertices || !n_quads) return DMC_ERR_INVALID_ARG;
+    if (num_smooth) return DMC_ERR_UNSUPPORTED;
+    ExtractArgs a;
+    dmc_status s = make_args(vol, xyz_min, xyz_max, iso, a);
+    if (s != DMC_OK) return s;
+    if ((vertex_capacity && !d_vertices) || (quad_capacity && !d_quads)) return DMC_ERR_INVALID_ARG;
+    Ctx *c = &ctx->c;
+    if (cudaSetDevice(c->device) != cudaSuccess) return DMC_ERR_CUDA;
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    a.verts = d_vertices; a.vcap = vertex_capacity;
+    a.quads = d_quads; a.qcap = quad_capacity;
+    a.tris = d_triangles;
+    a.n_vertices = n_vertices; a.n_quads = n_quads;
+    *n_vertices = 0; *n_quads = 0;
+    c->stats = dmc_stats{};
+    CUDA_TRY(cudaEventRecord(c->ev0, st));
+    if (a.n_cells == 0) return finish(ctx, st);
+    s = run_path(ctx, a, st);
+    dmc_status f = finish(ctx, st);
+    if (s == DMC_OK) s = f;
+    c->stats.n_vertices = *n_vertices;
+    c->stats.n_quads = *n_quads;
+    return s;
+}
+
+dmc_status dmc_run(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min[3], const float xyz_max[3],
+                   float iso, uint32_t num_smooth, int want_triangles, dmc_mesh *out)
+{
+    if (!ctx || !out) return DMC_ERR_INVALID_ARG;
+    memset(out, 0, sizeof(*out));
+    if (num_smooth) return DMC_ERR_UNSUPPORTED;
+    ExtractArgs a;
+    dmc_status s = make_args(vol, xyz_min, xyz_max, iso, a);
+    if (s != DMC_OK) return s;
+    Ctx *c = &ctx->c;
+    if (cudaSetDevice(c->device) != cudaSuccess) return DMC_ERR_CUDA;
+    cudaStream_t st = c->stream;
+    c->stats = dmc_stats{};
+    uint64_t V = 0, Q = 0;
+    a.n_vertices = &V; a.n_quads = &Q;
+    CUDA_TRY(cudaEventRecord(c->ev0, st));
+    if (a.n_cells > 0) {
+        // upload the host volume (dmc.cu:2077-2079)
+        uint64_t bytes = volume_bytes(vol);
+        s = reserve(&c->d_vol, &c->d_vol_bytes, bytes);
+        if (s != DMC_OK) return s;
+        CUDA_TRY(cudaMemcpyAsync(c->d_vol, vol->data, bytes, cudaMemcpyHostToDevice, st));
+        a.vol = c->d_vol;
+        // first try into the context's output buffers as they are; grow and
+        // retry once if the mesh is larger
+        for (int attempt = 0; attempt < 2; ++attempt) {
+            a.verts = (float *)ctx->out.v; a.vcap = ctx->out.vb / 12;
+            a.quads = (uint32_t *)ctx->out.q; a.qcap = ctx->out.qb / 16;
+            a.tris = want_triangles ? (uint32_t *)ctx->out.t : nullptr;
+            if (want_triangles && ctx->out.tb / 24 < a.qcap) a.qcap = ctx->out.tb / 24;
+            s = run_path(ctx, a, st);
+            if (s != DMC_ERR_OUTPUT_OVERFLOW || attempt == 1) break;
+            if (V >= 0xFFFFFFFFull || Q >= 0xFFFFFFFFull) break;
+            if ((s = reserve(&ctx->out.v, &ctx->out.vb, 12 * (V ? V : 1))) != DMC_OK) return s;
+            if ((s = reserve(&ctx->out.q, &ctx->out.qb, 16 * (Q ? Q : 1))) != DMC_OK) return s;
+            if (want_triangles && (s = reserve(&ctx->out.t, &ctx->out.tb, 24 * (Q ? Q : 1))) != DMC_OK) return s;
+            CUDA_TRY(cudaMemsetAsync(c->d_ctl, 0, sizeof(DevCtl), st));
+        }
+        if (s != DMC_OK) { finish(ctx, st); return s; }
+    }
+    s = finish(ctx, st);
+    c->stats.n_vertices = V; c->stats.n_quads = Q;
+    if (s != DMC_OK) return s;
+    // download the mesh (dmc.cu:2197-2205)
+    out->n_vertices = V; out->n_quads = Q; out->n_triangles = want_triangles ? 2 * Q : 0;
+    out->vertices = (float *)malloc(V ? 12 * V : 1);
+    out->quads = (uint32_t *)malloc(Q ? 16 * Q : 1);
+    if (want_triangles) out->triangles = (uint32_t *)malloc(Q ? 24 * Q : 1);
+    if (!out->vertices || !out->quads || (want_triangles && !out->triangles)) { dmc_mesh_free(out); return DMC_ERR_OOM; }
+    if (V) CUDA_TRY(cudaMemcpyAsync(out->vertices, ctx->out.v, 12 * V, cudaMemcpyDeviceToHost, st));
+    if (Q) CUDA_TRY(cudaMemcpyAsync(out->quads, ctx->out.q, 16 * Q, cudaMemcpyDeviceToHost, st));
+    if (Q && want_triangles) CUDA_TRY(cudaMemcpyAsync(out->triangles, ctx->out.t, 24 * Q, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return DMC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,267 @@
+// Simple extraction path: per-cell arrays, one look-back scan, per-cell emit.
+//
+// This path keeps one byte of configuration and one byte of counts per cell
+// and a 32-bit vertex and quad offset per cell (10 bytes per cell of scratch).
+// It is the straightforward restatement of the reference pipeline
+// (dmc.cu:2069-2208) with the reference's compaction replaced by dense
+// per-cell offsets; it exists to cross-check the brick path at sizes the CPU
+// oracle cannot reach quickly, and as the fallback for shapes the brick path
+// does not take.
+#include "dmc_device.cuh"
+#include "dmc_scan.cuh"
+#include "dmc_internal.h"
+
+namespace dmc {
+
+constexpr int kSimpleThreads = 256;
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;                 // cells per thread in the scan
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ void cell_xyz(uint64_t c, uint3 cells, uint32_t &x, uint32_t &y, uint32_t &z)
+{
+    uint64_t xy = (uint64_t)cells.x * cells.y;
+    z = (uint32_t)(c / xy);
+    uint64_t r = c - (uint64_t)z * xy;
+    y = (uint32_t)(r / cells.x);
+    x = (uint32_t)(r - (uint64_t)y * cells.x);
+}
+
+template <class T>
+__device__ __forceinline__ void load_corners(const T *vol, uint3 pts, uint32_t x, uint32_t y, uint32_t z, float v[8])
+{
+    uint64_t sy = pts.x, sz = (uint64_t)pts.x * pts.y;
+    uint64_t b = (uint64_t)z * sz + (uint64_t)y * sy + x;
+    v[0] = load_sample(vol, b);
+    v[1] = load_sample(vol, b + 1);
+    v[2] = load_sample(vol, b + sy + 1);
+    v[3] = load_sample(vol, b + sy);
+    v[4] = load_sample(vol, b + sz);
+    v[5] = load_sample(vol, b + sz + 1);
+    v[6] = load_sample(vol, b + sz + sy + 1);
+    v[7] = load_sample(vol, b + sz + sy);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kSimpleThreads) simple_classify(const T *vol, uint3 pts, uint3 cells, float iso,
+                                                                  uint8_t *cfg, uint64_t n_cells)
+{
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n_cells; c += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t x, y, z;
+        cell_xyz(c, cells, x, y, z);
+        float v[8];
+        load_corners(vol, pts, x, y, z, v);
+        cfg[c] = (uint8_t)config_of(v, iso);
+    }
+}
+
+// Per cell: nv (bits 0-3), owned quads (bits 4-5), lut2 (bit 7); 0 if inactive.
+template <class T>
+__global__ void __launch_bounds__(kSimpleThreads) simple_count(const T *vol, uint3 pts, uint3 cells, float iso,
+                                                               const uint8_t *cfg, uint8_t *cnt, uint64_t n_cells,
+                                                               unsigned long long *counters, const DeviceTables *__restrict__ tabp)
+{
+    const DeviceTables &tab = *tabp;
+    uint32_t n_active = 0, n_lut2 = 0, n_dropped = 0;
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n_cells; c += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t cf = cfg[c];
+        uint8_t out = 0;
+        if (cf != 0 && cf != 0xff) {
+            uint32_t x, y, z;
+            cell_xyz(c, cells, x, y, z);
+            ++n_active;
+            bool lut2 = false;
+            uint32_t face = tab.amb_face[cf];
+            if (face != 0xffu) {
+                // face -> neighbour direction (dmc.cu:631-632, 1250-1296)
+                int dir = tab.face_dir[face];
+                long long nx = x, ny = y, nz = z;
+                if (dir == 0) nx++; else if (dir == 1) nx--; else if (dir == 2) ny++;
+                else if (dir == 3) ny--; else if (dir == 4) nz++; else nz--;
+                if (nx >= 0 && ny >= 0 && nz >= 0 && nx < cells.x && ny < cells.y && nz < cells.z) {
+                    uint32_t ncf = cfg[((uint64_t)nz * cells.y + (uint64_t)ny) * cells.x + (uint64_t)nx];
+                    lut2 = tab.amb_face[ncf] != 0xffu;
+                }
+            }
+            n_lut2 += lut2;
+            float v[8];
+            load_corners(vol, pts, x, y, z, v);
+            uint32_t info = owned_edge_info(v, iso);
+            uint32_t nv = nvert_of(tab, cf, lut2) + __popc(info & 7u);
+            uint32_t nq = 0;
+#pragma unroll
+            for (int s = 0; s < 3; ++s) {
+                if (!(info & (1u << s)) || !owned_quad_in_volume(s, x, y, z, cells)) continue;
+                if (owned_sign_change(cf, s)) ++nq; else ++n_dropped;
+            }
+            out = (uint8_t)(nv | (nq << 4) | (lut2 ? 0x80u : 0u));
+        }
+        cnt[c] = out;
+    }
+    // block reduce the counters
+    __shared__ uint32_t s_a, s_l, s_d;
+    if (threadIdx.x == 0) { s_a = 0; s_l = 0; s_d = 0; }
+    __syncthreads();
+    if (n_active) atomicAdd(&s_a, n_active);
+    if (n_lut2) atomicAdd(&s_l, n_lut2);
+    if (n_dropped) atomicAdd(&s_d, n_dropped);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (s_a) atomicAdd(&counters[0], (unsigned long long)s_a);
+        if (s_l) atomicAdd(&counters[1], (unsigned long long)s_l);
+        if (s_d) atomicAdd(&counters[2], (unsigned long long)s_d);
+    }
+}
+
+// Exclusive scan of (nv, nq) over all cells -> per-cell vertex and quad offsets.
+__global__ void __launch_bounds__(kScanThreads) simple_scan(const uint8_t *cnt, uint64_t n_cells, ScanCtl ctl,
+                                                            uint32_t *vbase, uint32_t *qbase)
+{
+    __shared__ uint32_t s_slot;
+    __shared__ unsigned long long s_warp[kScanThreads / 32 + 1];
+    __shared__ unsigned long long s_ex[2];
+    const uint32_t tile = claim_tile(ctl.ticket, &s_slot);
+    const uint64_t first = (uint64_t)tile * kScanTile + (uint64_t)threadIdx.x * kScanItems;
+    uint32_t nv[kScanItems], nq[kScanItems];
+    uint32_t sv = 0, sq = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+        uint64_t c = first + i;
+        uint32_t b = c < n_cells ? cnt[c] : 0u;
+        nv[i] = b & 15u; nq[i] = (b >> 4) & 3u;
+        sv += nv[i]; sq += nq[i];
+    }
+    unsigned long long tot;
+    unsigned long long ex = block_exclusive_scan<kScanThreads>((unsigned long long)sv | ((unsigned long long)sq << 32), s_warp, &tot);
+    tile_prefix(ctl, tile, (uint32_t)tot, (uint32_t)(tot >> 32), s_ex);
+    unsigned long long bv = s_ex[0] + (uint32_t)ex, bq = s_ex[1] + (uint32_t)(ex >> 32);
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+        uint64_t c = first + i;
+        if (c < n_cells) { vbase[c] = (uint32_t)bv; qbase[c] = (uint32_t)bq; }
+        bv += nv[i]; bq += nq[i];
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kSimpleThreads) simple_emit(const T *vol, uint3 pts, uint3 cells, float iso, float3 mn, float3 rng,
+                                                              const uint8_t *cfg, const uint8_t *cnt,
+                                                              const uint32_t *vbase, const uint32_t *qbase, uint64_t n_cells,
+                                                              float *verts, uint64_t vcap, uint32_t *quads, uint64_t qcap,
+                                                              uint32_t *tris, uint32_t *err, const DeviceTables *__restrict__ tabp)
+{
+    const DeviceTables &tab = *tabp;
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n_cells; c += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t b = cnt[c];
+        if (b == 0) continue;
+        uint32_t cf = cfg[c];
+        bool lut2 = (b & 0x80u) != 0;
+        uint32_t nv = b & 15u, nq = (b >> 4) & 3u;
+        uint32_t x, y, z;
+        cell_xyz(c, cells, x, y, z);
+        float v[8];
+        load_corners(vol, pts, x, y, z, v);
+        uint32_t info = owned_edge_info(v, iso);
+        uint32_t niso = nvert_of(tab, cf, lut2);
+        uint64_t vb = vbase[c];
+        if (vb + nv > vcap) { atomicOr(err, DEV_ERR_OVERFLOW); continue; }
+        Geo g = cell_geo(x, y, z, cells, rng, mn);
+        dual_vertices(tab, v, g, iso, cf, lut2, x, y, z, niso, verts + 3 * vb);
+        owned_edge_vertices(v, g, iso, info, verts + 3 * (vb + niso));
+        if (!nq) continue;
+        uint64_t q = qbase[c];
+        if (q + nq > qcap) { atomicOr(err, DEV_ERR_OVERFLOW); continue; }
+#pragma unroll
+        for (int s = 0; s < 3; ++s) {
+            if (!(info & (1u << s)) || !owned_quad_in_volume(s, x, y, z, cells) || !owned_sign_change(cf, s)) continue;
+            bool ccw = (info >> (s + 3)) & 1u;
+            uint32_t idx[4];
+#pragma unroll
+            for (int it = 0; it < 4; ++it) {
+                int k = ccw ? it : (4 - it) & 3;
+                int re, dx, dy, dz;
+                ring_entry(s, k, re, dx, dy, dz);
+                uint64_t rc = ((uint64_t)(z + dz) * cells.y + (y + dy)) * cells.x + (x + dx);
+                uint32_t rb = cnt[rc];
+                uint32_t m = lut_m(tab, cfg[rc], (rb & 0x80u) != 0, re);
+                if (m == 0xffu) { atomicOr(err, DEV_ERR_BOUNDS); m = 0; }
+                idx[it] = vbase[rc] + m;
+            }
+            uint4 qv = make_uint4(idx[0], idx[1], idx[2], idx[3]);
+            reinterpret_cast<uint4 *>(quads)[q] = qv;
+            if (tris) {
+                uint32_t *t = tris + 6 * q;
+                t[0] = idx[0]; t[1] = idx[1]; t[2] = idx[2];
+                t[3] = idx[2]; t[4] = idx[3]; t[5] = idx[0];
+            }
+            ++q;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+
+static int grid_for(uint64_t n, int threads, int num_sms)
+{
+    uint64_t blocks = (n + threads - 1) / threads;
+    uint64_t cap = (uint64_t)num_sms * 16;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    return (int)blocks;
+}
+
+template <class T>
+static dmc_status simple_run_t(Ctx *ctx, const T *vol, const ExtractArgs &a, cudaStream_t st)
+{
+    const uint64_t C = a.n_cells;
+    const uint64_t n_tiles64 = (C + kScanTile - 1) / kScanTile;
+    if (n_tiles64 >= (1ull << 31)) return DMC_ERR_UNSUPPORTED;
+    const uint32_t n_tiles = (uint32_t)n_tiles64;
+    // scratch: cfg C, cnt C, vbase 4C, qbase 4C, tiles
+    size_t off = 0;
+    auto carve = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~(size_t)255; return o; };
+    size_t o_cfg = carve(C), o_cnt = carve(C), o_vb = carve(4 * C), o_qb = carve(4 * C);
+    size_t o_tiles = carve(sizeof(TileState) * n_tiles);
+    dmc_status s = ctx_reserve_scratch(ctx, off);
+    if (s != DMC_OK) return s;
+    uint8_t *base = (uint8_t *)ctx->scratch;
+    uint8_t *cfg = base + o_cfg, *cnt = base + o_cnt;
+    uint32_t *vb = (uint32_t *)(base + o_vb), *qb = (uint32_t *)(base + o_qb);
+    TileState *tiles = (TileState *)(base + o_tiles);
+
+    CUDA_TRY(cudaMemsetAsync(tiles, 0, sizeof(TileState) * n_tiles, st));
+    CUDA_TRY(cudaMemsetAsync(ctx->d_ctl, 0, sizeof(DevCtl), st));
+    const int g = grid_for(C, kSimpleThreads, ctx->num_sms);
+    simple_classify<T><<<g, kSimpleThreads, 0, st>>>(vol, a.pts, a.cells, a.iso, cfg, C);
+    simple_count<T><<<g, kSimpleThreads, 0, st>>>(vol, a.pts, a.cells, a.iso, cfg, cnt, C, ctx->d_ctl->counters, ctx->d_tab);
+    ScanCtl ctl;
+    ctl.tiles = tiles; ctl.ticket = &ctx->d_ctl->ticket; ctl.err = &ctx->d_ctl->err;
+    ctl.totals = ctx->d_ctl->totals; ctl.n_tiles = n_tiles;
+    simple_scan<<<n_tiles, kScanThreads, 0, st>>>(cnt, C, ctl, vb, qb);
+    CUDA_TRY(cudaGetLastError());
+    // totals decide whether the caller's buffers are large enough
+    CUDA_TRY(cudaMemcpyAsync(ctx->h_ctl, ctx->d_ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (ctx->h_ctl->err & DEV_ERR_TIMEOUT) return DMC_ERR_TIMEOUT;
+    const uint64_t V = ctx->h_ctl->totals[0], Q = ctx->h_ctl->totals[1];
+    *a.n_vertices = V; *a.n_quads = Q;
+    ctx->stats.n_active_cells = ctx->h_ctl->counters[0];
+    ctx->stats.n_lut2_cells = ctx->h_ctl->counters[1];
+    ctx->stats.n_dropped_quads = ctx->h_ctl->counters[2];
+    if (V >= 0xFFFFFFFFull || Q >= 0xFFFFFFFFull) return DMC_ERR_OUTPUT_OVERFLOW;
+    if (a.sizing_only) return DMC_OK;
+    if (V > a.vcap || Q > a.qcap) return DMC_ERR_OUTPUT_OVERFLOW;
+    simple_emit<T><<<g, kSimpleThreads, 0, st>>>(vol, a.pts, a.cells, a.iso, a.mn, a.rng, cfg, cnt, vb, qb, C,
+                                                  a.verts, a.vcap, a.quads, a.qcap, a.tris, &ctx->d_ctl->err, ctx->d_tab);
+    CUDA_TRY(cudaGetLastError());
+    return DMC_OK;
+}
+
+dmc_status simple_run(Ctx *ctx, const ExtractArgs &a, cudaStream_t st)
+{
+    if (a.dtype == DMC_F32) return simple_run_t<float>(ctx, (const float *)a.vol, a, st);
+    return simple_run_t<uint16_t>(ctx, (const uint16_t *)a.vol, a, st);
+}
+
+}  // namespace dmc

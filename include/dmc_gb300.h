@@ -1,0 +1,134 @@
+/*
+ * dmc_gb300.h — C ABI of the GB300 Dual Marching Cubes extractor.
+ *
+ * The reference (vcg-thin-meshgen/Framework, DMC_CUDA/DMC_CUDA/include/dmc.hpp)
+ * exposes three C++ calls: dmc::setup_device_luts() (dmc.hpp:40),
+ * dmc::run_dmc(vertices, triangles, grid, xyz_min, xyz_max, iso, num_smooth)
+ * (dmc.hpp:56-57) and dmc::cleanup_device_luts() (dmc.hpp:48).  Each entry
+ * point below names the reference call it replaces.  The ABI uses only plain
+ * pointers, sizes and enums, so any FFI (ctypes, cgo, JNI, N-API) can bind it.
+ *
+ * Conventions
+ *  - Volumes are x-fastest: sample (x, y, z) is data[(z * ny + y) * nx + x]
+ *    (utils::Array3D, utils.hpp:38).  dims are point counts; the cell grid is
+ *    (nx-1) x (ny-1) x (nz-1).
+ *  - World coordinates follow utils::ijk_to_xyz (utils.hpp:118-122):
+ *    x(i) = (float)i / (nx-1) * (xyz_max.x - xyz_min.x) + xyz_min.x.
+ *  - Output order matches the reference: vertices grouped by active cell in
+ *    ascending cell index, dual vertices first, then the crossings of the
+ *    cell's own edges 6, 9, 10; quads grouped by owner cell, edges 6, 9, 10.
+ *    Triangles are the reference's split (q0,q1,q2), (q2,q3,q0).
+ *  - Errors are returned as dmc_status; nothing prints or exits (the reference
+ *    calls exit(1) on any CUDA error, cuda_includes.h:13-19).
+ *  - A context is used by one host thread at a time; use one context per
+ *    thread.  Calls on different contexts may run concurrently.
+ */
+#ifndef DMC_GB300_H
+#define DMC_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    DMC_OK = 0,
+    DMC_ERR_INVALID_ARG = 1,
+    DMC_ERR_OOM = 2,
+    DMC_ERR_OUTPUT_OVERFLOW = 3,   /* caller buffers too small, or > 2^32-1 vertices/quads */
+    DMC_ERR_TIMEOUT = 4,           /* a bounded device-side wait gave up */
+    DMC_ERR_CUDA = 5,
+    DMC_ERR_UNSUPPORTED = 6,
+    DMC_ERR_DEVICE_CHECK = 7       /* a device-side bounds check failed */
+} dmc_status;
+
+typedef enum { DMC_F32 = 0, DMC_U16 = 1 } dmc_dtype;
+
+/* kernel family used by an extraction */
+typedef enum {
+    DMC_ALGO_AUTO = 0,      /* the fastest path for the input */
+    DMC_ALGO_SIMPLE = 1,    /* per-cell arrays + look-back scan (cross-check path) */
+    DMC_ALGO_BRICK = 2      /* bit-sliced brick sweep, count/scan/emit */
+} dmc_algo;
+
+typedef struct dmc_ctx dmc_ctx;
+
+typedef struct {
+    const void *data;     /* host or device pointer, see the call */
+    dmc_dtype dtype;
+    uint32_t dims[3];     /* points along x, y, z */
+} dmc_volume;
+
+/* Host mesh returned by dmc_run; release with dmc_mesh_free. */
+typedef struct {
+    float *vertices;          /* 3 * n_vertices, xyz */
+    uint32_t *quads;          /* 4 * n_quads */
+    uint32_t *triangles;      /* 3 * n_triangles (2 per quad), or NULL */
+    uint64_t n_vertices;
+    uint64_t n_quads;
+    uint64_t n_triangles;
+} dmc_mesh;
+
+/* Counters of the last extraction on a context. */
+typedef struct {
+    uint64_t n_vertices;
+    uint64_t n_quads;
+    uint64_t n_active_cells;
+    uint64_t n_lut2_cells;
+    uint64_t n_dropped_quads;   /* quads the reference would index with NO_VERTEX */
+    float device_ms;            /* device time of the last call (events) */
+    int algo;                   /* dmc_algo actually used */
+} dmc_stats;
+
+/* Library version string. */
+const char *dmc_version(void);
+/* sha256 of the lookup tables compiled into the library. */
+const char *dmc_tables_sha256(void);
+/* Human-readable name of a status. */
+const char *dmc_status_string(dmc_status s);
+
+/* Replaces dmc::setup_device_luts() (dmc.hpp:40, dmc.cu:713-779): creates a
+ * context bound to CUDA device `device` holding its stream, lookup tables and
+ * scratch memory.  No global state. */
+dmc_status dmc_create(dmc_ctx **ctx, int device);
+
+/* Replaces dmc::cleanup_device_luts() (dmc.hpp:48, dmc.cu:781-811). */
+dmc_status dmc_destroy(dmc_ctx *ctx);
+
+/* Select the kernel family for later calls on this context (default AUTO). */
+dmc_status dmc_set_algo(dmc_ctx *ctx, dmc_algo algo);
+
+/* Replaces dmc::run_dmc (dmc.hpp:56-57, dmc.cu:2069-2208).  `vol->data` is
+ * HOST memory.  Copies the volume to the device, extracts, and returns the
+ * mesh in host memory allocated by the library (triangles only when
+ * want_triangles != 0).  num_smooth > 0 runs the reference's vertex smoothing
+ * (dmc.cu:1914-1981) that many times. */
+dmc_status dmc_run(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min[3], const float xyz_max[3],
+                   float iso, uint32_t num_smooth, int want_triangles, dmc_mesh *out);
+
+/* Releases the buffers of a mesh returned by dmc_run. */
+void dmc_mesh_free(dmc_mesh *mesh);
+
+/* Device-memory form of dmc::run_dmc (no reference counterpart for the
+ * zero-copy variant; same semantics).  `vol->data` is DEVICE memory.  Output
+ * buffers are caller-owned device memory with the given capacities (in
+ * vertices / quads).  d_triangles may be NULL.  On DMC_ERR_OUTPUT_OVERFLOW the
+ * counts are still reported in *n_vertices / *n_quads so the caller can
+ * retry.  `stream` is a cudaStream_t (NULL: the context's stream).  The call
+ * returns after the mesh is complete. */
+dmc_status dmc_extract_device(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min[3], const float xyz_max[3],
+                              float iso, uint32_t num_smooth,
+                              float *d_vertices, uint64_t vertex_capacity,
+                              uint32_t *d_quads, uint64_t quad_capacity,
+                              uint32_t *d_triangles,
+                              uint64_t *n_vertices, uint64_t *n_quads, void *stream);
+
+/* Counters of the last call on this context. */
+dmc_status dmc_get_stats(const dmc_ctx *ctx, dmc_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DMC_GB300_H */

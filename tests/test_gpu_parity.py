@@ -1,0 +1,136 @@
+"""GPU parity: the CUDA extractor against the CPU oracle and the golden
+fixtures, through the C ABI.  Topology and counts must be identical; vertex
+positions must match bit for bit (FP32, same operation order)."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+ALGOS = ["simple"]
+
+
+def _bits_equal(a, b):
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    return a.shape == b.shape and np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def _check(mesh, ref):
+    assert mesh.vertices.shape == ref["vertices"].shape
+    assert mesh.quads.shape == ref["quads"].shape
+    assert np.array_equal(mesh.quads, ref["quads"])
+    bad = np.flatnonzero((mesh.vertices.view(np.uint32) != ref["vertices"].view(np.uint32)).any(1))
+    assert bad.size == 0, "first differing vertices %s: gpu %s oracle %s" % (
+        bad[:5], mesh.vertices[bad[:5]], ref["vertices"][bad[:5]])
+    tri = oracle.quads_to_triangles(ref["quads"])
+    assert np.array_equal(mesh.triangles, tri)
+
+
+def _supported(ex, algo):
+    ex.set_algo(algo)
+
+
+@pytest.fixture(params=ALGOS)
+def algo_extractor(request, extractor):
+    extractor.set_algo(request.param)
+    yield extractor, request.param
+    extractor.set_algo("auto")
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))), ids=os.path.basename)
+def test_golden(algo_extractor, path):
+    ex, algo = algo_extractor
+    g = np.load(path)
+    ref = dict(vertices=g["vertices"], quads=g["quads"])
+    m = ex.run(g["volume"], g["xyz_min"], g["xyz_max"], float(g["iso"]))
+    _check(m, ref)
+    st = ex.stats()
+    assert [st["n_active_cells"], st["n_lut2_cells"], st["n_dropped_quads"]] == g["counters"][:3].tolist()
+
+
+def test_sphere_64_c1(algo_extractor):
+    from framework_gb300 import fields
+    ex, _ = algo_extractor
+    vol = fields.sphere_sdf(64, radius=20.0, noise=0.01, seed=1).numpy()
+    _check(ex.run(vol, iso=0.0), oracle.extract(vol, iso=0.0))
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_random_fields(algo_extractor, seed):
+    ex, _ = algo_extractor
+    rng = np.random.default_rng(100 + seed)
+    shape = tuple(int(s) for s in rng.integers(3, 70, 3))
+    if seed % 2:
+        vol, iso = rng.integers(0, 5, shape).astype(np.uint16), 2.0
+    else:
+        vol, iso = rng.normal(size=shape).astype(np.float32), float(rng.normal() * 0.2)
+    mn, mx = (-3.0, 0.5, 1.0), (4.0, 2.5, 9.0)
+    _check(ex.run(vol, mn, mx, iso), oracle.extract(vol, mn, mx, iso))
+
+
+@pytest.mark.parametrize("dims", [(2, 2, 2), (3, 2, 2), (2, 40, 3), (70, 2, 5), (33, 65, 2), (129, 31, 3), (257, 9, 4)])
+def test_thin_and_ragged_shapes(algo_extractor, dims):
+    from framework_gb300 import fields
+    ex, _ = algo_extractor
+    nx, ny, nz = dims
+    vol = fields.gyroid(dims, 0.7, noise=0.05, seed=sum(dims)).numpy()
+    assert vol.shape == (nz, ny, nx)
+    _check(ex.run(vol, iso=0.05), oracle.extract(vol, iso=0.05))
+
+
+def test_noise_u16_medium(algo_extractor):
+    from framework_gb300 import fields
+    ex, _ = algo_extractor
+    vol = fields.as_u16_numpy(fields.value_noise_u16((96, 80, 72), base_period=32, seed=7))
+    r = oracle.extract(vol, iso=32768.0)
+    _check(ex.run(vol, iso=32768.0), r)
+
+
+def test_blobs_128(algo_extractor):
+    from framework_gb300 import fields
+    ex, _ = algo_extractor
+    vol = fields.gaussian_blobs((128, 128, 128), count=32, sigma=(8.0, 32.0), seed=2).numpy()
+    _check(ex.run(vol, iso=0.5), oracle.extract(vol, iso=0.5))
+
+
+def test_empty_inputs(extractor):
+    for vol in (np.zeros((1, 4, 4), np.float32), np.ones((5, 5, 5), np.float32), np.zeros((3, 3, 3), np.uint16)):
+        m = extractor.run(vol, iso=0.5)
+        assert len(m.vertices) == 0 and len(m.quads) == 0
+
+
+def test_device_api_matches_host_api(extractor):
+    import torch
+    from framework_gb300 import fields
+    vol = fields.gaussian_blobs((80, 70, 60), count=8, sigma=(5.0, 12.0), seed=5)
+    ref = oracle.extract(vol.numpy(), iso=0.5)
+    d = vol.cuda()
+    V, Q = len(ref["vertices"]), len(ref["quads"])
+    # too small: overflow status carries the needed counts
+    with pytest.raises(Exception) as ei:
+        extractor.extract_device(d, iso=0.5, vertices=torch.empty((1, 3), device="cuda"), quads=torch.empty((1, 4), dtype=torch.int32, device="cuda"))
+    assert getattr(ei.value, "counts", None) == (V, Q)
+    vb = torch.empty((V, 3), device="cuda")
+    qb = torch.empty((Q, 4), dtype=torch.int32, device="cuda")
+    tb = torch.empty((2 * Q, 3), dtype=torch.int32, device="cuda")
+    nv, nq = extractor.extract_device(d, iso=0.5, vertices=vb, quads=qb, triangles=tb)
+    assert (nv, nq) == (V, Q)
+    assert _bits_equal(vb.cpu().numpy(), ref["vertices"])
+    assert np.array_equal(qb.cpu().numpy().view(np.uint32), ref["quads"])
+    assert np.array_equal(tb.cpu().numpy().view(np.uint32), ref["triangles"])
+
+
+def test_reference_shaped_module_api():
+    import framework_gb300 as fg
+    from framework_gb300 import fields
+    vol = fields.sphere_sdf(21, radius=4.1 * 2, noise=0.0).numpy()
+    fg.setup_device_luts()
+    v, t = fg.run_dmc(vol, (-5, -5, -5), (5, 5, 5), 0.0)
+    fg.cleanup_device_luts()
+    r = oracle.extract(vol, (-5, -5, -5), (5, 5, 5), 0.0)
+    assert _bits_equal(v, r["vertices"]) and np.array_equal(t, r["triangles"])
