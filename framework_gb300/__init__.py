@@ -247,9 +247,11 @@ class Extractor:
         if triangles is not None:
             qcap = min(qcap, triangles.numel() // 6)
         nv, nq = ctypes.c_uint64(), ctypes.c_uint64()
-        st = stream if stream is not None else None
-        if st is not None and hasattr(st, "cuda_stream"):
-            st = st.cuda_stream
+        if stream is None:
+            # order the work after whatever torch queued on the current stream
+            import torch
+            stream = torch.cuda.current_stream()
+        st = stream.cuda_stream if hasattr(stream, "cuda_stream") else stream
         rc = self._lib.dmc_extract_device(self._h, ctypes.byref(vol), _f3(mn), _f3(mx), ctypes.c_float(iso), 0,
                                           vptr, vcap, qptr, qcap, tptr, ctypes.byref(nv), ctypes.byref(nq), st)
         if rc != 0:
