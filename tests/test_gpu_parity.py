@@ -11,7 +11,7 @@ import oracle
 
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-ALGOS = ["simple"]
+ALGOS = ["simple", "brick"]
 
 
 def _bits_equal(a, b):
