@@ -1,28 +1,27 @@
-// Brick path: bit-sliced classification over z-sweeping bricks, a segment
-// scan with decoupled look-back, and an emit sweep that writes vertices and
-// quads at their final positions.
+// Brick path: persistent warps sweep bricks of the volume along z.
 //
-// Layout.  A brick covers W = 32*NW cell columns (one thread per column) and
-// 32 cell rows and sweeps a run of z planes.  For each point plane, every
-// thread loads its column's 34 samples (rows y0..y0+33, coalesced along x)
-// and keeps only one bit per sample, "below the isovalue", packed in a 64-bit
-// mask.  A cell's configuration is then a handful of shifts on the masks of
-// two neighbouring columns in two planes; activity for all 33 rows of a
-// column is ~12 bitwise operations.  Only active cells (a few percent) take
-// the per-cell path (2B/3B test, counts, positions).
+// A brick is 128 cell columns x 32 cell rows x ZC planes and belongs to one
+// warp; each lane owns 4 consecutive columns and reads them with one vector
+// load per row (float4 / 4 x uint16), so every warp load is a contiguous,
+// coalesced run.  For every point plane a lane keeps one bit per sample,
+// "below the isovalue", in a 64-bit mask per column (rows 0..33).  A cell's
+// configuration is a few shifts on the masks of two columns in two planes,
+// and activity for all rows of a column is ~12 bitwise operations, so only
+// active cells (a few percent) take the per-cell path.  Warps never wait for
+// each other: there is no block-level barrier anywhere.
 //
-// Ordering.  Output order is the reference's: ascending cell index (x fastest,
-// utils.hpp:72), so a brick's cells at one plane and row form a contiguous
-// output range, a "segment" (plane k, row j, x segment xs).  The count sweep
-// writes per-segment (vertices, quads); a decoupled look-back scan turns them
-// into offsets; the emit sweep recomputes the classification, ranks the
-// active cells inside each segment and writes positions and quads.
-//
-// Halo.  Quads of a cell reference the dual vertices of its +x, +y, +z
-// neighbours (dmc.cu:1636-1664).  The emit sweep therefore also classifies
-// the first cell column of the next x segment (its vertices start exactly at
-// that segment's offset) and the first row of the next brick (ranked within
-// its own segment), and defers the quads of plane k until plane k+1 is known.
+// Output order is the reference's (ascending cell index, x fastest,
+// utils.hpp:72), so the active cells of one plane, row and 128-column
+// segment form one contiguous output range, a "segment" (k, j, xs).
+//   count sweep : per segment (vertices, quads)
+//   scan        : decoupled look-back over segments -> offsets
+//   emit sweep  : ranks the active cells of each row (4 ballots per row),
+//                 writes vertex positions and quads at their final places.
+// Quads reference the dual vertices of the +x, +y, +z neighbours
+// (dmc.cu:1636-1664): the emit sweep also ranks the first cell column of the
+// next segment (its vertices start at that segment's offset) and the first
+// row of the next brick (ranked inside its own segment), and writes the quads
+// of plane k once plane k+1 has been ranked.
 #include "dmc_device.cuh"
 #include "dmc_scan.cuh"
 #include "dmc_internal.h"
@@ -31,21 +30,52 @@ namespace dmc {
 
 namespace brick {
 
-constexpr int NW = 4;                 // warps per brick
-constexpr int W = 32 * NW;            // own cell columns
-constexpr int NT = 32 * NW;           // threads
-constexpr int ROWS = 32;              // own cell rows
-constexpr int HROWS = ROWS + 1;       // with the halo row
-constexpr int HCOLS = W + 1;          // with the halo column
-constexpr int MAXL = HROWS * HCOLS;   // list capacity (every cell active)
-constexpr int ZC = 32;                // planes per brick in the two-pass form
+constexpr int CPL = 4;                    // columns per lane
+constexpr int W = 32 * CPL;               // cell columns per brick (= segment width)
+constexpr int ROWS = 32;                  // own cell rows
+constexpr int HROWS = ROWS + 1;           // with the halo row
+constexpr int MAXL = HROWS * (W + 1);     // most active cells one plane of a brick can hold
+constexpr int CAP = 512;                  // entries kept in shared memory per plane
+constexpr int OVF = MAXL - CAP;           // entries per plane that spill to global scratch
+constexpr int NWB = 8;                    // warps per block (independent)
 constexpr int SCAN_NT = 256, SCAN_ITEMS = 8, SCAN_TILE = SCAN_NT * SCAN_ITEMS;
 
 struct Geom {
     uint3 pts, cells;
-    uint32_t nxs, nyb, nzc, zc;
+    uint32_t nxs, nyb, nzb, zc;
+    uint64_t nbricks;
     float iso;
+    uint32_t iso_u16;      // uint16 samples: v < iso  <=>  v < iso_u16 (65536: always)
     float3 mn, rng;
+    const float *coord;    // point coordinates: x[0..cx], y[0..cy], z[0..cz]
+};
+
+struct WarpSmem {
+    uint64_t mask[2][W + 2];           // column masks of point planes (by parity)
+    uint32_t ball[2][HROWS][CPL];      // per row, per column-in-lane: active lanes
+    uint64_t hact[2];                  // halo column activity (bit = row)
+    uint16_t rowstart[2][HROWS + 1];   // first list entry of each row
+    uint32_t rowbase[HROWS];           // running (v | q << 16) prefix at each row start
+    uint32_t segv[2][HROWS][2];        // vertex offset of (row, own / next segment)
+    uint32_t segq[2][HROWS];           // quad offset of (row, own segment)
+    uint32_t rowv[ROWS], rowq[ROWS];   // count sweep: per-row totals
+    uint32_t ent[2][CAP];              // packed cell: vrel 11 | qrel 10 | cfg 8 | lut2 1
+    uint16_t lst[2][CAP];              // row << 8 | col
+    uint8_t info[2][CAP];              // own-edge bipolar/ccw bits
+};
+
+struct Spill {                          // per warp slot, global memory
+    uint32_t ent[2][OVF];
+    uint16_t lst[2][OVF];
+    uint8_t info[2][OVF];
+};
+
+struct WarpMem {
+    WarpSmem *s;
+    Spill *g;
+    __device__ __forceinline__ uint32_t &ent(int p, uint32_t i) { return i < CAP ? s->ent[p][i] : g->ent[p][i - CAP]; }
+    __device__ __forceinline__ uint16_t &lst(int p, uint32_t i) { return i < CAP ? s->lst[p][i] : g->lst[p][i - CAP]; }
+    __device__ __forceinline__ uint8_t &info(int p, uint32_t i) { return i < CAP ? s->info[p][i] : g->info[p][i - CAP]; }
 };
 
 __device__ __forceinline__ uint64_t seg_index(const Geom &g, uint32_t k, uint32_t j, uint32_t xs)
@@ -59,66 +89,83 @@ __device__ __forceinline__ float sample_at(const T *vol, const Geom &g, uint32_t
     return load_sample(vol, ((uint64_t)z * g.pts.y + y) * g.pts.x + x);
 }
 
-// Masks of point plane p for columns x0 .. x0+W+1 into s_mask[0..W+2).
-// Bit r of column c: sample (x0+c, y0+r, p) < iso, r in 0..33.  Samples
-// outside the volume read as 0 (their cells are never active).
-template <class T>
-__device__ __forceinline__ void load_masks(const T *vol, const Geom &g, uint32_t x0, uint32_t y0, uint32_t p,
-                                           uint64_t *s_mask)
+__device__ __forceinline__ bool below_u16(uint32_t v, uint32_t thr) { return v < thr; }
+
+// Column masks of point plane p: bit r of column c = sample (x0+c, y0+r, p)
+// below the isovalue, rows 0..33, columns 0..W+1.  Samples outside the volume
+// read as 0; cells that touch them are never treated as active.
+template <class T, bool VEC>
+__device__ __forceinline__ void load_plane(const T *vol, const Geom &g, uint32_t x0, uint32_t y0, uint32_t p,
+                                           uint64_t *m, int lane)
 {
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    uint32_t lo[CPL] = {0, 0, 0, 0}, hi[CPL] = {0, 0, 0, 0};
+    const uint32_t xb = x0 + CPL * lane;
     const bool pz = p < g.pts.z;
-    {
-        const uint32_t x = x0 + t;
-        uint32_t lo = 0, hi = 0;
-        if (pz && x < g.pts.x) {
-            const T *col = vol + (uint64_t)p * g.pts.y * g.pts.x + x;
-            const uint32_t nrow = g.pts.y > y0 ? min(34u, g.pts.y - y0) : 0u;
-            const uint64_t sx = g.pts.x;
-            if (nrow == 34) {
-                float v[34];
+    if (pz && xb < g.pts.x) {
+        const uint64_t sx = g.pts.x;
+        const T *base = vol + ((uint64_t)p * g.pts.y + y0) * sx + xb;
+        const uint32_t nrow = min(34u, g.pts.y - y0);
+        if (VEC && nrow == 34 && xb + CPL <= g.pts.x) {
+            if constexpr (sizeof(T) == 4) {
 #pragma unroll
-                for (int r = 0; r < 34; ++r) v[r] = load_sample(col, (uint64_t)(y0 + r) * sx);
-#pragma unroll
-                for (int r = 0; r < 32; ++r) lo |= (v[r] < g.iso ? 1u : 0u) << r;
-                hi = (v[32] < g.iso ? 1u : 0u) | (v[33] < g.iso ? 2u : 0u);
+                for (int r = 0; r < 34; ++r) {
+                    const float4 v = __ldg(reinterpret_cast<const float4 *>(base + (uint64_t)r * sx));
+                    const uint32_t b0 = v.x < g.iso, b1 = v.y < g.iso, b2 = v.z < g.iso, b3 = v.w < g.iso;
+                    if (r < 32) { lo[0] |= b0 << r; lo[1] |= b1 << r; lo[2] |= b2 << r; lo[3] |= b3 << r; }
+                    else { hi[0] |= b0 << (r - 32); hi[1] |= b1 << (r - 32); hi[2] |= b2 << (r - 32); hi[3] |= b3 << (r - 32); }
+                }
             } else {
-                for (uint32_t r = 0; r < nrow; ++r) {
-                    float v = load_sample(col, (uint64_t)(y0 + r) * sx);
-                    if (v < g.iso) { if (r < 32) lo |= 1u << r; else hi |= 1u << (r - 32); }
+                const uint32_t thr2 = g.iso_u16 | (g.iso_u16 << 16);
+                const bool all = g.iso_u16 > 0xffffu;
+#pragma unroll
+                for (int r = 0; r < 34; ++r) {
+                    const uint2 w = __ldg(reinterpret_cast<const uint2 *>(base + (uint64_t)r * sx));
+                    const uint32_t c0 = all ? 0xffffffffu : __vcmpltu2(w.x, thr2);
+                    const uint32_t c1 = all ? 0xffffffffu : __vcmpltu2(w.y, thr2);
+                    const uint32_t b0 = c0 & 1u, b1 = (c0 >> 16) & 1u, b2 = c1 & 1u, b3 = (c1 >> 16) & 1u;
+                    if (r < 32) { lo[0] |= b0 << r; lo[1] |= b1 << r; lo[2] |= b2 << r; lo[3] |= b3 << r; }
+                    else { hi[0] |= b0 << (r - 32); hi[1] |= b1 << (r - 32); hi[2] |= b2 << (r - 32); hi[3] |= b3 << (r - 32); }
+                }
+            }
+        } else {
+            for (uint32_t r = 0; r < nrow; ++r) {
+#pragma unroll
+                for (int j = 0; j < CPL; ++j) {
+                    if (xb + j >= g.pts.x) continue;
+                    const float v = load_sample(base, (uint64_t)r * sx + j);
+                    const uint32_t b = v < g.iso;
+                    if (r < 32) lo[j] |= b << r; else hi[j] |= b << (r - 32);
                 }
             }
         }
-        s_mask[t] = (uint64_t)lo | ((uint64_t)hi << 32);
     }
-    if (warp == NW - 1) {
 #pragma unroll
-        for (int hc = 0; hc < 2; ++hc) {
-            const uint32_t x = x0 + W + hc;
-            const bool okx = pz && x < g.pts.x;
-            const uint32_t y = y0 + lane, y2 = y0 + 32 + lane;
-            bool b = okx && y < g.pts.y && sample_at(vol, g, x, y, p) < g.iso;
-            bool b2 = okx && lane < 2 && y2 < g.pts.y && sample_at(vol, g, x, y2, p) < g.iso;
-            uint32_t lo = __ballot_sync(0xffffffffu, b);
-            uint32_t hi = __ballot_sync(0xffffffffu, b2) & 3u;
-            if (lane == 0) s_mask[W + hc] = (uint64_t)lo | ((uint64_t)hi << 32);
-        }
+    for (int j = 0; j < CPL; ++j) m[CPL * lane + j] = (uint64_t)lo[j] | ((uint64_t)hi[j] << 32);
+#pragma unroll
+    for (int hc = 0; hc < 2; ++hc) {
+        const uint32_t x = x0 + W + hc;
+        const bool okx = pz && x < g.pts.x;
+        const uint32_t y = y0 + lane, y2 = y0 + 32 + lane;
+        const bool b = okx && y < g.pts.y && sample_at(vol, g, x, y, p) < g.iso;
+        const bool b2 = okx && lane < 2 && y2 < g.pts.y && sample_at(vol, g, x, y2, p) < g.iso;
+        const uint32_t l32 = __ballot_sync(0xffffffffu, b);
+        const uint32_t h2 = __ballot_sync(0xffffffffu, b2) & 3u;
+        if (lane == 0) m[W + hc] = (uint64_t)l32 | ((uint64_t)h2 << 32);
     }
 }
 
-// Rows r (bit r) whose cell (column with masks A,B bottom and C,D top, A/C at
-// x, B/D at x+1) has corners on both sides of the isovalue.
+// Rows r (bit r) whose cell has corners on both sides (A,B: plane k columns
+// c,c+1; C,D: plane k+1).
 __device__ __forceinline__ uint64_t active_rows(uint64_t A, uint64_t B, uint64_t C, uint64_t D)
 {
-    uint64_t a = A & B & C & D, o = A | B | C | D;
+    const uint64_t a = A & B & C & D, o = A | B | C | D;
     return (o | (o >> 1)) & ~(a & (a >> 1));
 }
 
-// Configuration of the cell in row r from the four column masks
-// (corner order of dmc.cu:1044-1054).
+// Configuration of the cell in row r (corner order of dmc.cu:1044-1054).
 __device__ __forceinline__ uint32_t cfg_from_masks(uint64_t A, uint64_t B, uint64_t C, uint64_t D, int r)
 {
-    uint32_t a = (uint32_t)(A >> r), b = (uint32_t)(B >> r), c = (uint32_t)(C >> r), d = (uint32_t)(D >> r);
+    const uint32_t a = (uint32_t)(A >> r), b = (uint32_t)(B >> r), c = (uint32_t)(C >> r), d = (uint32_t)(D >> r);
     return (a & 1u) | ((b & 1u) << 1) | ((b & 2u) << 1) | ((a & 2u) << 2) |
            ((c & 1u) << 4) | ((d & 1u) << 5) | ((d & 2u) << 5) | ((c & 2u) << 6);
 }
@@ -134,25 +181,25 @@ __device__ __forceinline__ uint32_t cfg_global(const T *vol, const Geom &g, uint
     return config_of(v, g.iso);
 }
 
-// 2B/3B correction (dmc.cu:1232-1371): the cell uses LUT2 when its config is
-// one of the 36 ambiguous ones and the face neighbour's config is too.  The
-// neighbour's config comes from the masks when it lies in the window
-// (columns 0..W, rows 0..32 of plane k), otherwise from eight global loads.
+// 2B/3B correction (dmc.cu:1232-1371): LUT2 when the config is one of the 36
+// ambiguous ones and so is the face neighbour's.  The neighbour's config
+// comes from the masks when it lies in the window (columns 0..W, rows 0..32,
+// same plane), otherwise from eight global loads.
 template <class T>
 __device__ __forceinline__ bool needs_lut2(const T *vol, const Geom &g, const DeviceTables &tab, uint32_t cfg,
                                            const uint64_t *mk, const uint64_t *mk1, int c, int r,
                                            uint32_t x, uint32_t y, uint32_t z)
 {
-    uint32_t face = tab.amb_face[cfg];
+    const uint32_t face = tab.amb_face[cfg];
     if (face == 0xffu) return false;
-    int dir = tab.face_dir[face];
-    int dx = dir == 0 ? 1 : (dir == 1 ? -1 : 0);
-    int dy = dir == 2 ? 1 : (dir == 3 ? -1 : 0);
-    int dz = dir == 4 ? 1 : (dir == 5 ? -1 : 0);
-    long long nx = (long long)x + dx, ny = (long long)y + dy, nz = (long long)z + dz;
+    const int dir = tab.face_dir[face];
+    const int dx = dir == 0 ? 1 : (dir == 1 ? -1 : 0);
+    const int dy = dir == 2 ? 1 : (dir == 3 ? -1 : 0);
+    const int dz = dir == 4 ? 1 : (dir == 5 ? -1 : 0);
+    const long long nx = (long long)x + dx, ny = (long long)y + dy, nz = (long long)z + dz;
     if (nx < 0 || ny < 0 || nz < 0 || nx >= g.cells.x || ny >= g.cells.y || nz >= g.cells.z) return false;
     uint32_t ncfg;
-    int nc = c + dx, nr = r + dy;
+    const int nc = c + dx, nr = r + dy;
     if (dz == 0 && nc >= 0 && nc <= W && nr >= 0 && nr <= ROWS)
         ncfg = cfg_from_masks(mk[nc], mk[nc + 1], mk1[nc], mk1[nc + 1], nr);
     else
@@ -160,13 +207,13 @@ __device__ __forceinline__ bool needs_lut2(const T *vol, const Geom &g, const De
     return tab.amb_face[ncfg] != 0xffu;
 }
 
-// Reference bipolarity and ccw bits of the cell's own edges, from corners
-// 2, 5, 6, 7 (dmc.cu:1199-1216); see owned_edge_info.
+// Reference bipolarity and ccw bits of the cell's own edges 6, 9, 10 from
+// corners 2, 5, 6, 7 (dmc.cu:1199-1216).
 template <class T>
 __device__ __forceinline__ uint32_t owned_info_global(const T *vol, const Geom &g, uint32_t x, uint32_t y, uint32_t z)
 {
-    float v2 = sample_at(vol, g, x + 1, y + 1, z), v5 = sample_at(vol, g, x + 1, y, z + 1);
-    float v6 = sample_at(vol, g, x + 1, y + 1, z + 1), v7 = sample_at(vol, g, x, y + 1, z + 1);
+    const float v2 = sample_at(vol, g, x + 1, y + 1, z), v5 = sample_at(vol, g, x + 1, y, z + 1);
+    const float v6 = sample_at(vol, g, x + 1, y + 1, z + 1), v7 = sample_at(vol, g, x, y + 1, z + 1);
     uint32_t info = 0;
     if (ref_bipolar(v2, v6, g.iso)) info |= 1u | (v2 <= g.iso ? 8u : 0u);
     if (ref_bipolar(v5, v6, g.iso)) info |= 2u | (v5 <= g.iso ? 16u : 0u);
@@ -175,72 +222,307 @@ __device__ __forceinline__ uint32_t owned_info_global(const T *vol, const Geom &
 }
 
 __device__ __forceinline__ uint32_t quad_count(uint32_t info, uint32_t cfg, uint32_t x, uint32_t y, uint32_t z,
-                                               uint3 cells, uint32_t *dropped)
+                                               uint3 cells, uint32_t &dropped)
 {
     uint32_t nq = 0;
 #pragma unroll
     for (int s = 0; s < 3; ++s) {
         if (!(info & (1u << s)) || !owned_quad_in_volume(s, x, y, z, cells)) continue;
-        if (owned_sign_change(cfg, s)) ++nq; else ++*dropped;
+        if (owned_sign_change(cfg, s)) ++nq; else ++dropped;
     }
     return nq;
 }
 
-__device__ __forceinline__ uint64_t row_valid_mask(uint32_t y0, uint32_t cy, int rows)
+__device__ __forceinline__ uint32_t pack_cell(uint32_t vrel, uint32_t qrel, uint32_t cfg, bool l2)
 {
-    uint32_t n = cy > y0 ? min((uint32_t)rows, cy - y0) : 0u;
-    return n >= 64 ? ~0ull : ((1ull << n) - 1ull);
+    return vrel | (qrel << 11) | (cfg << 21) | ((l2 ? 1u : 0u) << 29);
+}
+__device__ __forceinline__ uint32_t cell_vrel(uint32_t p) { return p & 0x7ffu; }
+__device__ __forceinline__ uint32_t cell_qrel(uint32_t p) { return (p >> 11) & 0x3ffu; }
+__device__ __forceinline__ uint32_t cell_cfg(uint32_t p) { return (p >> 21) & 0xffu; }
+__device__ __forceinline__ bool cell_l2(uint32_t p) { return (p >> 29) & 1u; }
+
+// List index of active cell (c, r) of the plane stored at parity p.
+__device__ __forceinline__ uint32_t entry_of(const WarpSmem &s, int p, int r, int c)
+{
+    if (c == W) return s.rowstart[p][r + 1] - 1u;
+    const int l = c >> 2, j = c & 3;
+    const uint32_t lt = (1u << l) - 1u;
+    uint32_t idx = s.rowstart[p][r];
+#pragma unroll
+    for (int jj = 0; jj < CPL; ++jj) {
+        const uint32_t b = s.ball[p][r][jj];
+        idx += __popc(b & lt) + ((jj < j) ? ((b >> l) & 1u) : 0u);
+    }
+    return idx;
 }
 
-// ---------------------------------------------------------------------------
-// count sweep: per-segment (vertices, quads)
-
-template <class T>
-__global__ void __launch_bounds__(NT) brick_count(const T *__restrict__ vol, Geom g, const DeviceTables *__restrict__ tabp,
-                                                  uint2 *__restrict__ seg_cnt, unsigned long long *counters)
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane)
 {
-    __shared__ uint64_t s_mask[2][W + 2];
-    __shared__ uint32_t s_rv[ROWS], s_rq[ROWS];
-    __shared__ uint32_t s_stat[3];
-    const DeviceTables &tab = *tabp;
-    const int t = threadIdx.x;
-    const uint32_t xs = blockIdx.x, yb = blockIdx.y, zb = blockIdx.z;
-    const uint32_t x0 = xs * W, y0 = yb * ROWS, z0 = zb * g.zc;
-    const uint32_t z1 = min(z0 + g.zc, g.cells.z);
-    const uint32_t x = x0 + t;
-    const bool colok = x < g.cells.x;
-    const uint64_t rowmask = row_valid_mask(y0, g.cells.y, ROWS);
-    uint32_t n_act = 0, n_l2 = 0, n_drop = 0;
-    if (t < 3) s_stat[t] = 0;
-
-    load_masks(vol, g, x0, y0, z0, s_mask[z0 & 1]);
-    for (uint32_t k = z0; k < z1; ++k) {
-        if (t < ROWS) { s_rv[t] = 0; s_rq[t] = 0; }
-        load_masks(vol, g, x0, y0, k + 1, s_mask[(k + 1) & 1]);
-        __syncthreads();
-        const uint64_t *mk = s_mask[k & 1], *mk1 = s_mask[(k + 1) & 1];
-        uint64_t act = colok ? active_rows(mk[t], mk[t + 1], mk1[t], mk1[t + 1]) & rowmask : 0ull;
-        while (act) {
-            const int r = __ffsll((long long)act) - 1;
-            act &= act - 1;
-            const uint32_t y = y0 + r;
-            const uint32_t cfg = cfg_from_masks(mk[t], mk[t + 1], mk1[t], mk1[t + 1], r);
-            const bool l2 = needs_lut2(vol, g, tab, cfg, mk, mk1, t, r, x, y, k);
-            const uint32_t info = owned_info_global(vol, g, x, y, k);
-            const uint32_t nv = nvert_of(tab, cfg, l2) + __popc(info & 7u);
-            const uint32_t nq = quad_count(info, cfg, x, y, k, g.cells, &n_drop);
-            atomicAdd(&s_rv[r], nv);
-            if (nq) atomicAdd(&s_rq[r], nq);
-            ++n_act; n_l2 += l2;
-        }
-        __syncthreads();
-        if (t < ROWS && y0 + t < g.cells.y) seg_cnt[seg_index(g, k, y0 + t, xs)] = make_uint2(s_rv[t], s_rq[t]);
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += y;
     }
-    if (n_act) atomicAdd(&s_stat[0], n_act);
-    if (n_l2) atomicAdd(&s_stat[1], n_l2);
-    if (n_drop) atomicAdd(&s_stat[2], n_drop);
-    __syncthreads();
-    if (t < 3 && s_stat[t]) atomicAdd(&counters[t], (unsigned long long)s_stat[t]);
+    return v;
+}
+
+enum Mode { COUNT = 0, EMIT = 1 };
+
+struct EmitOut {
+    const uint2 *seg_off;
+    float *verts; uint64_t vcap;
+    uint32_t *quads; uint64_t qcap;
+    uint32_t *tris;
+};
+
+template <class T, bool VEC, int MODE>
+__global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vol, Geom g,
+                                                        const DeviceTables *__restrict__ tabp,
+                                                        uint2 *__restrict__ seg_cnt, EmitOut out,
+                                                        Spill *__restrict__ spill, uint32_t *ticket,
+                                                        unsigned long long *counters, uint32_t *err)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    WarpSmem &S = reinterpret_cast<WarpSmem *>(smem_raw)[warp];
+    WarpMem M{&S, spill + (uint64_t)blockIdx.x * NWB + warp};
+    const DeviceTables &tab = *tabp;
+    const uint32_t nrows = MODE == EMIT ? HROWS : ROWS;
+    uint32_t n_act = 0, n_l2 = 0, n_drop = 0;
+
+    for (;;) {
+        uint32_t b = 0;
+        if (lane == 0) b = atomicAdd(ticket, 1u);
+        b = __shfl_sync(0xffffffffu, b, 0);
+        if (b >= g.nbricks) break;
+        const uint32_t xs = b % g.nxs, yb = (b / g.nxs) % g.nyb, zb = b / (g.nxs * g.nyb);
+        const uint32_t x0 = xs * W, y0 = yb * ROWS, z0 = zb * g.zc;
+        const uint32_t z1 = min(z0 + g.zc, g.cells.z);
+        const uint64_t rowmask = ((1ull << min(nrows, g.cells.y - y0)) - 1ull);
+        // end of the sweep: the emit sweep visits plane z1 too (quads of plane
+        // z1-1 need it; at the volume end it only writes those quads)
+        const uint32_t kend = MODE == EMIT ? z1 : z1 - 1;
+
+        load_plane<T, VEC>(vol, g, x0, y0, z0, S.mask[z0 & 1], lane);
+        for (uint32_t k = z0; k <= kend; ++k) {
+            const int cur = k & 1, prv = cur ^ 1;
+            const bool have_plane = k < g.cells.z;
+            if (have_plane) {
+                load_plane<T, VEC>(vol, g, x0, y0, k + 1, S.mask[(k + 1) & 1], lane);
+                if (MODE == EMIT) {
+                    for (uint32_t r = lane; r < HROWS; r += 32) {
+                        const uint32_t yy = y0 + r;
+                        uint2 own = make_uint2(0, 0), nxt = make_uint2(0, 0);
+                        if (yy < g.cells.y) {
+                            own = out.seg_off[seg_index(g, k, yy, xs)];
+                            if (xs + 1 < g.nxs) nxt = out.seg_off[seg_index(g, k, yy, xs + 1)];
+                        }
+                        S.segv[cur][r][0] = own.x; S.segv[cur][r][1] = nxt.x; S.segq[cur][r] = own.y;
+                    }
+                } else {
+                    S.rowv[lane] = 0; S.rowq[lane] = 0;
+                }
+            }
+            __syncwarp();
+            const uint64_t *mk = S.mask[cur], *mk1 = S.mask[(k + 1) & 1];
+            uint32_t L = 0;
+            if (have_plane) {
+                // activity of the lane's 4 columns (and, lane 0, the halo column)
+                uint64_t act[CPL];
+#pragma unroll
+                for (int j = 0; j < CPL; ++j) {
+                    const int c = CPL * lane + j;
+                    act[j] = (x0 + c < g.cells.x) ? active_rows(mk[c], mk[c + 1], mk1[c], mk1[c + 1]) & rowmask : 0ull;
+                }
+                uint64_t hact = 0;
+                if (MODE == EMIT && lane == 0 && x0 + W < g.cells.x)
+                    hact = active_rows(mk[W], mk[W + 1], mk1[W], mk1[W + 1]) & rowmask;
+                // per-row ballots: active lanes for each column-in-lane
+                for (uint32_t r = 0; r < nrows; ++r) {
+#pragma unroll
+                    for (int j = 0; j < CPL; ++j) {
+                        const uint32_t bb = __ballot_sync(0xffffffffu, (act[j] >> r) & 1ull);
+                        if (lane == (int)(r & 31)) S.ball[cur][r][j] = bb;
+                    }
+                }
+                if (lane == 0) S.hact[cur] = hact;
+                __syncwarp();
+                // row starts: lane r counts row r; lane 0 also row 32
+                uint32_t cnt = 0, cnt32 = 0;
+                if ((uint32_t)lane < nrows) {
+#pragma unroll
+                    for (int j = 0; j < CPL; ++j) cnt += __popc(S.ball[cur][lane][j]);
+                    cnt += (uint32_t)((S.hact[cur] >> lane) & 1ull);
+                }
+                if (MODE == EMIT && lane == 0) {
+#pragma unroll
+                    for (int j = 0; j < CPL; ++j) cnt32 += __popc(S.ball[cur][32][j]);
+                    cnt32 += (uint32_t)((S.hact[cur] >> 32) & 1ull);
+                }
+                const uint32_t inc = warp_incl_scan(cnt, lane);
+                const uint32_t tot32 = __shfl_sync(0xffffffffu, inc, 31);
+                S.rowstart[cur][lane] = (uint16_t)(inc - cnt);
+                if (lane == 0) {
+                    S.rowstart[cur][32] = (uint16_t)tot32;
+                    S.rowstart[cur][33] = (uint16_t)(tot32 + cnt32);
+                }
+                L = MODE == EMIT ? tot32 + __shfl_sync(0xffffffffu, cnt32, 0) : tot32;
+                __syncwarp();
+                // scatter list entries in output order
+#pragma unroll
+                for (int j = 0; j < CPL; ++j) {
+                    uint64_t a = act[j];
+                    while (a) {
+                        const int r = __ffsll((long long)a) - 1;
+                        a &= a - 1;
+                        M.lst(cur, entry_of(S, cur, r, CPL * lane + j)) = (uint16_t)((r << 8) | (CPL * lane + j));
+                    }
+                }
+                while (hact) {
+                    const int r = __ffsll((long long)hact) - 1;
+                    hact &= hact - 1;
+                    M.lst(cur, S.rowstart[cur][r + 1] - 1u) = (uint16_t)((r << 8) | W);
+                }
+                __syncwarp();
+            }
+            // per active cell: config, LUT choice, counts; ranks; vertices
+            uint32_t run = 0;
+            for (uint32_t base = 0; base < L; base += 32) {
+                const uint32_t i = base + lane;
+                const bool valid = i < L;
+                uint32_t packed = 0, cfg = 0, info = 0, nv = 0;
+                int r = 0, c = 0;
+                bool l2 = false;
+                uint32_t x = 0, y = 0;
+                if (valid) {
+                    const uint32_t e = M.lst(cur, i);
+                    r = e >> 8; c = e & 0xff;
+                    x = x0 + c; y = y0 + r;
+                    cfg = cfg_from_masks(mk[c], mk[c + 1], mk1[c], mk1[c + 1], r);
+                    l2 = needs_lut2(vol, g, tab, cfg, mk, mk1, c, r, x, y, k);
+                    info = owned_info_global(vol, g, x, y, k);
+                    nv = nvert_of(tab, cfg, l2) + __popc(info & 7u);
+                    uint32_t nq = 0;
+                    if (r < ROWS && c < W) nq = quad_count(info, cfg, x, y, k, g.cells, n_drop);
+                    packed = nv | (nq << 16);
+                    if (MODE == COUNT) {
+                        atomicAdd(&S.rowv[r], nv);
+                        if (nq) atomicAdd(&S.rowq[r], nq);
+                        ++n_act; n_l2 += l2;
+                    }
+                }
+                if (MODE == EMIT) {
+                    const uint32_t inc = warp_incl_scan(packed, lane);
+                    const uint32_t ex = run + inc - packed;
+                    run += __shfl_sync(0xffffffffu, inc, 31);
+                    if (valid && i == S.rowstart[cur][r]) S.rowbase[r] = ex;
+                    __syncwarp();
+                    if (valid) {
+                        const uint32_t rb = S.rowbase[r];
+                        const uint32_t vrel = c == W ? 0u : (ex & 0xffffu) - (rb & 0xffffu);
+                        const uint32_t qrel = (ex >> 16) - (rb >> 16);
+                        M.ent(cur, i) = pack_cell(vrel, qrel, cfg, l2);
+                        M.info(cur, i) = (uint8_t)info;
+                        if (k < z1 && r < ROWS && c < W) {
+                            const uint64_t vb = (uint64_t)S.segv[cur][r][0] + vrel;
+                            if (vb + nv > out.vcap) {
+                                atomicOr(err, DEV_ERR_OVERFLOW);
+                            } else {
+                                float v[8];
+                                v[0] = sample_at(vol, g, x, y, k);         v[1] = sample_at(vol, g, x + 1, y, k);
+                                v[2] = sample_at(vol, g, x + 1, y + 1, k); v[3] = sample_at(vol, g, x, y + 1, k);
+                                v[4] = sample_at(vol, g, x, y, k + 1);     v[5] = sample_at(vol, g, x + 1, y, k + 1);
+                                v[6] = sample_at(vol, g, x + 1, y + 1, k + 1); v[7] = sample_at(vol, g, x, y + 1, k + 1);
+                                Geo geo;
+                                geo.x0 = g.coord[x]; geo.x1 = g.coord[x + 1];
+                                geo.y0 = g.coord[g.pts.x + y]; geo.y1 = g.coord[g.pts.x + y + 1];
+                                geo.z0 = g.coord[g.pts.x + g.pts.y + k]; geo.z1 = g.coord[g.pts.x + g.pts.y + k + 1];
+                                const uint32_t niso = nvert_of(tab, cfg, l2);
+                                dual_vertices(tab, v, geo, g.iso, cfg, l2, x, y, k, niso, out.verts + 3 * vb);
+                                owned_edge_vertices(v, geo, g.iso, info, out.verts + 3 * (vb + niso));
+                            }
+                        }
+                    }
+                    __syncwarp();
+                }
+            }
+            if (MODE == COUNT) {
+                __syncwarp();
+                if (have_plane && (uint32_t)lane < ROWS && y0 + lane < g.cells.y)
+                    seg_cnt[seg_index(g, k, y0 + lane, xs)] = make_uint2(S.rowv[lane], S.rowq[lane]);
+            }
+            // quads of own cells of plane k-1: their +z ring cells are in plane k
+            if (MODE == EMIT && k > z0) {
+                const uint32_t kp = k - 1;
+                const uint32_t Lp = S.rowstart[prv][HROWS];
+                for (uint32_t i = lane; i < Lp; i += 32) {
+                    const uint32_t e = M.lst(prv, i);
+                    const int r = e >> 8, c = e & 0xff;
+                    if (r >= ROWS || c >= W) continue;
+                    const uint32_t x = x0 + c, y = y0 + r;
+                    const uint32_t d = M.ent(prv, i);
+                    const uint32_t cfg = cell_cfg(d);
+                    const uint32_t info = M.info(prv, i);
+                    uint64_t q = (uint64_t)S.segq[prv][r] + cell_qrel(d);
+#pragma unroll
+                    for (int s = 0; s < 3; ++s) {
+                        if (!(info & (1u << s)) || !owned_quad_in_volume(s, x, y, kp, g.cells) || !owned_sign_change(cfg, s)) continue;
+                        if (q >= out.qcap) { atomicOr(err, DEV_ERR_OVERFLOW); break; }
+                        const bool ccw = (info >> (s + 3)) & 1u;
+                        uint32_t idx[4];
+#pragma unroll
+                        for (int it = 0; it < 4; ++it) {
+                            const int kk = ccw ? it : (4 - it) & 3;
+                            int re, dx, dy, dz;
+                            ring_entry(s, kk, re, dx, dy, dz);
+                            const int rr = r + dy, rc = c + dx, pl = dz ? cur : prv;
+                            const uint32_t ri = entry_of(S, pl, rr, rc);
+                            if (ri >= S.rowstart[pl][HROWS]) { atomicOr(err, DEV_ERR_BOUNDS); idx[it] = 0; continue; }
+                            const uint32_t rd = M.ent(pl, ri);
+                            uint32_t m = lut_m(tab, cell_cfg(rd), cell_l2(rd), re);
+                            if (m == 0xffu) { atomicOr(err, DEV_ERR_BOUNDS); m = 0; }
+                            idx[it] = S.segv[pl][rr][rc == W ? 1 : 0] + cell_vrel(rd) + m;
+                        }
+                        reinterpret_cast<uint4 *>(out.quads)[q] = make_uint4(idx[0], idx[1], idx[2], idx[3]);
+                        if (out.tris) {
+                            uint32_t *tp = out.tris + 6 * q;
+                            tp[0] = idx[0]; tp[1] = idx[1]; tp[2] = idx[2];
+                            tp[3] = idx[2]; tp[4] = idx[3]; tp[5] = idx[0];
+                        }
+                        ++q;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+    if (MODE == COUNT) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            n_act += __shfl_xor_sync(0xffffffffu, n_act, o);
+            n_l2 += __shfl_xor_sync(0xffffffffu, n_l2, o);
+            n_drop += __shfl_xor_sync(0xffffffffu, n_drop, o);
+        }
+        if (lane == 0) {
+            if (n_act) atomicAdd(&counters[0], (unsigned long long)n_act);
+            if (n_l2) atomicAdd(&counters[1], (unsigned long long)n_l2);
+            if (n_drop) atomicAdd(&counters[2], (unsigned long long)n_drop);
+        }
+    }
+}
+
+// point coordinates x(i) = ijk_to_xyz(i, cells.x, ...) etc. (utils.hpp:118-122)
+__global__ void coord_table(float *coord, uint3 pts, uint3 cells, float3 rng, float3 mn)
+{
+    const uint32_t n = pts.x + pts.y + pts.z;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float v;
+        if (i < pts.x) v = ijk_to_xyz(i, cells.x, rng.x, mn.x);
+        else if (i < pts.x + pts.y) v = ijk_to_xyz(i - pts.x, cells.y, rng.y, mn.y);
+        else v = ijk_to_xyz(i - pts.x - pts.y, cells.z, rng.z, mn.z);
+        coord[i] = v;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -272,276 +554,6 @@ __global__ void __launch_bounds__(SCAN_NT) seg_scan(const uint2 *__restrict__ cn
     }
 }
 
-// ---------------------------------------------------------------------------
-// emit sweep
-
-struct EmitSmem {
-    uint64_t mask[2][W + 2];
-    uint32_t dense[2][HROWS][HCOLS];     // per cell: vrel 11 | qrel 10 | cfg 8 | lut2 1  (active cells only)
-    uint16_t list[2][MAXL];              // active cells in output order: row << 9 | col
-    uint32_t nlist[2];
-    uint32_t ball[NW][HROWS];            // per warp, per row: active lanes
-    uint32_t rowstart[HROWS + 1];        // list index of each row's first entry
-    uint32_t warpbase[NW][HROWS];        // list index of warp w's first entry in row r
-    uint64_t halo_act;                   // active rows of the halo column
-    uint32_t segv[2][HROWS][2];          // vertex offset of (row, own segment / next segment)
-    uint32_t segq[2][HROWS];             // quad offset of (row, own segment)
-    uint32_t rowbase_v[HROWS], rowbase_q[HROWS];
-    uint8_t nvq[MAXL];                   // per list entry: nv | nq << 4
-    unsigned long long scan_warp[NW + 1];
-};
-
-__device__ __forceinline__ uint32_t pack_cell(uint32_t vrel, uint32_t qrel, uint32_t cfg, bool l2)
-{
-    return vrel | (qrel << 11) | (cfg << 21) | ((l2 ? 1u : 0u) << 29);
-}
-__device__ __forceinline__ uint32_t cell_vrel(uint32_t p) { return p & 0x7ffu; }
-__device__ __forceinline__ uint32_t cell_qrel(uint32_t p) { return (p >> 11) & 0x3ffu; }
-__device__ __forceinline__ uint32_t cell_cfg(uint32_t p) { return (p >> 21) & 0xffu; }
-__device__ __forceinline__ bool cell_l2(uint32_t p) { return (p >> 29) & 1u; }
-
-template <class T>
-__global__ void __launch_bounds__(NT) brick_emit(const T *__restrict__ vol, Geom g, const DeviceTables *__restrict__ tabp,
-                                                 const uint2 *__restrict__ seg_off, float *__restrict__ verts, uint64_t vcap,
-                                                 uint32_t *__restrict__ quads, uint64_t qcap, uint32_t *__restrict__ tris,
-                                                 uint32_t *err)
-{
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    EmitSmem &S = *reinterpret_cast<EmitSmem *>(smem_raw);
-    const DeviceTables &tab = *tabp;
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    const uint32_t xs = blockIdx.x, yb = blockIdx.y, zb = blockIdx.z;
-    const uint32_t x0 = xs * W, y0 = yb * ROWS, z0 = zb * g.zc;
-    const uint32_t z1 = min(z0 + g.zc, g.cells.z);             // own planes [z0, z1)
-    const uint32_t zlast = min(z1, g.cells.z - 1);             // classified planes [z0, zlast]
-    const uint64_t hrowmask = row_valid_mask(y0, g.cells.y, HROWS);
-    const bool colok = x0 + t < g.cells.x;
-    const bool halo_col_ok = x0 + W < g.cells.x;
-
-    load_masks(vol, g, x0, y0, z0, S.mask[z0 & 1]);
-    for (uint32_t k = z0; k <= zlast; ++k) {
-        const int cur = k & 1, prv = cur ^ 1;
-        load_masks(vol, g, x0, y0, k + 1, S.mask[(k + 1) & 1]);
-        // segment offsets of this plane's rows
-        if (t < HROWS) {
-            const uint32_t y = y0 + t;
-            uint2 own = make_uint2(0, 0), nxt = make_uint2(0, 0);
-            if (y < g.cells.y) {
-                own = seg_off[seg_index(g, k, y, xs)];
-                if (xs + 1 < g.nxs) nxt = seg_off[seg_index(g, k, y, xs + 1)];
-            }
-            S.segv[cur][t][0] = own.x; S.segv[cur][t][1] = nxt.x; S.segq[cur][t] = own.y;
-        }
-        __syncthreads();
-        const uint64_t *mk = S.mask[cur], *mk1 = S.mask[(k + 1) & 1];
-        // 1. activity of own column t (rows 0..32) and of the halo column
-        const uint64_t act = colok ? active_rows(mk[t], mk[t + 1], mk1[t], mk1[t + 1]) & hrowmask : 0ull;
-        if (t == 0)
-            S.halo_act = halo_col_ok ? active_rows(mk[W], mk[W + 1], mk1[W], mk1[W + 1]) & hrowmask : 0ull;
-#pragma unroll 1
-        for (int r = 0; r < HROWS; ++r) {
-            uint32_t b = __ballot_sync(0xffffffffu, (act >> r) & 1ull);
-            if (lane == 0) S.ball[warp][r] = b;
-        }
-        __syncthreads();
-        // 2. list layout: rows in order, within a row warps in order, halo column last
-        if (warp == 0) {
-            uint32_t run = 0;
-            for (int r0 = 0; r0 < HROWS; r0 += 32) {
-                const int r = r0 + lane;
-                uint32_t cnt = 0;
-                if (r < HROWS) {
-                    for (int w = 0; w < NW; ++w) cnt += __popc(S.ball[w][r]);
-                    cnt += (uint32_t)((S.halo_act >> r) & 1ull);
-                }
-                uint32_t inc = cnt;
-                for (int o = 1; o < 32; o <<= 1) {
-                    uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
-                    if (lane >= o) inc += y;
-                }
-                if (r < HROWS) {
-                    uint32_t start = run + inc - cnt;
-                    S.rowstart[r] = start;
-                    for (int w = 0; w < NW; ++w) { S.warpbase[w][r] = start; start += __popc(S.ball[w][r]); }
-                }
-                run += __shfl_sync(0xffffffffu, inc, 31);
-            }
-            if (lane == 0) { S.rowstart[HROWS] = run; S.nlist[cur] = run; }
-        }
-        __syncthreads();
-        // 3. scatter entries into the list
-        {
-            uint64_t a = act;
-            const uint32_t lt = (1u << lane) - 1u;
-            while (a) {
-                const int r = __ffsll((long long)a) - 1;
-                a &= a - 1;
-                const uint32_t pos = S.warpbase[warp][r] + __popc(S.ball[warp][r] & lt);
-                S.list[cur][pos] = (uint16_t)((r << 9) | t);
-            }
-            if (t == 0) {
-                uint64_t h = S.halo_act;
-                while (h) {
-                    const int r = __ffsll((long long)h) - 1;
-                    h &= h - 1;
-                    S.list[cur][S.rowstart[r + 1] - 1] = (uint16_t)((r << 9) | W);
-                }
-            }
-        }
-        __syncthreads();
-        // 4. per entry: config, LUT choice, counts (contiguous chunk per thread)
-        const uint32_t L = S.nlist[cur];
-        const uint32_t per = (L + NT - 1) / NT;
-        const uint32_t e0 = min(L, per * t), e1 = min(L, e0 + per);
-        uint32_t sv = 0, sq = 0;
-        for (uint32_t e = e0; e < e1; ++e) {
-            const uint32_t ent = S.list[cur][e];
-            const int r = ent >> 9, c = ent & 0x1ff;
-            const uint32_t x = x0 + c, y = y0 + r;
-            const uint32_t cfg = cfg_from_masks(mk[c], mk[c + 1], mk1[c], mk1[c + 1], r);
-            const bool l2 = needs_lut2(vol, g, tab, cfg, mk, mk1, c, r, x, y, k);
-            const uint32_t info = owned_info_global(vol, g, x, y, k);
-            const uint32_t nv = nvert_of(tab, cfg, l2) + __popc(info & 7u);
-            uint32_t nq = 0, dummy = 0;
-            if (r < ROWS && c < W) nq = quad_count(info, cfg, x, y, k, g.cells, &dummy);
-            S.nvq[e] = (uint8_t)(nv | (nq << 4));
-            S.dense[cur][r][c] = pack_cell(0, 0, cfg, l2);
-            sv += nv; sq += nq;
-        }
-        unsigned long long tot;
-        unsigned long long ex = block_exclusive_scan<NT>((unsigned long long)sv | ((unsigned long long)sq << 32), S.scan_warp, &tot);
-        uint32_t pv = (uint32_t)ex, pq = (uint32_t)(ex >> 32);
-        for (uint32_t e = e0; e < e1; ++e) {
-            const uint32_t ent = S.list[cur][e];
-            const int r = ent >> 9;
-            if (e == S.rowstart[r]) { S.rowbase_v[r] = pv; S.rowbase_q[r] = pq; }
-            const uint32_t b = S.nvq[e];
-            pv += b & 15u; pq += b >> 4;
-        }
-        __syncthreads();
-        pv = (uint32_t)ex; pq = (uint32_t)(ex >> 32);
-        for (uint32_t e = e0; e < e1; ++e) {
-            const uint32_t ent = S.list[cur][e];
-            const int r = ent >> 9, c = ent & 0x1ff;
-            uint32_t vrel = pv - S.rowbase_v[r], qrel = pq - S.rowbase_q[r];
-            if (c == W) vrel = 0;                 // first cell of the next segment
-            uint32_t &d = S.dense[cur][r][c];
-            d = pack_cell(vrel, qrel, cell_cfg(d), cell_l2(d));
-            const uint32_t b = S.nvq[e];
-            pv += b & 15u; pq += b >> 4;
-        }
-        __syncthreads();
-        // 5. vertices of own cells of plane k
-        if (k < z1) {
-            for (uint32_t e = e0; e < e1; ++e) {
-                const uint32_t ent = S.list[cur][e];
-                const int r = ent >> 9, c = ent & 0x1ff;
-                if (r >= ROWS || c >= W) continue;
-                const uint32_t x = x0 + c, y = y0 + r;
-                const uint32_t d = S.dense[cur][r][c];
-                const uint32_t cfg = cell_cfg(d);
-                const bool l2 = cell_l2(d);
-                const uint64_t vb = (uint64_t)S.segv[cur][r][0] + cell_vrel(d);
-                const uint32_t nv = S.nvq[e] & 15u;
-                if (vb + nv > vcap) { atomicOr(err, DEV_ERR_OVERFLOW); continue; }
-                float v[8];
-                v[0] = sample_at(vol, g, x, y, k);         v[1] = sample_at(vol, g, x + 1, y, k);
-                v[2] = sample_at(vol, g, x + 1, y + 1, k); v[3] = sample_at(vol, g, x, y + 1, k);
-                v[4] = sample_at(vol, g, x, y, k + 1);     v[5] = sample_at(vol, g, x + 1, y, k + 1);
-                v[6] = sample_at(vol, g, x + 1, y + 1, k + 1); v[7] = sample_at(vol, g, x, y + 1, k + 1);
-                const uint32_t info = owned_edge_info(v, g.iso);
-                const uint32_t niso = nvert_of(tab, cfg, l2);
-                Geo geo = cell_geo(x, y, k, g.cells, g.rng, g.mn);
-                dual_vertices(tab, v, geo, g.iso, cfg, l2, x, y, k, niso, verts + 3 * vb);
-                owned_edge_vertices(v, geo, g.iso, info, verts + 3 * (vb + niso));
-            }
-        }
-        // 6. quads of own cells of plane k-1 (their +z ring cells are in plane k)
-        if (k > z0) {
-            const uint32_t kp = k - 1;
-            const uint32_t Lp = S.nlist[prv];
-            const uint32_t perp = (Lp + NT - 1) / NT;
-            const uint32_t f0 = min(Lp, perp * t), f1 = min(Lp, f0 + perp);
-            for (uint32_t e = f0; e < f1; ++e) {
-                const uint32_t ent = S.list[prv][e];
-                const int r = ent >> 9, c = ent & 0x1ff;
-                if (r >= ROWS || c >= W) continue;
-                const uint32_t x = x0 + c, y = y0 + r;
-                const uint32_t d = S.dense[prv][r][c];
-                const uint32_t cfg = cell_cfg(d);
-                const uint32_t info = owned_info_global(vol, g, x, y, kp);
-                uint64_t q = (uint64_t)S.segq[prv][r] + cell_qrel(d);
-#pragma unroll
-                for (int s = 0; s < 3; ++s) {
-                    if (!(info & (1u << s)) || !owned_quad_in_volume(s, x, y, kp, g.cells) || !owned_sign_change(cfg, s)) continue;
-                    if (q >= qcap) { atomicOr(err, DEV_ERR_OVERFLOW); break; }
-                    const bool ccw = (info >> (s + 3)) & 1u;
-                    uint32_t idx[4];
-#pragma unroll
-                    for (int it = 0; it < 4; ++it) {
-                        const int kk = ccw ? it : (4 - it) & 3;
-                        int re, dx, dy, dz;
-                        ring_entry(s, kk, re, dx, dy, dz);
-                        const int rr = r + dy, rc = c + dx, pl = dz ? cur : prv;
-                        const uint32_t rd = S.dense[pl][rr][rc];
-                        uint32_t m = lut_m(tab, cell_cfg(rd), cell_l2(rd), re);
-                        if (m == 0xffu) { atomicOr(err, DEV_ERR_BOUNDS); m = 0; }
-                        idx[it] = S.segv[pl][rr][rc == W ? 1 : 0] + cell_vrel(rd) + m;
-                    }
-                    reinterpret_cast<uint4 *>(quads)[q] = make_uint4(idx[0], idx[1], idx[2], idx[3]);
-                    if (tris) {
-                        uint32_t *tp = tris + 6 * q;
-                        tp[0] = idx[0]; tp[1] = idx[1]; tp[2] = idx[2];
-                        tp[3] = idx[2]; tp[4] = idx[3]; tp[5] = idx[0];
-                    }
-                    ++q;
-                }
-            }
-        }
-        __syncthreads();
-    }
-    // quads of the last own plane when it is the last plane of the volume
-    // (only edge-6 quads remain; their ring stays in that plane)
-    if (z1 == g.cells.z && zlast + 1 == z1) {
-        const uint32_t kp = zlast;
-        const int prv = kp & 1;
-        const uint32_t Lp = S.nlist[prv];
-        const uint32_t perp = (Lp + NT - 1) / NT;
-        const uint32_t f0 = min(Lp, perp * t), f1 = min(Lp, f0 + perp);
-        for (uint32_t e = f0; e < f1; ++e) {
-            const uint32_t ent = S.list[prv][e];
-            const int r = ent >> 9, c = ent & 0x1ff;
-            if (r >= ROWS || c >= W) continue;
-            const uint32_t x = x0 + c, y = y0 + r;
-            const uint32_t d = S.dense[prv][r][c];
-            const uint32_t cfg = cell_cfg(d);
-            const uint32_t info = owned_info_global(vol, g, x, y, kp);
-            uint64_t q = (uint64_t)S.segq[prv][r] + cell_qrel(d);
-            if (!(info & 1u) || !owned_quad_in_volume(0, x, y, kp, g.cells) || !owned_sign_change(cfg, 0)) continue;
-            if (q >= qcap) { atomicOr(err, DEV_ERR_OVERFLOW); continue; }
-            const bool ccw = (info >> 3) & 1u;
-            uint32_t idx[4];
-#pragma unroll
-            for (int it = 0; it < 4; ++it) {
-                const int kk = ccw ? it : (4 - it) & 3;
-                int re, dx, dy, dz;
-                ring_entry(0, kk, re, dx, dy, dz);
-                const int rr = r + dy, rc = c + dx;
-                const uint32_t rd = S.dense[prv][rr][rc];
-                uint32_t m = lut_m(tab, cell_cfg(rd), cell_l2(rd), re);
-                if (m == 0xffu) { atomicOr(err, DEV_ERR_BOUNDS); m = 0; }
-                idx[it] = S.segv[prv][rr][rc == W ? 1 : 0] + cell_vrel(rd) + m;
-            }
-            reinterpret_cast<uint4 *>(quads)[q] = make_uint4(idx[0], idx[1], idx[2], idx[3]);
-            if (tris) {
-                uint32_t *tp = tris + 6 * q;
-                tp[0] = idx[0]; tp[1] = idx[1]; tp[2] = idx[2];
-                tp[3] = idx[2]; tp[4] = idx[3]; tp[5] = idx[0];
-            }
-        }
-    }
-}
-
 }  // namespace brick
 
 // ---------------------------------------------------------------------------
@@ -549,38 +561,88 @@ __global__ void __launch_bounds__(NT) brick_emit(const T *__restrict__ vol, Geom
 
 bool brick_supports(const ExtractArgs &a)
 {
-    // 32-bit point indices per axis; at least one cell
     return a.cells.x >= 1 && a.cells.y >= 1 && a.cells.z >= 1;
 }
 
-template <class T>
-static dmc_status brick_run_t(Ctx *ctx, const T *vol, const ExtractArgs &a, cudaStream_t st)
+template <class T, bool VEC, int MODE>
+static dmc_status launch_sweep(Ctx *ctx, const T *vol, const brick::Geom &g, uint2 *seg_cnt, const brick::EmitOut &out,
+                               brick::Spill *spill, int grid, uint32_t *ticket, cudaStream_t st)
+{
+    using namespace brick;
+    const size_t smem = sizeof(WarpSmem) * NWB;
+    CUDA_TRY(cudaFuncSetAttribute(brick_sweep<T, VEC, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    brick_sweep<T, VEC, MODE><<<grid, 32 * NWB, smem, st>>>(vol, g, ctx->d_tab, seg_cnt, out, spill, ticket,
+                                                           ctx->d_ctl->counters, &ctx->d_ctl->err);
+    CUDA_TRY(cudaGetLastError());
+    return DMC_OK;
+}
+
+template <class T, bool VEC>
+static int sweep_grid(Ctx *ctx)
+{
+    using namespace brick;
+    const size_t smem = sizeof(WarpSmem) * NWB;
+    cudaFuncSetAttribute(brick_sweep<T, VEC, EMIT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(brick_sweep<T, VEC, COUNT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int b0 = 0, b1 = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, brick_sweep<T, VEC, EMIT>, 32 * NWB, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, brick_sweep<T, VEC, COUNT>, 32 * NWB, smem);
+    int b = b0 < b1 ? b0 : b1;
+    if (b < 1) b = 1;
+    return b * ctx->num_sms;
+}
+
+template <class T, bool VEC>
+static dmc_status brick_run_v(Ctx *ctx, const T *vol, const ExtractArgs &a, cudaStream_t st)
 {
     using namespace brick;
     Geom g;
     g.pts = a.pts; g.cells = a.cells; g.iso = a.iso; g.mn = a.mn; g.rng = a.rng;
+    {
+        // uint16 compare threshold: smallest integer t with (v < iso) == (v < t)
+        float f = a.iso;
+        uint32_t t;
+        if (!(f > 0.f)) t = 0;                       // also NaN
+        else if (f > 65535.f) t = 65536;
+        else { uint32_t fl = (uint32_t)f; t = ((float)fl == f) ? fl : fl + 1; }
+        g.iso_u16 = t;
+    }
     g.nxs = (a.cells.x + W - 1) / W;
     g.nyb = (a.cells.y + ROWS - 1) / ROWS;
-    g.zc = ZC;
-    g.nzc = (a.cells.z + ZC - 1) / ZC;
-    if (g.nyb > 65535 || g.nzc > 65535) return DMC_ERR_UNSUPPORTED;
+    g.zc = 16;
+    g.nzb = (a.cells.z + g.zc - 1) / g.zc;
+    g.nbricks = (uint64_t)g.nxs * g.nyb * g.nzb;
+    if (g.nbricks >= 0xF0000000ull) return DMC_ERR_UNSUPPORTED;
     const uint64_t nseg = (uint64_t)a.cells.z * a.cells.y * g.nxs;
     const uint64_t n_tiles64 = (nseg + SCAN_TILE - 1) / SCAN_TILE;
     if (n_tiles64 >= (1ull << 31)) return DMC_ERR_UNSUPPORTED;
     const uint32_t n_tiles = (uint32_t)n_tiles64;
+    const int grid = sweep_grid<T, VEC>(ctx);
+    const uint64_t n_coord = (uint64_t)a.pts.x + a.pts.y + a.pts.z;
+
     size_t off = 0;
     auto carve = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~(size_t)255; return o; };
     const size_t o_cnt = carve(8 * nseg), o_off = carve(8 * nseg), o_tiles = carve(sizeof(TileState) * n_tiles);
+    const size_t o_spill = carve(sizeof(Spill) * (size_t)grid * NWB);
+    const size_t o_coord = carve(4 * n_coord);
+    const size_t o_tk = carve(256);
     dmc_status s = ctx_reserve_scratch(ctx, off);
     if (s != DMC_OK) return s;
     uint8_t *base = (uint8_t *)ctx->scratch;
     uint2 *seg_cnt = (uint2 *)(base + o_cnt), *seg_off = (uint2 *)(base + o_off);
     TileState *tiles = (TileState *)(base + o_tiles);
+    Spill *spill = (Spill *)(base + o_spill);
+    float *coord = (float *)(base + o_coord);
+    uint32_t *tickets = (uint32_t *)(base + o_tk);
+    g.coord = coord;
 
     CUDA_TRY(cudaMemsetAsync(tiles, 0, sizeof(TileState) * n_tiles, st));
+    CUDA_TRY(cudaMemsetAsync(tickets, 0, 256, st));
     CUDA_TRY(cudaMemsetAsync(ctx->d_ctl, 0, sizeof(DevCtl), st));
-    const dim3 grid(g.nxs, g.nyb, g.nzc);
-    brick_count<T><<<grid, NT, 0, st>>>(vol, g, ctx->d_tab, seg_cnt, ctx->d_ctl->counters);
+    coord_table<<<(unsigned)((n_coord + 255) / 256), 256, 0, st>>>(coord, a.pts, a.cells, a.rng, a.mn);
+    EmitOut none{};
+    s = launch_sweep<T, VEC, COUNT>(ctx, vol, g, seg_cnt, none, spill, grid, &tickets[0], st);
+    if (s != DMC_OK) return s;
     ScanCtl ctl;
     ctl.tiles = tiles; ctl.ticket = &ctx->d_ctl->ticket; ctl.err = &ctx->d_ctl->err;
     ctl.totals = ctx->d_ctl->totals; ctl.n_tiles = n_tiles;
@@ -597,12 +659,18 @@ static dmc_status brick_run_t(Ctx *ctx, const T *vol, const ExtractArgs &a, cuda
     if (V >= 0xFFFFFFFFull || Q >= 0xFFFFFFFFull) return DMC_ERR_OUTPUT_OVERFLOW;
     if (a.sizing_only) return DMC_OK;
     if (V > a.vcap || Q > a.qcap) return DMC_ERR_OUTPUT_OVERFLOW;
-    const size_t smem = sizeof(EmitSmem);
-    CUDA_TRY(cudaFuncSetAttribute(brick_emit<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    brick_emit<T><<<grid, NT, smem, st>>>(vol, g, ctx->d_tab, seg_off, a.verts, a.vcap, a.quads, a.qcap, a.tris,
-                                          &ctx->d_ctl->err);
-    CUDA_TRY(cudaGetLastError());
-    return DMC_OK;
+    EmitOut eo;
+    eo.seg_off = seg_off; eo.verts = a.verts; eo.vcap = a.vcap; eo.quads = a.quads; eo.qcap = a.qcap; eo.tris = a.tris;
+    return launch_sweep<T, VEC, EMIT>(ctx, vol, g, nullptr, eo, spill, grid, &tickets[1], st);
+}
+
+template <class T>
+static dmc_status brick_run_t(Ctx *ctx, const T *vol, const ExtractArgs &a, cudaStream_t st)
+{
+    // vector loads need every row start aligned to the vector size
+    const size_t vb = sizeof(T) * brick::CPL;
+    const bool vec = ((uintptr_t)vol % vb == 0) && (((size_t)a.pts.x * sizeof(T)) % vb == 0);
+    return vec ? brick_run_v<T, true>(ctx, vol, a, st) : brick_run_v<T, false>(ctx, vol, a, st);
 }
 
 dmc_status brick_run(Ctx *ctx, const ExtractArgs &a, cudaStream_t st)
