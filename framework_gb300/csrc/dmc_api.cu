@@ -40,6 +40,12 @@ dmc_status upload_tables(Ctx *ctx)
     memcpy(h.amb_face, DMC_AMBIGUOUS_FACE, sizeof(h.amb_face));
     memset(h.face_dir, 0, sizeof(h.face_dir));
     memcpy(h.face_dir, DMC_FACE_DIR, 6);
+    for (int c = 0; c < 256; ++c) {
+        uint16_t m = 0;
+        for (int e = 0; e < 12; ++e)
+            if (DMC_EDGE_LUT1[c * 12 + e] != 0xff) m |= (uint16_t)(1u << e);
+        h.crossed[c] = m;
+    }
     CUDA_TRY(cudaMalloc(&ctx->d_tab, sizeof(DeviceTables)));
     CUDA_TRY(cudaMemcpy(ctx->d_tab, &h, sizeof(DeviceTables), cudaMemcpyHostToDevice));
     return DMC_OK;

@@ -267,8 +267,6 @@ __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane)
     return v;
 }
 
-enum Mode { COUNT = 0, EMIT = 1 };
-
 struct EmitOut {
     const uint2 *seg_off;
     float *verts; uint64_t vcap;
@@ -276,59 +274,141 @@ struct EmitOut {
     uint32_t *tris;
 };
 
-template <class T, bool VEC, int MODE>
-__global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vol, Geom g,
+// Stage the lookup tables in shared memory (once per block; warps are persistent).
+__device__ __forceinline__ const DeviceTables &stage_tables(const DeviceTables *g, DeviceTables *s)
+{
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(g);
+    uint32_t *dst = reinterpret_cast<uint32_t *>(s);
+    for (uint32_t i = threadIdx.x; i < sizeof(DeviceTables) / 4; i += blockDim.x) dst[i] = src[i];
+    __syncthreads();
+    return *s;
+}
+
+__device__ __forceinline__ uint32_t claim_brick(uint32_t *ticket, int lane)
+{
+    uint32_t b = 0;
+    if (lane == 0) b = atomicAdd(ticket, 1u);
+    return __shfl_sync(0xffffffffu, b, 0);
+}
+
+// The eight corner samples of cell (x, y, z), with one 64-bit index.
+template <class T>
+__device__ __forceinline__ void load_cell(const T *vol, const Geom &g, uint32_t x, uint32_t y, uint32_t z, float v[8])
+{
+    const uint64_t sy = g.pts.x, sz = (uint64_t)g.pts.x * g.pts.y;
+    const T *p = vol + (uint64_t)z * sz + (uint64_t)y * sy + x;
+    v[0] = load_sample(p, 0);           v[1] = load_sample(p, 1);
+    v[2] = load_sample(p, sy + 1);      v[3] = load_sample(p, sy);
+    v[4] = load_sample(p, sz);          v[5] = load_sample(p, sz + 1);
+    v[6] = load_sample(p, sz + sy + 1); v[7] = load_sample(p, sz + sy);
+}
+
+// Count sweep: per segment (vertices, quads) of the brick's own 32 rows.
+template <class T, bool VEC>
+__global__ void __launch_bounds__(32 * NWB) brick_count(const T *__restrict__ vol, Geom g,
                                                         const DeviceTables *__restrict__ tabp,
-                                                        uint2 *__restrict__ seg_cnt, EmitOut out,
-                                                        Spill *__restrict__ spill, uint32_t *ticket,
-                                                        unsigned long long *counters, uint32_t *err)
+                                                        uint2 *__restrict__ seg_cnt, uint32_t *ticket,
+                                                        unsigned long long *counters)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    WarpSmem &S = reinterpret_cast<WarpSmem *>(smem_raw)[warp];
-    WarpMem M{&S, spill + (uint64_t)blockIdx.x * NWB + warp};
-    const DeviceTables &tab = *tabp;
-    const uint32_t nrows = MODE == EMIT ? HROWS : ROWS;
+    const DeviceTables &tab = stage_tables(tabp, reinterpret_cast<DeviceTables *>(smem_raw));
+    WarpSmem &S = reinterpret_cast<WarpSmem *>(smem_raw + sizeof(DeviceTables))[warp];
     uint32_t n_act = 0, n_l2 = 0, n_drop = 0;
+    S.rowv[lane] = 0;
 
     for (;;) {
-        uint32_t b = 0;
-        if (lane == 0) b = atomicAdd(ticket, 1u);
-        b = __shfl_sync(0xffffffffu, b, 0);
+        const uint32_t b = claim_brick(ticket, lane);
         if (b >= g.nbricks) break;
         const uint32_t xs = b % g.nxs, yb = (b / g.nxs) % g.nyb, zb = b / (g.nxs * g.nyb);
         const uint32_t x0 = xs * W, y0 = yb * ROWS, z0 = zb * g.zc;
         const uint32_t z1 = min(z0 + g.zc, g.cells.z);
-        const uint64_t rowmask = ((1ull << min(nrows, g.cells.y - y0)) - 1ull);
-        // end of the sweep: the emit sweep visits plane z1 too (quads of plane
-        // z1-1 need it; at the volume end it only writes those quads)
-        const uint32_t kend = MODE == EMIT ? z1 : z1 - 1;
-
+        const uint64_t rowmask = ((1ull << min((uint32_t)ROWS, g.cells.y - y0)) - 1ull);
         load_plane<T, VEC>(vol, g, x0, y0, z0, S.mask[z0 & 1], lane);
-        for (uint32_t k = z0; k <= kend; ++k) {
-            const int cur = k & 1, prv = cur ^ 1;
-            const bool have_plane = k < g.cells.z;
-            if (have_plane) {
-                load_plane<T, VEC>(vol, g, x0, y0, k + 1, S.mask[(k + 1) & 1], lane);
-                if (MODE == EMIT) {
-                    for (uint32_t r = lane; r < HROWS; r += 32) {
-                        const uint32_t yy = y0 + r;
-                        uint2 own = make_uint2(0, 0), nxt = make_uint2(0, 0);
-                        if (yy < g.cells.y) {
-                            own = out.seg_off[seg_index(g, k, yy, xs)];
-                            if (xs + 1 < g.nxs) nxt = out.seg_off[seg_index(g, k, yy, xs + 1)];
-                        }
-                        S.segv[cur][r][0] = own.x; S.segv[cur][r][1] = nxt.x; S.segq[cur][r] = own.y;
-                    }
-                } else {
-                    S.rowv[lane] = 0; S.rowq[lane] = 0;
+        for (uint32_t k = z0; k < z1; ++k) {
+            load_plane<T, VEC>(vol, g, x0, y0, k + 1, S.mask[(k + 1) & 1], lane);
+            __syncwarp();
+            const uint64_t *mk = S.mask[k & 1], *mk1 = S.mask[(k + 1) & 1];
+#pragma unroll 1
+            for (int j = 0; j < CPL; ++j) {
+                const int c = CPL * lane + j;
+                const uint32_t x = x0 + c;
+                uint64_t a = x < g.cells.x ? active_rows(mk[c], mk[c + 1], mk1[c], mk1[c + 1]) & rowmask : 0ull;
+                while (a) {
+                    const int r = __ffsll((long long)a) - 1;
+                    a &= a - 1;
+                    const uint32_t y = y0 + r;
+                    const uint32_t cfg = cfg_from_masks(mk[c], mk[c + 1], mk1[c], mk1[c + 1], r);
+                    const bool l2 = needs_lut2(vol, g, tab, cfg, mk, mk1, c, r, x, y, k);
+                    const uint32_t info = owned_info_global(vol, g, x, y, k);
+                    const uint32_t nv = nvert_of(tab, cfg, l2) + __popc(info & 7u);
+                    const uint32_t nq = quad_count(info, cfg, x, y, k, g.cells, n_drop);
+                    atomicAdd(&S.rowv[r], nv | (nq << 16));
+                    ++n_act; n_l2 += l2;
                 }
             }
             __syncwarp();
-            const uint64_t *mk = S.mask[cur], *mk1 = S.mask[(k + 1) & 1];
+            if (y0 + lane < g.cells.y) {
+                const uint32_t t = S.rowv[lane];
+                seg_cnt[seg_index(g, k, y0 + lane, xs)] = make_uint2(t & 0xffffu, t >> 16);
+            }
+            S.rowv[lane] = 0;
+            __syncwarp();
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        n_act += __shfl_xor_sync(0xffffffffu, n_act, o);
+        n_l2 += __shfl_xor_sync(0xffffffffu, n_l2, o);
+        n_drop += __shfl_xor_sync(0xffffffffu, n_drop, o);
+    }
+    if (lane == 0) {
+        if (n_act) atomicAdd(&counters[0], (unsigned long long)n_act);
+        if (n_l2) atomicAdd(&counters[1], (unsigned long long)n_l2);
+        if (n_drop) atomicAdd(&counters[2], (unsigned long long)n_drop);
+    }
+}
+
+// Emit sweep: ranks active cells, writes vertices of plane k and quads of plane k-1.
+template <class T, bool VEC>
+__global__ void __launch_bounds__(32 * NWB) brick_emit(const T *__restrict__ vol, Geom g,
+                                                       const DeviceTables *__restrict__ tabp, EmitOut out,
+                                                       Spill *__restrict__ spill, uint32_t *ticket, uint32_t *err)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const DeviceTables &tab = stage_tables(tabp, reinterpret_cast<DeviceTables *>(smem_raw));
+    WarpSmem &S = reinterpret_cast<WarpSmem *>(smem_raw + sizeof(DeviceTables))[warp];
+    WarpMem M{&S, spill + (uint64_t)blockIdx.x * NWB + warp};
+
+    for (;;) {
+        const uint32_t b = claim_brick(ticket, lane);
+        if (b >= g.nbricks) break;
+        const uint32_t xs = b % g.nxs, yb = (b / g.nxs) % g.nyb, zb = b / (g.nxs * g.nyb);
+        const uint32_t x0 = xs * W, y0 = yb * ROWS, z0 = zb * g.zc;
+        const uint32_t z1 = min(z0 + g.zc, g.cells.z);
+        const uint64_t rowmask = ((1ull << min((uint32_t)HROWS, g.cells.y - y0)) - 1ull);
+
+        load_plane<T, VEC>(vol, g, x0, y0, z0, S.mask[z0 & 1], lane);
+        // planes z0..z1: plane z1 (when inside the volume) is ranked only so
+        // that the quads of plane z1-1 can reference it
+        for (uint32_t k = z0; k <= z1; ++k) {
+            const int cur = k & 1, prv = cur ^ 1;
+            const bool have_plane = k < g.cells.z;
             uint32_t L = 0;
             if (have_plane) {
-                // activity of the lane's 4 columns (and, lane 0, the halo column)
+                load_plane<T, VEC>(vol, g, x0, y0, k + 1, S.mask[(k + 1) & 1], lane);
+                for (uint32_t r = lane; r < HROWS; r += 32) {
+                    const uint32_t yy = y0 + r;
+                    uint2 own = make_uint2(0, 0), nxt = make_uint2(0, 0);
+                    if (yy < g.cells.y) {
+                        own = out.seg_off[seg_index(g, k, yy, xs)];
+                        if (xs + 1 < g.nxs) nxt = out.seg_off[seg_index(g, k, yy, xs + 1)];
+                    }
+                    S.segv[cur][r][0] = own.x; S.segv[cur][r][1] = nxt.x; S.segq[cur][r] = own.y;
+                }
+                __syncwarp();
+                const uint64_t *mk = S.mask[cur], *mk1 = S.mask[(k + 1) & 1];
                 uint64_t act[CPL];
 #pragma unroll
                 for (int j = 0; j < CPL; ++j) {
@@ -336,40 +416,34 @@ __global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vo
                     act[j] = (x0 + c < g.cells.x) ? active_rows(mk[c], mk[c + 1], mk1[c], mk1[c + 1]) & rowmask : 0ull;
                 }
                 uint64_t hact = 0;
-                if (MODE == EMIT && lane == 0 && x0 + W < g.cells.x)
-                    hact = active_rows(mk[W], mk[W + 1], mk1[W], mk1[W + 1]) & rowmask;
-                // per-row ballots: active lanes for each column-in-lane
-                for (uint32_t r = 0; r < nrows; ++r) {
+                if (lane == 0 && x0 + W < g.cells.x) hact = active_rows(mk[W], mk[W + 1], mk1[W], mk1[W + 1]) & rowmask;
+                // per-row ballots: the row's active cells in x order
+#pragma unroll 1
+                for (int r = 0; r < HROWS; ++r) {
 #pragma unroll
                     for (int j = 0; j < CPL; ++j) {
                         const uint32_t bb = __ballot_sync(0xffffffffu, (act[j] >> r) & 1ull);
-                        if (lane == (int)(r & 31)) S.ball[cur][r][j] = bb;
+                        if (lane == (r & 31)) S.ball[cur][r][j] = bb;
                     }
                 }
                 if (lane == 0) S.hact[cur] = hact;
                 __syncwarp();
-                // row starts: lane r counts row r; lane 0 also row 32
                 uint32_t cnt = 0, cnt32 = 0;
-                if ((uint32_t)lane < nrows) {
 #pragma unroll
-                    for (int j = 0; j < CPL; ++j) cnt += __popc(S.ball[cur][lane][j]);
-                    cnt += (uint32_t)((S.hact[cur] >> lane) & 1ull);
-                }
-                if (MODE == EMIT && lane == 0) {
+                for (int j = 0; j < CPL; ++j) cnt += __popc(S.ball[cur][lane][j]);
+                cnt += (uint32_t)((S.hact[cur] >> lane) & 1ull);
+                if (lane == 0) {
 #pragma unroll
                     for (int j = 0; j < CPL; ++j) cnt32 += __popc(S.ball[cur][32][j]);
                     cnt32 += (uint32_t)((S.hact[cur] >> 32) & 1ull);
                 }
                 const uint32_t inc = warp_incl_scan(cnt, lane);
                 const uint32_t tot32 = __shfl_sync(0xffffffffu, inc, 31);
+                cnt32 = __shfl_sync(0xffffffffu, cnt32, 0);
                 S.rowstart[cur][lane] = (uint16_t)(inc - cnt);
-                if (lane == 0) {
-                    S.rowstart[cur][32] = (uint16_t)tot32;
-                    S.rowstart[cur][33] = (uint16_t)(tot32 + cnt32);
-                }
-                L = MODE == EMIT ? tot32 + __shfl_sync(0xffffffffu, cnt32, 0) : tot32;
+                if (lane == 0) { S.rowstart[cur][32] = (uint16_t)tot32; S.rowstart[cur][33] = (uint16_t)(tot32 + cnt32); }
+                L = tot32 + cnt32;
                 __syncwarp();
-                // scatter list entries in output order
 #pragma unroll
                 for (int j = 0; j < CPL; ++j) {
                     uint64_t a = act[j];
@@ -386,74 +460,60 @@ __global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vo
                 }
                 __syncwarp();
             }
-            // per active cell: config, LUT choice, counts; ranks; vertices
+            // ranked active cells: counts, offsets inside their segment, vertices
+            const uint64_t *mk = S.mask[cur], *mk1 = S.mask[(k + 1) & 1];
             uint32_t run = 0;
             for (uint32_t base = 0; base < L; base += 32) {
                 const uint32_t i = base + lane;
                 const bool valid = i < L;
                 uint32_t packed = 0, cfg = 0, info = 0, nv = 0;
                 int r = 0, c = 0;
-                bool l2 = false;
+                bool l2 = false, own = false;
                 uint32_t x = 0, y = 0;
+                float v[8];
                 if (valid) {
                     const uint32_t e = M.lst(cur, i);
                     r = e >> 8; c = e & 0xff;
                     x = x0 + c; y = y0 + r;
-                    cfg = cfg_from_masks(mk[c], mk[c + 1], mk1[c], mk1[c + 1], r);
+                    own = r < ROWS && c < W;
+                    load_cell(vol, g, x, y, k, v);
+                    cfg = config_of(v, g.iso);
                     l2 = needs_lut2(vol, g, tab, cfg, mk, mk1, c, r, x, y, k);
-                    info = owned_info_global(vol, g, x, y, k);
+                    info = owned_edge_info(v, g.iso);
                     nv = nvert_of(tab, cfg, l2) + __popc(info & 7u);
-                    uint32_t nq = 0;
-                    if (r < ROWS && c < W) nq = quad_count(info, cfg, x, y, k, g.cells, n_drop);
+                    uint32_t nq = 0, dummy = 0;
+                    if (own) nq = quad_count(info, cfg, x, y, k, g.cells, dummy);
                     packed = nv | (nq << 16);
-                    if (MODE == COUNT) {
-                        atomicAdd(&S.rowv[r], nv);
-                        if (nq) atomicAdd(&S.rowq[r], nq);
-                        ++n_act; n_l2 += l2;
-                    }
                 }
-                if (MODE == EMIT) {
-                    const uint32_t inc = warp_incl_scan(packed, lane);
-                    const uint32_t ex = run + inc - packed;
-                    run += __shfl_sync(0xffffffffu, inc, 31);
-                    if (valid && i == S.rowstart[cur][r]) S.rowbase[r] = ex;
-                    __syncwarp();
-                    if (valid) {
-                        const uint32_t rb = S.rowbase[r];
-                        const uint32_t vrel = c == W ? 0u : (ex & 0xffffu) - (rb & 0xffffu);
-                        const uint32_t qrel = (ex >> 16) - (rb >> 16);
-                        M.ent(cur, i) = pack_cell(vrel, qrel, cfg, l2);
-                        M.info(cur, i) = (uint8_t)info;
-                        if (k < z1 && r < ROWS && c < W) {
-                            const uint64_t vb = (uint64_t)S.segv[cur][r][0] + vrel;
-                            if (vb + nv > out.vcap) {
-                                atomicOr(err, DEV_ERR_OVERFLOW);
-                            } else {
-                                float v[8];
-                                v[0] = sample_at(vol, g, x, y, k);         v[1] = sample_at(vol, g, x + 1, y, k);
-                                v[2] = sample_at(vol, g, x + 1, y + 1, k); v[3] = sample_at(vol, g, x, y + 1, k);
-                                v[4] = sample_at(vol, g, x, y, k + 1);     v[5] = sample_at(vol, g, x + 1, y, k + 1);
-                                v[6] = sample_at(vol, g, x + 1, y + 1, k + 1); v[7] = sample_at(vol, g, x, y + 1, k + 1);
-                                Geo geo;
-                                geo.x0 = g.coord[x]; geo.x1 = g.coord[x + 1];
-                                geo.y0 = g.coord[g.pts.x + y]; geo.y1 = g.coord[g.pts.x + y + 1];
-                                geo.z0 = g.coord[g.pts.x + g.pts.y + k]; geo.z1 = g.coord[g.pts.x + g.pts.y + k + 1];
-                                const uint32_t niso = nvert_of(tab, cfg, l2);
-                                dual_vertices(tab, v, geo, g.iso, cfg, l2, x, y, k, niso, out.verts + 3 * vb);
-                                owned_edge_vertices(v, geo, g.iso, info, out.verts + 3 * (vb + niso));
-                            }
+                const uint32_t incl = warp_incl_scan(packed, lane);
+                const uint32_t ex = run + incl - packed;
+                run += __shfl_sync(0xffffffffu, incl, 31);
+                if (valid && i == S.rowstart[cur][r]) S.rowbase[r] = ex;
+                __syncwarp();
+                if (valid) {
+                    const uint32_t rb = S.rowbase[r];
+                    const uint32_t vrel = c == W ? 0u : (ex & 0xffffu) - (rb & 0xffffu);
+                    const uint32_t qrel = (ex >> 16) - (rb >> 16);
+                    M.ent(cur, i) = pack_cell(vrel, qrel, cfg, l2);
+                    M.info(cur, i) = (uint8_t)info;
+                    if (own && k < z1) {
+                        const uint64_t vb = (uint64_t)S.segv[cur][r][0] + vrel;
+                        if (vb + nv > out.vcap) {
+                            atomicOr(err, DEV_ERR_OVERFLOW);
+                        } else {
+                            Geo geo;
+                            geo.x0 = g.coord[x]; geo.x1 = g.coord[x + 1];
+                            geo.y0 = g.coord[g.pts.x + y]; geo.y1 = g.coord[g.pts.x + y + 1];
+                            geo.z0 = g.coord[g.pts.x + g.pts.y + k]; geo.z1 = g.coord[g.pts.x + g.pts.y + k + 1];
+                            cell_vertices(tab, v, geo, g.iso, cfg, l2, nvert_of(tab, cfg, l2), info, x, y, k,
+                                          out.verts + 3 * vb);
                         }
                     }
-                    __syncwarp();
                 }
-            }
-            if (MODE == COUNT) {
                 __syncwarp();
-                if (have_plane && (uint32_t)lane < ROWS && y0 + lane < g.cells.y)
-                    seg_cnt[seg_index(g, k, y0 + lane, xs)] = make_uint2(S.rowv[lane], S.rowq[lane]);
             }
             // quads of own cells of plane k-1: their +z ring cells are in plane k
-            if (MODE == EMIT && k > z0) {
+            if (k > z0) {
                 const uint32_t kp = k - 1;
                 const uint32_t Lp = S.rowstart[prv][HROWS];
                 for (uint32_t i = lane; i < Lp; i += 32) {
@@ -495,19 +555,6 @@ __global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vo
                 }
             }
             __syncwarp();
-        }
-    }
-    if (MODE == COUNT) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            n_act += __shfl_xor_sync(0xffffffffu, n_act, o);
-            n_l2 += __shfl_xor_sync(0xffffffffu, n_l2, o);
-            n_drop += __shfl_xor_sync(0xffffffffu, n_drop, o);
-        }
-        if (lane == 0) {
-            if (n_act) atomicAdd(&counters[0], (unsigned long long)n_act);
-            if (n_l2) atomicAdd(&counters[1], (unsigned long long)n_l2);
-            if (n_drop) atomicAdd(&counters[2], (unsigned long long)n_drop);
         }
     }
 }
@@ -564,29 +611,17 @@ bool brick_supports(const ExtractArgs &a)
     return a.cells.x >= 1 && a.cells.y >= 1 && a.cells.z >= 1;
 }
 
-template <class T, bool VEC, int MODE>
-static dmc_status launch_sweep(Ctx *ctx, const T *vol, const brick::Geom &g, uint2 *seg_cnt, const brick::EmitOut &out,
-                               brick::Spill *spill, int grid, uint32_t *ticket, cudaStream_t st)
-{
-    using namespace brick;
-    const size_t smem = sizeof(WarpSmem) * NWB;
-    CUDA_TRY(cudaFuncSetAttribute(brick_sweep<T, VEC, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    brick_sweep<T, VEC, MODE><<<grid, 32 * NWB, smem, st>>>(vol, g, ctx->d_tab, seg_cnt, out, spill, ticket,
-                                                           ctx->d_ctl->counters, &ctx->d_ctl->err);
-    CUDA_TRY(cudaGetLastError());
-    return DMC_OK;
-}
+constexpr size_t kSweepSmem = sizeof(DeviceTables) + sizeof(brick::WarpSmem) * brick::NWB;
 
 template <class T, bool VEC>
 static int sweep_grid(Ctx *ctx)
 {
     using namespace brick;
-    const size_t smem = sizeof(WarpSmem) * NWB;
-    cudaFuncSetAttribute(brick_sweep<T, VEC, EMIT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(brick_sweep<T, VEC, COUNT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(brick_emit<T, VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSweepSmem);
+    cudaFuncSetAttribute(brick_count<T, VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSweepSmem);
     int b0 = 0, b1 = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, brick_sweep<T, VEC, EMIT>, 32 * NWB, smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, brick_sweep<T, VEC, COUNT>, 32 * NWB, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, brick_emit<T, VEC>, 32 * NWB, kSweepSmem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, brick_count<T, VEC>, 32 * NWB, kSweepSmem);
     int b = b0 < b1 ? b0 : b1;
     if (b < 1) b = 1;
     return b * ctx->num_sms;
@@ -609,7 +644,11 @@ static dmc_status brick_run_v(Ctx *ctx, const T *vol, const ExtractArgs &a, cuda
     }
     g.nxs = (a.cells.x + W - 1) / W;
     g.nyb = (a.cells.y + ROWS - 1) / ROWS;
-    g.zc = 16;
+    const int grid = sweep_grid<T, VEC>(ctx);
+    // planes per brick: long sweeps amortise the z halo, but keep at least
+    // three bricks per warp so that the persistent warps stay busy
+    g.zc = 32;
+    while (g.zc > 4 && (uint64_t)g.nxs * g.nyb * ((a.cells.z + g.zc - 1) / g.zc) < 3ull * grid * NWB) g.zc >>= 1;
     g.nzb = (a.cells.z + g.zc - 1) / g.zc;
     g.nbricks = (uint64_t)g.nxs * g.nyb * g.nzb;
     if (g.nbricks >= 0xF0000000ull) return DMC_ERR_UNSUPPORTED;
@@ -617,7 +656,6 @@ static dmc_status brick_run_v(Ctx *ctx, const T *vol, const ExtractArgs &a, cuda
     const uint64_t n_tiles64 = (nseg + SCAN_TILE - 1) / SCAN_TILE;
     if (n_tiles64 >= (1ull << 31)) return DMC_ERR_UNSUPPORTED;
     const uint32_t n_tiles = (uint32_t)n_tiles64;
-    const int grid = sweep_grid<T, VEC>(ctx);
     const uint64_t n_coord = (uint64_t)a.pts.x + a.pts.y + a.pts.z;
 
     size_t off = 0;
@@ -640,9 +678,9 @@ static dmc_status brick_run_v(Ctx *ctx, const T *vol, const ExtractArgs &a, cuda
     CUDA_TRY(cudaMemsetAsync(tickets, 0, 256, st));
     CUDA_TRY(cudaMemsetAsync(ctx->d_ctl, 0, sizeof(DevCtl), st));
     coord_table<<<(unsigned)((n_coord + 255) / 256), 256, 0, st>>>(coord, a.pts, a.cells, a.rng, a.mn);
-    EmitOut none{};
-    s = launch_sweep<T, VEC, COUNT>(ctx, vol, g, seg_cnt, none, spill, grid, &tickets[0], st);
-    if (s != DMC_OK) return s;
+    brick_count<T, VEC><<<grid, 32 * NWB, kSweepSmem, st>>>(vol, g, ctx->d_tab, seg_cnt, &tickets[0],
+                                                             ctx->d_ctl->counters);
+    CUDA_TRY(cudaGetLastError());
     ScanCtl ctl;
     ctl.tiles = tiles; ctl.ticket = &ctx->d_ctl->ticket; ctl.err = &ctx->d_ctl->err;
     ctl.totals = ctx->d_ctl->totals; ctl.n_tiles = n_tiles;
@@ -661,7 +699,9 @@ static dmc_status brick_run_v(Ctx *ctx, const T *vol, const ExtractArgs &a, cuda
     if (V > a.vcap || Q > a.qcap) return DMC_ERR_OUTPUT_OVERFLOW;
     EmitOut eo;
     eo.seg_off = seg_off; eo.verts = a.verts; eo.vcap = a.vcap; eo.quads = a.quads; eo.qcap = a.qcap; eo.tris = a.tris;
-    return launch_sweep<T, VEC, EMIT>(ctx, vol, g, nullptr, eo, spill, grid, &tickets[1], st);
+    brick_emit<T, VEC><<<grid, 32 * NWB, kSweepSmem, st>>>(vol, g, ctx->d_tab, eo, spill, &tickets[1], &ctx->d_ctl->err);
+    CUDA_TRY(cudaGetLastError());
+    return DMC_OK;
 }
 
 template <class T>

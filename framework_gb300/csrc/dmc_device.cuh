@@ -23,6 +23,7 @@ struct DeviceTables {
     uint8_t nvert[2][256];           // dual vertices per config
     uint8_t amb_face[256];           // ambiguous face of a 2B/3B config, 0xff otherwise
     uint8_t face_dir[8];             // neighbour direction of a face: 0 +x,1 -x,2 +y,3 -y,4 +z,5 -z
+    uint16_t crossed[256];           // bit e: edge e changes sign under this config
 };
 
 // Owner of each cell edge: offset (0 or -1 per axis) to the cell that owns it
@@ -212,6 +213,112 @@ __device__ __forceinline__ void owned_edge_vertices(const float v[8], const Geo 
     if (info & 1u) { float3 c = edge_crossing(6, v, g, iso);  out[3*n] = c.x; out[3*n+1] = c.y; out[3*n+2] = c.z; ++n; }
     if (info & 2u) { float3 c = edge_crossing(9, v, g, iso);  out[3*n] = c.x; out[3*n+1] = c.y; out[3*n+2] = c.z; ++n; }
     if (info & 4u) { float3 c = edge_crossing(10, v, g, iso); out[3*n] = c.x; out[3*n+1] = c.y; out[3*n+2] = c.z; ++n; }
+}
+
+// Corners of each edge in the order its owner evaluates the crossing
+// (owner edge 6: low z to high z; 9: low y to high y; 10: high x to low x),
+// 4 bits per edge, edge 0 in the lowest nibble.
+constexpr unsigned long long kEdgeFrom = 0x465532100211ull;
+constexpr unsigned long long kEdgeTo = 0x776476543320ull;
+
+__device__ __forceinline__ float pick8(const float v[8], int c)
+{
+    const float s01 = (c & 1) ? v[1] : v[0], s23 = (c & 1) ? v[3] : v[2];
+    const float s45 = (c & 1) ? v[5] : v[4], s67 = (c & 1) ? v[7] : v[6];
+    const float t0 = (c & 2) ? s23 : s01, t1 = (c & 2) ? s67 : s45;
+    return (c & 4) ? t1 : t0;
+}
+
+// edge_crossing for a run-time edge index, without a per-edge branch.
+__device__ __forceinline__ float3 crossing_any(int e, const float v[8], const Geo &g, float iso)
+{
+    const int a = (int)((kEdgeFrom >> (4 * e)) & 15ull), b = (int)((kEdgeTo >> (4 * e)) & 15ull);
+    // corner c sits at x = (c ^ c >> 1) & 1, y = c >> 1 & 1, z = c >> 2
+    const float ax = ((a ^ (a >> 1)) & 1) ? g.x1 : g.x0, ay = ((a >> 1) & 1) ? g.y1 : g.y0, az = (a >> 2) ? g.z1 : g.z0;
+    const float bx = ((b ^ (b >> 1)) & 1) ? g.x1 : g.x0, by = ((b >> 1) & 1) ? g.y1 : g.y0, bz = (b >> 2) ? g.z1 : g.z0;
+    return lerp3(ax, ay, az, bx, by, bz, pick8(v, a), pick8(v, b), iso);
+}
+
+__device__ __forceinline__ float3 add3(float3 a, float3 b)
+{
+    return make_float3(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z));
+}
+
+// acc / n as the reference computes it (a true IEEE division); division by a
+// power of two is the exact multiplication by its reciprocal, so it is used
+// for n = 1, 2, 4, 8 (same rounded result).
+__device__ __forceinline__ float3 div3(float3 a, uint32_t n)
+{
+    if ((n & (n - 1)) == 0) {
+        const float r = n == 1 ? 1.f : (n == 2 ? 0.5f : (n == 4 ? 0.25f : 0.125f));
+        if (n <= 8) return make_float3(__fmul_rn(a.x, r), __fmul_rn(a.y, r), __fmul_rn(a.z, r));
+    }
+    const float d = __uint2float_rn(n);
+    return make_float3(__fdiv_rn(a.x, d), __fdiv_rn(a.y, d), __fdiv_rn(a.z, d));
+}
+
+__device__ __forceinline__ void store3(float *p, float3 c) { p[0] = c.x; p[1] = c.y; p[2] = c.z; }
+
+// All vertices of an active cell, written to out: the niso dual vertices,
+// then the crossings of its own edges 6, 9, 10 flagged in info (bits 0-2).
+// Same values as dual_vertices + owned_edge_vertices, but only the crossed
+// edges are evaluated, each once.
+__device__ __forceinline__ void cell_vertices(const DeviceTables &tab, const float v[8], const Geo &g, float iso,
+                                              uint32_t cfg, bool lut2, uint32_t niso, uint32_t info,
+                                              uint32_t x, uint32_t y, uint32_t z, float *out)
+{
+    const uint32_t cm = tab.crossed[cfg];
+    uint32_t om = cm;                      // crossed edges whose owner lies inside the volume
+    if (x == 0) om &= ~0x898u;             // edges 3, 4, 7, 11 are owned at -x
+    if (y == 0) om &= ~0x131u;             // edges 0, 4, 5, 8 are owned at -y
+    if (z == 0) om &= ~0x00fu;             // edges 0, 1, 2, 3 are owned at -z
+    float3 c6 = make_float3(0.f, 0.f, 0.f), c9 = c6, c10 = c6;
+    uint32_t have = 0;                     // bit 0/1/2: c6/c9/c10 computed
+    if (niso == 1) {
+        uint32_t mm = om ? om : cm;
+        float3 acc = make_float3(0.f, 0.f, 0.f);
+        uint32_t n = 0;
+        while (mm) {
+            const int e = __ffs(mm) - 1;
+            mm &= mm - 1;
+            const float3 c = crossing_any(e, v, g, iso);
+            if (e == 6) { c6 = c; have |= 1u; } else if (e == 9) { c9 = c; have |= 2u; } else if (e == 10) { c10 = c; have |= 4u; }
+            acc = n ? add3(acc, c) : c;
+            ++n;
+        }
+        store3(out, div3(acc, n));
+    } else {
+        float3 acc[4];
+        uint32_t cnt[4] = {0, 0, 0, 0};
+        uint32_t mm = om;
+        while (mm) {
+            const int e = __ffs(mm) - 1;
+            mm &= mm - 1;
+            const float3 c = crossing_any(e, v, g, iso);
+            if (e == 6) { c6 = c; have |= 1u; } else if (e == 9) { c9 = c; have |= 2u; } else if (e == 10) { c10 = c; have |= 4u; }
+            const uint32_t m = lut_m(tab, cfg, lut2, e);
+            acc[m] = cnt[m] ? add3(acc[m], c) : c;
+            cnt[m]++;
+        }
+        for (uint32_t m = 0; m < niso; ++m) {
+            if (cnt[m] == 0) {
+                uint32_t fm = cm;
+                while (fm) {
+                    const int e = __ffs(fm) - 1;
+                    fm &= fm - 1;
+                    if (lut_m(tab, cfg, lut2, e) != m) continue;
+                    const float3 c = crossing_any(e, v, g, iso);
+                    acc[m] = cnt[m] ? add3(acc[m], c) : c;
+                    cnt[m]++;
+                }
+            }
+            store3(out + 3 * m, div3(acc[m], cnt[m]));
+        }
+    }
+    uint32_t k = niso;
+    if (info & 1u) { store3(out + 3 * k, (have & 1u) ? c6 : crossing_any(6, v, g, iso)); ++k; }
+    if (info & 2u) { store3(out + 3 * k, (have & 2u) ? c9 : crossing_any(9, v, g, iso)); ++k; }
+    if (info & 4u) { store3(out + 3 * k, (have & 4u) ? c10 : crossing_any(10, v, g, iso)); ++k; }
 }
 
 // Device-side error codes (written with atomicOr to ctx error word).
