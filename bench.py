@@ -1,0 +1,318 @@
+#!/usr/bin/env python3
+"""Benchmark: Dual Marching Cubes throughput on one GB300.
+
+Default workload: 1024^3 uint16 lattice value noise (4 octaves, base period
+128 voxels, persistence 0.5, quantised to 0..65535), isovalue 32768 -- the
+reference's plain-extractor configuration with the HBM-roofline target.
+Synthetic data generated on the device from a fixed seed.
+
+One step = one full extraction (count sweep, segment scan, emit sweep) of the
+resident volume into preallocated device buffers.  The input (2 GiB) is
+larger than L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload noise1024|blobs512|sphere64]
+
+Prints one JSON line (rank 0).  --impl reference times the reference
+algorithm's CPU restatement (the reference itself is CUDA-only, Fermi-era and
+has no CPU path) with all host threads on a bounded z-slab sample.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (dims, dtype, iso, description)
+    "noise1024": ((1024, 1024, 1024), "uint16", 32768.0,
+                  "1024^3 uint16 4-octave lattice value noise (period 128, persistence 0.5), iso 32768"),
+    "blobs512": ((512, 512, 512), "float32", 0.5,
+                 "512^3 float32 sum of 32 Gaussian blobs (sigma 8-32, amplitude 0.5-1.5), iso 0.5"),
+    "sphere64": ((64, 64, 64), "float32", 0.0,
+                 "64^3 float32 sphere SDF radius 20 + uniform noise 0.01, iso 0"),
+}
+
+
+def make_volume(name, device, zrange=None):
+    import torch
+    from framework_gb300 import fields
+    dims, dtype, iso, _ = WORKLOADS[name]
+    if name == "noise1024":
+        vol = fields.value_noise_u16(dims, device=device)
+    elif name == "blobs512":
+        vol = fields.gaussian_blobs(dims, device=device)
+    else:
+        vol = fields.sphere_sdf(64, radius=20.0, noise=0.01, seed=1).to(device)
+    if device != "cpu":
+        torch.cuda.synchronize()
+    return vol, iso
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append(dict(sm=float(parts[1]), smax=float(parts[2]), power=float(parts[3]),
+                                 hw=parts[5], hwt=parts[6], swt=parts[7], swpc=parts[8]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        reasons = set()
+        for r in rows:
+            for key, name in (("hw", "hw_slowdown"), ("hwt", "hw_thermal_slowdown"),
+                              ("swt", "sw_thermal_slowdown"), ("swpc", "sw_power_cap")):
+                if r[key].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(r["sm"] for r in rows), "sm_max_mhz": max(r["smax"] for r in rows),
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(workload):
+    """DRAM bytes per launch of the emit kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p))
+    return d.get(workload)
+
+
+def cpu_oracle_sample(vol_host, iso, target_s=10.0):
+    """Time the CPU restatement with all host threads on a z-slab sample of
+    the workload, sized for ~target_s of work.  Returns GVoxels/s, cores, sample text."""
+    import numpy as np
+    import oracle
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    nz = vol_host.shape[0]
+    planes = min(nz, 34)
+    t0 = time.perf_counter()
+    oracle.extract(np.ascontiguousarray(vol_host[:planes]), iso=iso)
+    dt = time.perf_counter() - t0
+    want = int(planes * target_s / max(dt, 1e-3))
+    planes = max(planes, min(nz, want))
+    sample = np.ascontiguousarray(vol_host[:planes])
+    t0 = time.perf_counter()
+    oracle.extract(sample, iso=iso)
+    dt = time.perf_counter() - t0
+    return sample.size / dt / 1e9, cores, "z-slab of %d x %d x %d points (%.1f s)" % (
+        sample.shape[2], sample.shape[1], sample.shape[0], dt)
+
+
+def run_reference(args, rank):
+    """CPU restatement of the reference algorithm, all host threads."""
+    import numpy as np
+    import torch
+    if rank != 0:
+        return
+    dims, dtype, iso, desc = WORKLOADS[args.workload]
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    vol, iso = make_volume(args.workload, dev)
+    from framework_gb300 import fields
+    host = fields.as_u16_numpy(vol) if dtype == "uint16" else vol.cpu().numpy()
+    import oracle
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    # bounded sample per step: a z-slab sized for ~10 s per step in total
+    planes = min(host.shape[0], 34)
+    t0 = time.perf_counter()
+    oracle.extract(np.ascontiguousarray(host[:planes]), iso=iso)
+    dt = time.perf_counter() - t0
+    budget = 120.0 / max(1, args.steps + args.warmup)
+    planes = max(2, min(host.shape[0], int(planes * budget / max(dt, 1e-3))))
+    sample = np.ascontiguousarray(host[:planes])
+    for _ in range(args.warmup):
+        oracle.extract(sample, iso=iso)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.extract(sample, iso=iso)
+        times.append(time.perf_counter() - t0)
+    t = sum(times)
+    value = sample.size * args.steps / t / 1e9
+    line = {
+        "impl": "reference", "metric": "GVoxels/s", "value": round(value, 4), "unit": "GVoxels/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * t / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u16" if dtype == "uint16" else "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "desc": desc, "sample_points": int(sample.size)},
+        "cpu_baseline": {"value": round(value, 4), "unit": "GVoxels/s", "cores": cores, "kind": "port",
+                         "sample": "z-slab %dx%dx%d of the workload" % (sample.shape[2], sample.shape[1], sample.shape[0])},
+        "e2e": {"value": round(value, 4), "unit": "GVoxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="noise1024", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    if args.impl == "reference":
+        run_reference(args, rank)
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    torch.cuda.set_device(local)
+    import framework_gb300 as fg
+    from framework_gb300 import fields
+    dims, dtype, iso, desc = WORKLOADS[args.workload]
+    vol, iso = make_volume(args.workload, "cuda")
+    N = vol.numel()
+    ex = fg.Extractor(local, algo="brick")
+    try:
+        ex.extract_device(vol, iso=iso)
+        raise RuntimeError("expected a sizing overflow")
+    except fg.DMCError as e:
+        V, Q = e.counts
+    vbuf = torch.empty((max(V, 1), 3), device="cuda")
+    qbuf = torch.empty((max(Q, 1), 4), dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    for _ in range(args.warmup):
+        ex.extract_device(vol, iso=iso, vertices=vbuf, quads=qbuf)
+    clocks = ClockSampler(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    emit_ms, count_ms, scan_ms = [], [], []
+    ev0.record(stream)
+    for _ in range(args.steps):
+        ex.extract_device(vol, iso=iso, vertices=vbuf, quads=qbuf)
+        st = ex.stats()
+        emit_ms.append(st["emit_ms"]); count_ms.append(st["count_ms"]); scan_ms.append(st["scan_ms"])
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    st = ex.stats()
+
+    # end to end through the host API: pinned host volume in, host mesh out
+    host_t = torch.empty(vol.shape, dtype=vol.dtype, pin_memory=True)
+    host_t.copy_(vol)
+    host = fields.as_u16_numpy(host_t) if dtype == "uint16" else host_t.numpy()
+    e2e_steps = max(1, min(args.e2e_steps, args.steps))
+    ex.run(host, iso=iso, triangles=True)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        m = ex.run(host, iso=iso, triangles=True)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    assert len(m.vertices) == V and len(m.quads) == Q
+
+    line = None
+    if rank == 0:
+        hbm, peak_kind = peaks()
+        elem = 2 if dtype == "uint16" else 4
+        alg_bytes = elem * N + 12 * V + 16 * Q
+        emit_avg = sum(emit_ms) / len(emit_ms)
+        achieved = alg_bytes / (emit_avg * 1e-3) / 1e9
+        value = N * world / (ms * 1e-3) / 1e9
+        cpu = None
+        if not args.no_cpu_baseline:
+            v, cores, sample = cpu_oracle_sample(host, iso)
+            cpu = {"value": round(v, 4), "unit": "GVoxels/s", "cores": cores, "kind": "port", "sample": sample}
+        line = {
+            "metric": "GVoxels/s", "value": round(value, 3), "unit": "GVoxels/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u16" if dtype == "uint16" else "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "desc": desc, "dims": list(dims), "iso": iso,
+                       "vertices": V, "quads": Q, "active_cells": st["n_active_cells"],
+                       "algo": "brick", "l2": "input larger than L2 (no flush needed)",
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "kernel_ms": {"count": round(sum(count_ms) / len(count_ms), 4),
+                                     "scan": round(sum(scan_ms) / len(scan_ms), 4),
+                                     "emit": round(emit_avg, 4)}},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                         "frac": round(achieved / hbm, 4), "traffic": profile_traffic(args.workload),
+                         "kernel": "brick_emit", "peak_kind": peak_kind,
+                         "algorithmic_bytes": alg_bytes,
+                         "pipeline_frac": round(alg_bytes / (ms * 1e-3) / 1e9 / hbm, 4)},
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(N / e2e_s / 1e9, 3), "unit": "GVoxels/s", "h2d_bytes_per_step": elem * N,
+                    "d2h_bytes_per_step": 12 * V + 16 * Q + 24 * Q, "steps": e2e_steps},
+            "gpu_launches": 4 * args.steps,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    ex.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -56,7 +56,8 @@ class _Mesh(ctypes.Structure):
 class Stats(ctypes.Structure):
     _fields_ = [("n_vertices", ctypes.c_uint64), ("n_quads", ctypes.c_uint64),
                 ("n_active_cells", ctypes.c_uint64), ("n_lut2_cells", ctypes.c_uint64),
-                ("n_dropped_quads", ctypes.c_uint64), ("device_ms", ctypes.c_float), ("algo", ctypes.c_int)]
+                ("n_dropped_quads", ctypes.c_uint64), ("device_ms", ctypes.c_float), ("algo", ctypes.c_int),
+                ("count_ms", ctypes.c_float), ("scan_ms", ctypes.c_float), ("emit_ms", ctypes.c_float)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -119,6 +119,12 @@ static dmc_status finish(dmc_ctx *ctx, cudaStream_t st)
     float ms = 0.f;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
     c->stats.device_ms = ms;
+    if (c->evk_used) {
+        cudaEventElapsedTime(&c->stats.count_ms, c->evk[0], c->evk[1]);
+        cudaEventElapsedTime(&c->stats.scan_ms, c->evk[1], c->evk[2]);
+        cudaEventElapsedTime(&c->stats.emit_ms, c->evk[3], c->evk[4]);
+        c->evk_used = false;
+    }
     uint32_t err = c->h_ctl->err;
     if (err & DEV_ERR_TIMEOUT) return DMC_ERR_TIMEOUT;
     if (err & DEV_ERR_OVERFLOW) return DMC_ERR_OUTPUT_OVERFLOW;
@@ -163,6 +169,9 @@ dmc_status dmc_create(dmc_ctx **out, int device)
         cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
         if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { s = DMC_ERR_CUDA; break; }
         if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) { s = DMC_ERR_CUDA; break; }
+        for (int i = 0; i < 5; ++i)
+            if (cudaEventCreate(&c->evk[i]) != cudaSuccess) { s = DMC_ERR_CUDA; break; }
+        if (s != DMC_OK) break;
         if (cudaMalloc(&c->d_ctl, sizeof(DevCtl)) != cudaSuccess) { s = DMC_ERR_OOM; break; }
         if (cudaMallocHost(&c->h_ctl, sizeof(DevCtl)) != cudaSuccess) { s = DMC_ERR_OOM; break; }
         s = upload_tables(c);
@@ -183,6 +192,8 @@ dmc_status dmc_destroy(dmc_ctx *ctx)
     if (c->h_ctl) cudaFreeHost(c->h_ctl);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    for (int i = 0; i < 5; ++i)
+        if (c->evk[i]) cudaEventDestroy(c->evk[i]);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete ctx;
     return DMC_OK;

@@ -678,14 +678,18 @@ static dmc_status brick_run_v(Ctx *ctx, const T *vol, const ExtractArgs &a, cuda
     CUDA_TRY(cudaMemsetAsync(tickets, 0, 256, st));
     CUDA_TRY(cudaMemsetAsync(ctx->d_ctl, 0, sizeof(DevCtl), st));
     coord_table<<<(unsigned)((n_coord + 255) / 256), 256, 0, st>>>(coord, a.pts, a.cells, a.rng, a.mn);
+    ctx->evk_used = false;
+    CUDA_TRY(cudaEventRecord(ctx->evk[0], st));
     brick_count<T, VEC><<<grid, 32 * NWB, kSweepSmem, st>>>(vol, g, ctx->d_tab, seg_cnt, &tickets[0],
                                                              ctx->d_ctl->counters);
     CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaEventRecord(ctx->evk[1], st));
     ScanCtl ctl;
     ctl.tiles = tiles; ctl.ticket = &ctx->d_ctl->ticket; ctl.err = &ctx->d_ctl->err;
     ctl.totals = ctx->d_ctl->totals; ctl.n_tiles = n_tiles;
     seg_scan<<<n_tiles, SCAN_NT, 0, st>>>(seg_cnt, nseg, ctl, seg_off);
     CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaEventRecord(ctx->evk[2], st));
     CUDA_TRY(cudaMemcpyAsync(ctx->h_ctl, ctx->d_ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
     if (ctx->h_ctl->err & DEV_ERR_TIMEOUT) return DMC_ERR_TIMEOUT;
@@ -699,8 +703,11 @@ static dmc_status brick_run_v(Ctx *ctx, const T *vol, const ExtractArgs &a, cuda
     if (V > a.vcap || Q > a.qcap) return DMC_ERR_OUTPUT_OVERFLOW;
     EmitOut eo;
     eo.seg_off = seg_off; eo.verts = a.verts; eo.vcap = a.vcap; eo.quads = a.quads; eo.qcap = a.qcap; eo.tris = a.tris;
+    CUDA_TRY(cudaEventRecord(ctx->evk[3], st));
     brick_emit<T, VEC><<<grid, 32 * NWB, kSweepSmem, st>>>(vol, g, ctx->d_tab, eo, spill, &tickets[1], &ctx->d_ctl->err);
     CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaEventRecord(ctx->evk[4], st));
+    ctx->evk_used = true;
     return DMC_OK;
 }
 

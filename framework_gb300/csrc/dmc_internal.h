@@ -33,6 +33,8 @@ struct Ctx {
     int num_sms = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t evk[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};   // per-kernel timing (brick path)
+    bool evk_used = false;
     void *scratch = nullptr;           // grow-only device scratch
     size_t scratch_bytes = 0;
     DevCtl *d_ctl = nullptr;

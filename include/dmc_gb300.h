@@ -80,6 +80,9 @@ typedef struct {
     uint64_t n_dropped_quads;   /* quads the reference would index with NO_VERTEX */
     float device_ms;            /* device time of the last call (events) */
     int algo;                   /* dmc_algo actually used */
+    float count_ms;             /* brick path: count sweep, segment scan, emit sweep */
+    float scan_ms;
+    float emit_ms;
 } dmc_stats;
 
 /* Library version string. */
