@@ -46,12 +46,18 @@ struct Geom {
     uint64_t nbricks;
     float iso;
     uint32_t iso_u16;      // uint16 samples: v < iso  <=>  v < iso_u16 (65536: always)
+    uint32_t isole_u16;    // uint16 samples: v <= iso <=>  v < isole_u16
     float3 mn, rng;
     const float *coord;    // point coordinates: x[0..cx], y[0..cy], z[0..cz]
 };
 
+struct PlaneMasks {
+    uint64_t lt[W + 2];                // bit r: sample (x0+c, y0+r) < iso
+    uint64_t le[W + 2];                // bit r: sample <= iso
+};
+
 struct WarpSmem {
-    uint64_t mask[2][W + 2];           // column masks of point planes (by parity)
+    PlaneMasks mask[2];                // point planes by parity
     uint32_t ball[2][HROWS][CPL];      // per row, per column-in-lane: active lanes
     uint64_t hact[2];                  // halo column activity (bit = row)
     uint16_t rowstart[2][HROWS + 1];   // first list entry of each row
@@ -92,13 +98,19 @@ __device__ __forceinline__ float sample_at(const T *vol, const Geom &g, uint32_t
 __device__ __forceinline__ bool below_u16(uint32_t v, uint32_t thr) { return v < thr; }
 
 // Column masks of point plane p: bit r of column c = sample (x0+c, y0+r, p)
-// below the isovalue, rows 0..33, columns 0..W+1.  Samples outside the volume
-// read as 0; cells that touch them are never treated as active.
+// below (lt) / at or below (le) the isovalue, rows 0..33, columns 0..W+1.
+// Samples outside the volume read as 0; cells touching them are never active.
+__device__ __forceinline__ uint32_t spread16(uint32_t a, uint32_t b, bool upper)
+{
+    // a holds rows 0..15 of two columns (low/high halfword), b rows 16..31
+    return upper ? ((a >> 16) | (b & 0xffff0000u)) : ((a & 0xffffu) | (b << 16));
+}
+
 template <class T, bool VEC>
 __device__ __forceinline__ void load_plane(const T *vol, const Geom &g, uint32_t x0, uint32_t y0, uint32_t p,
-                                           uint64_t *m, int lane)
+                                           PlaneMasks &m, int lane)
 {
-    uint32_t lo[CPL] = {0, 0, 0, 0}, hi[CPL] = {0, 0, 0, 0};
+    uint64_t lt[CPL] = {0, 0, 0, 0}, le[CPL] = {0, 0, 0, 0};
     const uint32_t xb = x0 + CPL * lane;
     const bool pz = p < g.pts.z;
     if (pz && xb < g.pts.x) {
@@ -107,25 +119,60 @@ __device__ __forceinline__ void load_plane(const T *vol, const Geom &g, uint32_t
         const uint32_t nrow = min(34u, g.pts.y - y0);
         if (VEC && nrow == 34 && xb + CPL <= g.pts.x) {
             if constexpr (sizeof(T) == 4) {
+                uint32_t a[CPL] = {0, 0, 0, 0}, b[CPL] = {0, 0, 0, 0}, ha[CPL] = {0, 0, 0, 0}, hb[CPL] = {0, 0, 0, 0};
+                const float4 *q = reinterpret_cast<const float4 *>(base);
+                const uint64_t step = sx / 4;
 #pragma unroll
                 for (int r = 0; r < 34; ++r) {
-                    const float4 v = __ldg(reinterpret_cast<const float4 *>(base + (uint64_t)r * sx));
-                    const uint32_t b0 = v.x < g.iso, b1 = v.y < g.iso, b2 = v.z < g.iso, b3 = v.w < g.iso;
-                    if (r < 32) { lo[0] |= b0 << r; lo[1] |= b1 << r; lo[2] |= b2 << r; lo[3] |= b3 << r; }
-                    else { hi[0] |= b0 << (r - 32); hi[1] |= b1 << (r - 32); hi[2] |= b2 << (r - 32); hi[3] |= b3 << (r - 32); }
+                    const float4 v = __ldg(q);
+                    q += step;
+                    const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                    for (int j = 0; j < CPL; ++j) {
+                        if (r < 32) {
+                            if (vv[j] < g.iso) a[j] |= 1u << r;
+                            if (vv[j] <= g.iso) b[j] |= 1u << r;
+                        } else {
+                            if (vv[j] < g.iso) ha[j] |= 1u << (r - 32);
+                            if (vv[j] <= g.iso) hb[j] |= 1u << (r - 32);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < CPL; ++j) {
+                    lt[j] = (uint64_t)a[j] | ((uint64_t)ha[j] << 32);
+                    le[j] = (uint64_t)b[j] | ((uint64_t)hb[j] << 32);
                 }
             } else {
-                const uint32_t thr2 = g.iso_u16 | (g.iso_u16 << 16);
-                const bool all = g.iso_u16 > 0xffffu;
+                // two samples per 32-bit word: per-halfword compares; bit r of
+                // rows 0..15 of columns (0,1) accumulate in one word, (2,3) in another
+                const bool all_lt = g.iso_u16 > 0xffffu, all_le = g.isole_u16 > 0xffffu;
+                const uint32_t tl = all_lt ? 0u : (g.iso_u16 | (g.iso_u16 << 16));
+                const uint32_t te = all_le ? 0u : (g.isole_u16 | (g.isole_u16 << 16));
+                uint32_t l01a = 0, l23a = 0, l01b = 0, l23b = 0, l01h = 0, l23h = 0;
+                uint32_t e01a = 0, e23a = 0, e01b = 0, e23b = 0, e01h = 0, e23h = 0;
+                const uint2 *q = reinterpret_cast<const uint2 *>(base);
+                const uint64_t step = sx / 4;
 #pragma unroll
                 for (int r = 0; r < 34; ++r) {
-                    const uint2 w = __ldg(reinterpret_cast<const uint2 *>(base + (uint64_t)r * sx));
-                    const uint32_t c0 = all ? 0xffffffffu : __vcmpltu2(w.x, thr2);
-                    const uint32_t c1 = all ? 0xffffffffu : __vcmpltu2(w.y, thr2);
-                    const uint32_t b0 = c0 & 1u, b1 = (c0 >> 16) & 1u, b2 = c1 & 1u, b3 = (c1 >> 16) & 1u;
-                    if (r < 32) { lo[0] |= b0 << r; lo[1] |= b1 << r; lo[2] |= b2 << r; lo[3] |= b3 << r; }
-                    else { hi[0] |= b0 << (r - 32); hi[1] |= b1 << (r - 32); hi[2] |= b2 << (r - 32); hi[3] |= b3 << (r - 32); }
+                    const uint2 w = __ldg(q);
+                    q += step;
+                    const uint32_t c0 = (all_lt ? 0xffffffffu : __vcmpltu2(w.x, tl)) & 0x00010001u;
+                    const uint32_t c1 = (all_lt ? 0xffffffffu : __vcmpltu2(w.y, tl)) & 0x00010001u;
+                    const uint32_t d0 = (all_le ? 0xffffffffu : __vcmpltu2(w.x, te)) & 0x00010001u;
+                    const uint32_t d1 = (all_le ? 0xffffffffu : __vcmpltu2(w.y, te)) & 0x00010001u;
+                    if (r < 16) { l01a |= c0 << r; l23a |= c1 << r; e01a |= d0 << r; e23a |= d1 << r; }
+                    else if (r < 32) { l01b |= c0 << (r - 16); l23b |= c1 << (r - 16); e01b |= d0 << (r - 16); e23b |= d1 << (r - 16); }
+                    else { l01h |= c0 << (r - 32); l23h |= c1 << (r - 32); e01h |= d0 << (r - 32); e23h |= d1 << (r - 32); }
                 }
+                lt[0] = spread16(l01a, l01b, false) | ((uint64_t)(l01h & 3u) << 32);
+                lt[1] = spread16(l01a, l01b, true) | ((uint64_t)((l01h >> 16) & 3u) << 32);
+                lt[2] = spread16(l23a, l23b, false) | ((uint64_t)(l23h & 3u) << 32);
+                lt[3] = spread16(l23a, l23b, true) | ((uint64_t)((l23h >> 16) & 3u) << 32);
+                le[0] = spread16(e01a, e01b, false) | ((uint64_t)(e01h & 3u) << 32);
+                le[1] = spread16(e01a, e01b, true) | ((uint64_t)((e01h >> 16) & 3u) << 32);
+                le[2] = spread16(e23a, e23b, false) | ((uint64_t)(e23h & 3u) << 32);
+                le[3] = spread16(e23a, e23b, true) | ((uint64_t)((e23h >> 16) & 3u) << 32);
             }
         } else {
             for (uint32_t r = 0; r < nrow; ++r) {
@@ -133,24 +180,30 @@ __device__ __forceinline__ void load_plane(const T *vol, const Geom &g, uint32_t
                 for (int j = 0; j < CPL; ++j) {
                     if (xb + j >= g.pts.x) continue;
                     const float v = load_sample(base, (uint64_t)r * sx + j);
-                    const uint32_t b = v < g.iso;
-                    if (r < 32) lo[j] |= b << r; else hi[j] |= b << (r - 32);
+                    if (v < g.iso) lt[j] |= 1ull << r;
+                    if (v <= g.iso) le[j] |= 1ull << r;
                 }
             }
         }
     }
 #pragma unroll
-    for (int j = 0; j < CPL; ++j) m[CPL * lane + j] = (uint64_t)lo[j] | ((uint64_t)hi[j] << 32);
+    for (int j = 0; j < CPL; ++j) { m.lt[CPL * lane + j] = lt[j]; m.le[CPL * lane + j] = le[j]; }
 #pragma unroll
     for (int hc = 0; hc < 2; ++hc) {
         const uint32_t x = x0 + W + hc;
         const bool okx = pz && x < g.pts.x;
         const uint32_t y = y0 + lane, y2 = y0 + 32 + lane;
-        const bool b = okx && y < g.pts.y && sample_at(vol, g, x, y, p) < g.iso;
-        const bool b2 = okx && lane < 2 && y2 < g.pts.y && sample_at(vol, g, x, y2, p) < g.iso;
-        const uint32_t l32 = __ballot_sync(0xffffffffu, b);
-        const uint32_t h2 = __ballot_sync(0xffffffffu, b2) & 3u;
-        if (lane == 0) m[W + hc] = (uint64_t)l32 | ((uint64_t)h2 << 32);
+        const float v = (okx && y < g.pts.y) ? sample_at(vol, g, x, y, p) : 0.f;
+        const float v2 = (okx && lane < 2 && y2 < g.pts.y) ? sample_at(vol, g, x, y2, p) : 0.f;
+        const bool in1 = okx && y < g.pts.y, in2 = okx && lane < 2 && y2 < g.pts.y;
+        const uint32_t l32 = __ballot_sync(0xffffffffu, in1 && v < g.iso);
+        const uint32_t h2 = __ballot_sync(0xffffffffu, in2 && v2 < g.iso) & 3u;
+        const uint32_t e32 = __ballot_sync(0xffffffffu, in1 && v <= g.iso);
+        const uint32_t eh2 = __ballot_sync(0xffffffffu, in2 && v2 <= g.iso) & 3u;
+        if (lane == 0) {
+            m.lt[W + hc] = (uint64_t)l32 | ((uint64_t)h2 << 32);
+            m.le[W + hc] = (uint64_t)e32 | ((uint64_t)eh2 << 32);
+        }
     }
 }
 
@@ -303,6 +356,44 @@ __device__ __forceinline__ void load_cell(const T *vol, const Geom &g, uint32_t 
     v[6] = load_sample(p, sz + sy + 1); v[7] = load_sample(p, sz + sy);
 }
 
+// Reference bipolarity and ccw bits of the cell's own edges (dmc.cu:1199-1216)
+// from the "below" (lt) and "at or below" (le) bits of corners 2, 5, 6, 7:
+// ref_bipolar(a,b) = not both below, not both above, not both equal.
+__device__ __forceinline__ uint32_t info_from_bits(uint32_t cfg, uint32_t le4)
+{
+    // le4: bit 0 corner 2, bit 1 corner 5, bit 2 corner 6, bit 3 corner 7
+    const uint32_t l2 = (cfg >> 2) & 1u, l5 = (cfg >> 5) & 1u, l6 = (cfg >> 6) & 1u, l7 = (cfg >> 7) & 1u;
+    const uint32_t e2 = le4 & 1u, e5 = (le4 >> 1) & 1u, e6 = (le4 >> 2) & 1u, e7 = (le4 >> 3) & 1u;
+    auto bip = [](uint32_t la, uint32_t ea, uint32_t lb, uint32_t eb) -> uint32_t {
+        const uint32_t qa = ea & ~la, qb = eb & ~lb;          // exactly at the isovalue
+        return ~(la & lb) & (ea | eb) & ~(qa & qb) & 1u;
+    };
+    const uint32_t b6 = bip(l2, e2, l6, e6), b9 = bip(l5, e5, l6, e6), b10 = bip(l7, e7, l6, e6);
+    return b6 | (b9 << 1) | (b10 << 2) | ((b6 & e2) << 3) | ((b9 & e5) << 4) | ((b10 & e7) << 5);
+}
+
+// le bits of corners 2, 5, 6, 7 of the cell in row r (masks of columns c, c+1
+// in planes k (A,B) and k+1 (C,D)).
+__device__ __forceinline__ uint32_t le4_from_masks(uint64_t B, uint64_t C, uint64_t D, int r)
+{
+    return (uint32_t)((B >> (r + 1)) & 1u) | ((uint32_t)((D >> r) & 1u) << 1) |
+           ((uint32_t)((D >> (r + 1)) & 1u) << 2) | ((uint32_t)((C >> (r + 1)) & 1u) << 3);
+}
+
+// 32x32 bit transpose across the warp: on entry lane l holds column l (bit r
+// = row r); on exit lane r holds row r (bit l = column l).
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x, int lane)
+{
+    const uint32_t lo[5] = {0x0000ffffu, 0x00ff00ffu, 0x0f0f0f0fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        const int s = 16 >> i;
+        const uint32_t y = __shfl_xor_sync(0xffffffffu, x, s);
+        x = (lane & s) ? ((x & ~lo[i]) | ((y & ~lo[i]) >> s)) : ((x & lo[i]) | ((y & lo[i]) << s));
+    }
+    return x;
+}
+
 // Count sweep: per segment (vertices, quads) of the brick's own 32 rows.
 template <class T, bool VEC>
 __global__ void __launch_bounds__(32 * NWB) brick_count(const T *__restrict__ vol, Geom g,
@@ -328,24 +419,28 @@ __global__ void __launch_bounds__(32 * NWB) brick_count(const T *__restrict__ vo
         for (uint32_t k = z0; k < z1; ++k) {
             load_plane<T, VEC>(vol, g, x0, y0, k + 1, S.mask[(k + 1) & 1], lane);
             __syncwarp();
-            const uint64_t *mk = S.mask[k & 1], *mk1 = S.mask[(k + 1) & 1];
+            const uint64_t *mk = S.mask[k & 1].lt, *mk1 = S.mask[(k + 1) & 1].lt;
+            const uint64_t *ek = S.mask[k & 1].le, *ek1 = S.mask[(k + 1) & 1].le;
 #pragma unroll 1
             for (int j = 0; j < CPL; ++j) {
                 const int c = CPL * lane + j;
                 const uint32_t x = x0 + c;
-                uint64_t a = x < g.cells.x ? active_rows(mk[c], mk[c + 1], mk1[c], mk1[c + 1]) & rowmask : 0ull;
-                while (a) {
+                const uint64_t A = mk[c], B = mk[c + 1], C = mk1[c], D = mk1[c + 1];
+                uint64_t a = x < g.cells.x ? active_rows(A, B, C, D) & rowmask : 0ull;
+                if (!a) continue;
+                const uint64_t EB = ek[c + 1], EC = ek1[c], ED = ek1[c + 1];
+                do {
                     const int r = __ffsll((long long)a) - 1;
                     a &= a - 1;
                     const uint32_t y = y0 + r;
-                    const uint32_t cfg = cfg_from_masks(mk[c], mk[c + 1], mk1[c], mk1[c + 1], r);
+                    const uint32_t cfg = cfg_from_masks(A, B, C, D, r);
                     const bool l2 = needs_lut2(vol, g, tab, cfg, mk, mk1, c, r, x, y, k);
-                    const uint32_t info = owned_info_global(vol, g, x, y, k);
+                    const uint32_t info = info_from_bits(cfg, le4_from_masks(EB, EC, ED, r));
                     const uint32_t nv = nvert_of(tab, cfg, l2) + __popc(info & 7u);
                     const uint32_t nq = quad_count(info, cfg, x, y, k, g.cells, n_drop);
                     atomicAdd(&S.rowv[r], nv | (nq << 16));
                     ++n_act; n_l2 += l2;
-                }
+                } while (a);
             }
             __syncwarp();
             if (y0 + lane < g.cells.y) {
@@ -408,7 +503,7 @@ __global__ void __launch_bounds__(32 * NWB) brick_emit(const T *__restrict__ vol
                     S.segv[cur][r][0] = own.x; S.segv[cur][r][1] = nxt.x; S.segq[cur][r] = own.y;
                 }
                 __syncwarp();
-                const uint64_t *mk = S.mask[cur], *mk1 = S.mask[(k + 1) & 1];
+                const uint64_t *mk = S.mask[cur].lt, *mk1 = S.mask[(k + 1) & 1].lt;
                 uint64_t act[CPL];
 #pragma unroll
                 for (int j = 0; j < CPL; ++j) {
@@ -417,31 +512,25 @@ __global__ void __launch_bounds__(32 * NWB) brick_emit(const T *__restrict__ vol
                 }
                 uint64_t hact = 0;
                 if (lane == 0 && x0 + W < g.cells.x) hact = active_rows(mk[W], mk[W + 1], mk1[W], mk1[W + 1]) & rowmask;
-                // per-row ballots: the row's active cells in x order
-#pragma unroll 1
-                for (int r = 0; r < HROWS; ++r) {
-#pragma unroll
-                    for (int j = 0; j < CPL; ++j) {
-                        const uint32_t bb = __ballot_sync(0xffffffffu, (act[j] >> r) & 1ull);
-                        if (lane == (r & 31)) S.ball[cur][r][j] = bb;
-                    }
-                }
-                if (lane == 0) S.hact[cur] = hact;
-                __syncwarp();
+                // rows 0..31: bit transpose gives each lane its row's active
+                // lanes per column-in-lane; row 32 by ballots
                 uint32_t cnt = 0, cnt32 = 0;
 #pragma unroll
-                for (int j = 0; j < CPL; ++j) cnt += __popc(S.ball[cur][lane][j]);
-                cnt += (uint32_t)((S.hact[cur] >> lane) & 1ull);
-                if (lane == 0) {
-#pragma unroll
-                    for (int j = 0; j < CPL; ++j) cnt32 += __popc(S.ball[cur][32][j]);
-                    cnt32 += (uint32_t)((S.hact[cur] >> 32) & 1ull);
+                for (int j = 0; j < CPL; ++j) {
+                    const uint32_t rowbits = warp_transpose32((uint32_t)act[j], lane);
+                    S.ball[cur][lane][j] = rowbits;
+                    cnt += __popc(rowbits);
+                    const uint32_t b32 = __ballot_sync(0xffffffffu, (act[j] >> 32) & 1ull);
+                    if (lane == 0) S.ball[cur][32][j] = b32;
+                    cnt32 += __popc(b32);
                 }
+                hact = __shfl_sync(0xffffffffu, hact, 0);
+                cnt += (uint32_t)((hact >> lane) & 1ull);
+                cnt32 += (uint32_t)((hact >> 32) & 1ull);
                 const uint32_t inc = warp_incl_scan(cnt, lane);
                 const uint32_t tot32 = __shfl_sync(0xffffffffu, inc, 31);
-                cnt32 = __shfl_sync(0xffffffffu, cnt32, 0);
                 S.rowstart[cur][lane] = (uint16_t)(inc - cnt);
-                if (lane == 0) { S.rowstart[cur][32] = (uint16_t)tot32; S.rowstart[cur][33] = (uint16_t)(tot32 + cnt32); }
+                if (lane == 0) { S.rowstart[cur][32] = (uint16_t)tot32; S.rowstart[cur][33] = (uint16_t)(tot32 + cnt32); S.hact[cur] = hact; }
                 L = tot32 + cnt32;
                 __syncwarp();
 #pragma unroll
@@ -453,15 +542,19 @@ __global__ void __launch_bounds__(32 * NWB) brick_emit(const T *__restrict__ vol
                         M.lst(cur, entry_of(S, cur, r, CPL * lane + j)) = (uint16_t)((r << 8) | (CPL * lane + j));
                     }
                 }
-                while (hact) {
-                    const int r = __ffsll((long long)hact) - 1;
-                    hact &= hact - 1;
-                    M.lst(cur, S.rowstart[cur][r + 1] - 1u) = (uint16_t)((r << 8) | W);
+                if (lane == 0) {
+                    uint64_t h = hact;
+                    while (h) {
+                        const int r = __ffsll((long long)h) - 1;
+                        h &= h - 1;
+                        M.lst(cur, S.rowstart[cur][r + 1] - 1u) = (uint16_t)((r << 8) | W);
+                    }
                 }
                 __syncwarp();
             }
             // ranked active cells: counts, offsets inside their segment, vertices
-            const uint64_t *mk = S.mask[cur], *mk1 = S.mask[(k + 1) & 1];
+            const uint64_t *mk = S.mask[cur].lt, *mk1 = S.mask[(k + 1) & 1].lt;
+            const uint64_t *ek = S.mask[cur].le, *ek1 = S.mask[(k + 1) & 1].le;
             uint32_t run = 0;
             for (uint32_t base = 0; base < L; base += 32) {
                 const uint32_t i = base + lane;
@@ -470,16 +563,14 @@ __global__ void __launch_bounds__(32 * NWB) brick_emit(const T *__restrict__ vol
                 int r = 0, c = 0;
                 bool l2 = false, own = false;
                 uint32_t x = 0, y = 0;
-                float v[8];
                 if (valid) {
                     const uint32_t e = M.lst(cur, i);
                     r = e >> 8; c = e & 0xff;
                     x = x0 + c; y = y0 + r;
                     own = r < ROWS && c < W;
-                    load_cell(vol, g, x, y, k, v);
-                    cfg = config_of(v, g.iso);
+                    cfg = cfg_from_masks(mk[c], mk[c + 1], mk1[c], mk1[c + 1], r);
                     l2 = needs_lut2(vol, g, tab, cfg, mk, mk1, c, r, x, y, k);
-                    info = owned_edge_info(v, g.iso);
+                    info = info_from_bits(cfg, le4_from_masks(ek[c + 1], ek1[c], ek1[c + 1], r));
                     nv = nvert_of(tab, cfg, l2) + __popc(info & 7u);
                     uint32_t nq = 0, dummy = 0;
                     if (own) nq = quad_count(info, cfg, x, y, k, g.cells, dummy);
@@ -501,6 +592,8 @@ __global__ void __launch_bounds__(32 * NWB) brick_emit(const T *__restrict__ vol
                         if (vb + nv > out.vcap) {
                             atomicOr(err, DEV_ERR_OVERFLOW);
                         } else {
+                            float v[8];
+                            load_cell(vol, g, x, y, k, v);
                             Geo geo;
                             geo.x0 = g.coord[x]; geo.x1 = g.coord[x + 1];
                             geo.y0 = g.coord[g.pts.x + y]; geo.y1 = g.coord[g.pts.x + y + 1];
@@ -512,7 +605,11 @@ __global__ void __launch_bounds__(32 * NWB) brick_emit(const T *__restrict__ vol
                 }
                 __syncwarp();
             }
-            // quads of own cells of plane k-1: their +z ring cells are in plane k
+            // quads of own cells of plane k-1: their +z ring cells are in plane k.
+            // Ring cells (dmc.cu:653-664): e6 -> (c,r) (c+1,r) (c+1,r+1) (c,r+1) in
+            // plane k-1; e9 -> (c,r,k-1) (c,r,k) (c+1,r,k) (c+1,r,k-1); e10 ->
+            // (c,r,k-1) (c,r+1,k-1) (c,r+1,k) (c,r,k).  A +x neighbour of an active
+            // cell that is itself active is the next entry of the same row.
             if (k > z0) {
                 const uint32_t kp = k - 1;
                 const uint32_t Lp = S.rowstart[prv][HROWS];
@@ -524,25 +621,51 @@ __global__ void __launch_bounds__(32 * NWB) brick_emit(const T *__restrict__ vol
                     const uint32_t d = M.ent(prv, i);
                     const uint32_t cfg = cell_cfg(d);
                     const uint32_t info = M.info(prv, i);
+                    uint32_t want = 0;
+#pragma unroll
+                    for (int s = 0; s < 3; ++s)
+                        if ((info & (1u << s)) && owned_quad_in_volume(s, x, y, kp, g.cells) && owned_sign_change(cfg, s)) want |= 1u << s;
+                    if (!want) continue;
                     uint64_t q = (uint64_t)S.segq[prv][r] + cell_qrel(d);
+                    // entries of the ring cells: (plane, row, col) -> list index
+                    const uint32_t e_up = (want & 5u) ? entry_of(S, prv, r + 1, c) : 0u;    // (c, r+1, k-1)
+                    const uint32_t e_z = (want & 6u) ? entry_of(S, cur, r, c) : 0u;        // (c, r, k)
+                    const uint32_t e_zup = (want & 4u) ? entry_of(S, cur, r + 1, c) : 0u;  // (c, r+1, k)
 #pragma unroll
                     for (int s = 0; s < 3; ++s) {
-                        if (!(info & (1u << s)) || !owned_quad_in_volume(s, x, y, kp, g.cells) || !owned_sign_change(cfg, s)) continue;
+                        if (!(want & (1u << s))) continue;
                         if (q >= out.qcap) { atomicOr(err, DEV_ERR_OVERFLOW); break; }
+                        // ccw ring order: ring slots 0..3 = (plane, list index, ring edge)
+                        uint32_t ri[4]; int rp[4], rr[4], rc[4];
+                        const int E[3][4] = {{6, 7, 4, 5}, {9, 1, 3, 11}, {10, 8, 0, 2}};
+                        if (s == 0) {
+                            rp[0] = prv; ri[0] = i;        rr[0] = r;     rc[0] = c;
+                            rp[1] = prv; ri[1] = i + 1;    rr[1] = r;     rc[1] = c + 1;
+                            rp[2] = prv; ri[2] = e_up + 1; rr[2] = r + 1; rc[2] = c + 1;
+                            rp[3] = prv; ri[3] = e_up;     rr[3] = r + 1; rc[3] = c;
+                        } else if (s == 1) {
+                            rp[0] = prv; ri[0] = i;        rr[0] = r;     rc[0] = c;
+                            rp[1] = cur; ri[1] = e_z;      rr[1] = r;     rc[1] = c;
+                            rp[2] = cur; ri[2] = e_z + 1;  rr[2] = r;     rc[2] = c + 1;
+                            rp[3] = prv; ri[3] = i + 1;    rr[3] = r;     rc[3] = c + 1;
+                        } else {
+                            rp[0] = prv; ri[0] = i;        rr[0] = r;     rc[0] = c;
+                            rp[1] = prv; ri[1] = e_up;     rr[1] = r + 1; rc[1] = c;
+                            rp[2] = cur; ri[2] = e_zup;    rr[2] = r + 1; rc[2] = c;
+                            rp[3] = cur; ri[3] = e_z;      rr[3] = r;     rc[3] = c;
+                        }
                         const bool ccw = (info >> (s + 3)) & 1u;
                         uint32_t idx[4];
 #pragma unroll
                         for (int it = 0; it < 4; ++it) {
                             const int kk = ccw ? it : (4 - it) & 3;
-                            int re, dx, dy, dz;
-                            ring_entry(s, kk, re, dx, dy, dz);
-                            const int rr = r + dy, rc = c + dx, pl = dz ? cur : prv;
-                            const uint32_t ri = entry_of(S, pl, rr, rc);
-                            if (ri >= S.rowstart[pl][HROWS]) { atomicOr(err, DEV_ERR_BOUNDS); idx[it] = 0; continue; }
-                            const uint32_t rd = M.ent(pl, ri);
-                            uint32_t m = lut_m(tab, cell_cfg(rd), cell_l2(rd), re);
+                            const int pl = rp[kk];
+                            const uint32_t li = ri[kk];
+                            if (li >= S.rowstart[pl][HROWS]) { atomicOr(err, DEV_ERR_BOUNDS); idx[it] = 0; continue; }
+                            const uint32_t rd = M.ent(pl, li);
+                            uint32_t m = lut_m(tab, cell_cfg(rd), cell_l2(rd), E[s][kk]);
                             if (m == 0xffu) { atomicOr(err, DEV_ERR_BOUNDS); m = 0; }
-                            idx[it] = S.segv[pl][rr][rc == W ? 1 : 0] + cell_vrel(rd) + m;
+                            idx[it] = S.segv[pl][rr[kk]][rc[kk] == W ? 1 : 0] + cell_vrel(rd) + m;
                         }
                         reinterpret_cast<uint4 *>(out.quads)[q] = make_uint4(idx[0], idx[1], idx[2], idx[3]);
                         if (out.tris) {
@@ -641,6 +764,12 @@ static dmc_status brick_run_v(Ctx *ctx, const T *vol, const ExtractArgs &a, cuda
         else if (f > 65535.f) t = 65536;
         else { uint32_t fl = (uint32_t)f; t = ((float)fl == f) ? fl : fl + 1; }
         g.iso_u16 = t;
+        // v <= iso  <=>  v < floor(iso) + 1
+        uint32_t te;
+        if (!(f >= 0.f)) te = 0;
+        else if (f >= 65535.f) te = 65536;
+        else te = (uint32_t)f + 1;
+        g.isole_u16 = te;
     }
     g.nxs = (a.cells.x + W - 1) / W;
     g.nyb = (a.cells.y + ROWS - 1) / ROWS;
