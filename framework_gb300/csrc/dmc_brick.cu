@@ -107,8 +107,8 @@ __device__ __forceinline__ uint32_t spread16(uint32_t a, uint32_t b, bool upper)
 }
 
 template <class T, bool VEC>
-__device__ __forceinline__ void load_plane(const T *vol, const Geom &g, uint32_t x0, uint32_t y0, uint32_t p,
-                                           PlaneMasks &m, int lane)
+__device__ __noinline__ void load_plane(const T *vol, const Geom &g, uint32_t x0, uint32_t y0, uint32_t p,
+                                        PlaneMasks &m, int lane)
 {
     uint64_t lt[CPL] = {0, 0, 0, 0}, le[CPL] = {0, 0, 0, 0};
     const uint32_t xb = x0 + CPL * lane;
@@ -119,60 +119,64 @@ __device__ __forceinline__ void load_plane(const T *vol, const Geom &g, uint32_t
         const uint32_t nrow = min(34u, g.pts.y - y0);
         if (VEC && nrow == 34 && xb + CPL <= g.pts.x) {
             if constexpr (sizeof(T) == 4) {
-                uint32_t a[CPL] = {0, 0, 0, 0}, b[CPL] = {0, 0, 0, 0}, ha[CPL] = {0, 0, 0, 0}, hb[CPL] = {0, 0, 0, 0};
                 const float4 *q = reinterpret_cast<const float4 *>(base);
                 const uint64_t step = sx / 4;
-#pragma unroll
-                for (int r = 0; r < 34; ++r) {
-                    const float4 v = __ldg(q);
-                    q += step;
-                    const float vv[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-                    for (int j = 0; j < CPL; ++j) {
-                        if (r < 32) {
-                            if (vv[j] < g.iso) a[j] |= 1u << r;
-                            if (vv[j] <= g.iso) b[j] |= 1u << r;
-                        } else {
-                            if (vv[j] < g.iso) ha[j] |= 1u << (r - 32);
-                            if (vv[j] <= g.iso) hb[j] |= 1u << (r - 32);
-                        }
-                    }
+                uint32_t a0 = 0, a1 = 0, a2 = 0, a3 = 0, b0 = 0, b1 = 0, b2 = 0, b3 = 0;
+#pragma unroll 8
+                for (int r = 0; r < 32; ++r) {
+                    const float4 v = __ldg(q + r * step);
+                    const uint32_t bit = 1u << r;
+                    a0 |= v.x < g.iso ? bit : 0u; a1 |= v.y < g.iso ? bit : 0u;
+                    a2 |= v.z < g.iso ? bit : 0u; a3 |= v.w < g.iso ? bit : 0u;
+                    b0 |= v.x <= g.iso ? bit : 0u; b1 |= v.y <= g.iso ? bit : 0u;
+                    b2 |= v.z <= g.iso ? bit : 0u; b3 |= v.w <= g.iso ? bit : 0u;
                 }
+                uint32_t h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 #pragma unroll
-                for (int j = 0; j < CPL; ++j) {
-                    lt[j] = (uint64_t)a[j] | ((uint64_t)ha[j] << 32);
-                    le[j] = (uint64_t)b[j] | ((uint64_t)hb[j] << 32);
+                for (int r = 0; r < 2; ++r) {
+                    const float4 v = __ldg(q + (32 + r) * step);
+                    const uint32_t bit = 1u << r;
+                    h[0] |= v.x < g.iso ? bit : 0u; h[1] |= v.y < g.iso ? bit : 0u;
+                    h[2] |= v.z < g.iso ? bit : 0u; h[3] |= v.w < g.iso ? bit : 0u;
+                    h[4] |= v.x <= g.iso ? bit : 0u; h[5] |= v.y <= g.iso ? bit : 0u;
+                    h[6] |= v.z <= g.iso ? bit : 0u; h[7] |= v.w <= g.iso ? bit : 0u;
                 }
+                lt[0] = a0 | ((uint64_t)h[0] << 32); lt[1] = a1 | ((uint64_t)h[1] << 32);
+                lt[2] = a2 | ((uint64_t)h[2] << 32); lt[3] = a3 | ((uint64_t)h[3] << 32);
+                le[0] = b0 | ((uint64_t)h[4] << 32); le[1] = b1 | ((uint64_t)h[5] << 32);
+                le[2] = b2 | ((uint64_t)h[6] << 32); le[3] = b3 | ((uint64_t)h[7] << 32);
             } else {
-                // two samples per 32-bit word: per-halfword compares; bit r of
-                // rows 0..15 of columns (0,1) accumulate in one word, (2,3) in another
+                // two samples per 32-bit word, per-halfword compares: rows
+                // 0..15 of columns (0,1) accumulate in one word, (2,3) in another
                 const bool all_lt = g.iso_u16 > 0xffffu, all_le = g.isole_u16 > 0xffffu;
                 const uint32_t tl = all_lt ? 0u : (g.iso_u16 | (g.iso_u16 << 16));
                 const uint32_t te = all_le ? 0u : (g.isole_u16 | (g.isole_u16 << 16));
-                uint32_t l01a = 0, l23a = 0, l01b = 0, l23b = 0, l01h = 0, l23h = 0;
-                uint32_t e01a = 0, e23a = 0, e01b = 0, e23b = 0, e01h = 0, e23h = 0;
                 const uint2 *q = reinterpret_cast<const uint2 *>(base);
                 const uint64_t step = sx / 4;
+                uint32_t acc[3][4];   // [rows 0-15, 16-31, 32-33][lt01, lt23, le01, le23]
 #pragma unroll
-                for (int r = 0; r < 34; ++r) {
-                    const uint2 w = __ldg(q);
-                    q += step;
-                    const uint32_t c0 = (all_lt ? 0xffffffffu : __vcmpltu2(w.x, tl)) & 0x00010001u;
-                    const uint32_t c1 = (all_lt ? 0xffffffffu : __vcmpltu2(w.y, tl)) & 0x00010001u;
-                    const uint32_t d0 = (all_le ? 0xffffffffu : __vcmpltu2(w.x, te)) & 0x00010001u;
-                    const uint32_t d1 = (all_le ? 0xffffffffu : __vcmpltu2(w.y, te)) & 0x00010001u;
-                    if (r < 16) { l01a |= c0 << r; l23a |= c1 << r; e01a |= d0 << r; e23a |= d1 << r; }
-                    else if (r < 32) { l01b |= c0 << (r - 16); l23b |= c1 << (r - 16); e01b |= d0 << (r - 16); e23b |= d1 << (r - 16); }
-                    else { l01h |= c0 << (r - 32); l23h |= c1 << (r - 32); e01h |= d0 << (r - 32); e23h |= d1 << (r - 32); }
+                for (int h = 0; h < 3; ++h) {
+                    acc[h][0] = acc[h][1] = acc[h][2] = acc[h][3] = 0;
+                    const int r0 = 16 * h, n = h < 2 ? 16 : 2;
+#pragma unroll 8
+                    for (int i = 0; i < n; ++i) {
+                        const uint2 w = __ldg(q + (r0 + i) * step);
+                        const uint32_t c0 = all_lt ? 0x00010001u : (__vcmpltu2(w.x, tl) & 0x00010001u);
+                        const uint32_t c1 = all_lt ? 0x00010001u : (__vcmpltu2(w.y, tl) & 0x00010001u);
+                        const uint32_t d0 = all_le ? 0x00010001u : (__vcmpltu2(w.x, te) & 0x00010001u);
+                        const uint32_t d1 = all_le ? 0x00010001u : (__vcmpltu2(w.y, te) & 0x00010001u);
+                        acc[h][0] |= c0 << i; acc[h][1] |= c1 << i; acc[h][2] |= d0 << i; acc[h][3] |= d1 << i;
+                    }
                 }
-                lt[0] = spread16(l01a, l01b, false) | ((uint64_t)(l01h & 3u) << 32);
-                lt[1] = spread16(l01a, l01b, true) | ((uint64_t)((l01h >> 16) & 3u) << 32);
-                lt[2] = spread16(l23a, l23b, false) | ((uint64_t)(l23h & 3u) << 32);
-                lt[3] = spread16(l23a, l23b, true) | ((uint64_t)((l23h >> 16) & 3u) << 32);
-                le[0] = spread16(e01a, e01b, false) | ((uint64_t)(e01h & 3u) << 32);
-                le[1] = spread16(e01a, e01b, true) | ((uint64_t)((e01h >> 16) & 3u) << 32);
-                le[2] = spread16(e23a, e23b, false) | ((uint64_t)(e23h & 3u) << 32);
-                le[3] = spread16(e23a, e23b, true) | ((uint64_t)((e23h >> 16) & 3u) << 32);
+#pragma unroll
+                for (int t = 0; t < 2; ++t) {        // t = 0: lt, 1: le
+                    uint64_t *dst = t ? le : lt;
+                    const uint32_t *a = &acc[0][2 * t], *b = &acc[1][2 * t], *hh = &acc[2][2 * t];
+                    dst[0] = spread16(a[0], b[0], false) | ((uint64_t)(hh[0] & 3u) << 32);
+                    dst[1] = spread16(a[0], b[0], true) | ((uint64_t)((hh[0] >> 16) & 3u) << 32);
+                    dst[2] = spread16(a[1], b[1], false) | ((uint64_t)(hh[1] & 3u) << 32);
+                    dst[3] = spread16(a[1], b[1], true) | ((uint64_t)((hh[1] >> 16) & 3u) << 32);
+                }
             }
         } else {
             for (uint32_t r = 0; r < nrow; ++r) {
@@ -188,14 +192,14 @@ __device__ __forceinline__ void load_plane(const T *vol, const Geom &g, uint32_t
     }
 #pragma unroll
     for (int j = 0; j < CPL; ++j) { m.lt[CPL * lane + j] = lt[j]; m.le[CPL * lane + j] = le[j]; }
-#pragma unroll
+#pragma unroll 1
     for (int hc = 0; hc < 2; ++hc) {
         const uint32_t x = x0 + W + hc;
         const bool okx = pz && x < g.pts.x;
         const uint32_t y = y0 + lane, y2 = y0 + 32 + lane;
-        const float v = (okx && y < g.pts.y) ? sample_at(vol, g, x, y, p) : 0.f;
-        const float v2 = (okx && lane < 2 && y2 < g.pts.y) ? sample_at(vol, g, x, y2, p) : 0.f;
         const bool in1 = okx && y < g.pts.y, in2 = okx && lane < 2 && y2 < g.pts.y;
+        const float v = in1 ? sample_at(vol, g, x, y, p) : 0.f;
+        const float v2 = in2 ? sample_at(vol, g, x, y2, p) : 0.f;
         const uint32_t l32 = __ballot_sync(0xffffffffu, in1 && v < g.iso);
         const uint32_t h2 = __ballot_sync(0xffffffffu, in2 && v2 < g.iso) & 3u;
         const uint32_t e32 = __ballot_sync(0xffffffffu, in1 && v <= g.iso);
