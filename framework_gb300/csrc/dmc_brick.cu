@@ -35,7 +35,7 @@ constexpr int W = 32 * CPL;               // cell columns per brick (= segment w
 constexpr int ROWS = 32;                  // own cell rows
 constexpr int HROWS = ROWS + 1;           // with the halo row
 constexpr int MAXL = HROWS * (W + 1);     // most active cells one plane of a brick can hold
-constexpr int CAP = 512;                  // entries kept in shared memory per plane
+constexpr int CAP = 320;                  // entries kept in shared memory per plane
 constexpr int OVF = MAXL - CAP;           // entries per plane that spill to global scratch
 constexpr int NWB = 8;                    // warps per block (independent)
 constexpr int SCAN_NT = 256, SCAN_ITEMS = 8, SCAN_TILE = SCAN_NT * SCAN_ITEMS;
@@ -64,7 +64,7 @@ struct WarpSmem {
     uint32_t rowbase[HROWS];           // running (v | q << 16) prefix at each row start
     uint32_t segv[2][HROWS][2];        // vertex offset of (row, own / next segment)
     uint32_t segq[2][HROWS];           // quad offset of (row, own segment)
-    uint32_t rowv[ROWS], rowq[ROWS];   // count sweep: per-row totals
+    uint32_t rowtot[ROWS];             // count sweep: per-row (v | q << 16)
     uint32_t ent[2][CAP];              // packed cell: vrel 11 | qrel 10 | cfg 8 | lut2 1
     uint16_t lst[2][CAP];              // row << 8 | col
     uint8_t info[2][CAP];              // own-edge bipolar/ccw bits
@@ -106,10 +106,23 @@ __device__ __forceinline__ uint32_t spread16(uint32_t a, uint32_t b, bool upper)
     return upper ? ((a >> 16) | (b & 0xffff0000u)) : ((a & 0xffffu) | (b << 16));
 }
 
+struct PlaneArgs {
+    uint3 pts;
+    float iso;
+    uint32_t thr_lt, thr_le;   // uint16 thresholds (see Geom)
+};
+
+template <class T>
+__device__ __forceinline__ float sample_p(const T *vol, uint3 pts, uint32_t x, uint32_t y, uint32_t z)
+{
+    return load_sample(vol, ((uint64_t)z * pts.y + y) * pts.x + x);
+}
+
 template <class T, bool VEC>
-__device__ __noinline__ void load_plane(const T *vol, const Geom &g, uint32_t x0, uint32_t y0, uint32_t p,
+__device__ __noinline__ void load_plane(const T *vol, const PlaneArgs ga, uint32_t x0, uint32_t y0, uint32_t p,
                                         PlaneMasks &m, int lane)
 {
+    struct { uint3 pts; float iso; uint32_t iso_u16, isole_u16; } g = {ga.pts, ga.iso, ga.thr_lt, ga.thr_le};
     uint64_t lt[CPL] = {0, 0, 0, 0}, le[CPL] = {0, 0, 0, 0};
     const uint32_t xb = x0 + CPL * lane;
     const bool pz = p < g.pts.z;
@@ -198,8 +211,8 @@ __device__ __noinline__ void load_plane(const T *vol, const Geom &g, uint32_t x0
         const bool okx = pz && x < g.pts.x;
         const uint32_t y = y0 + lane, y2 = y0 + 32 + lane;
         const bool in1 = okx && y < g.pts.y, in2 = okx && lane < 2 && y2 < g.pts.y;
-        const float v = in1 ? sample_at(vol, g, x, y, p) : 0.f;
-        const float v2 = in2 ? sample_at(vol, g, x, y2, p) : 0.f;
+        const float v = in1 ? sample_p(vol, g.pts, x, y, p) : 0.f;
+        const float v2 = in2 ? sample_p(vol, g.pts, x, y2, p) : 0.f;
         const uint32_t l32 = __ballot_sync(0xffffffffu, in1 && v < g.iso);
         const uint32_t h2 = __ballot_sync(0xffffffffu, in2 && v2 < g.iso) & 3u;
         const uint32_t e32 = __ballot_sync(0xffffffffu, in1 && v <= g.iso);
@@ -398,87 +411,28 @@ __device__ __forceinline__ uint32_t warp_transpose32(uint32_t x, int lane)
     return x;
 }
 
-// Count sweep: per segment (vertices, quads) of the brick's own 32 rows.
-template <class T, bool VEC>
-__global__ void __launch_bounds__(32 * NWB) brick_count(const T *__restrict__ vol, Geom g,
+// One sweep kernel for both passes.
+//   EMIT = false (count): ranks the active cells of the brick's own 32 rows
+//     and writes per-segment (vertices, quads) totals.
+//   EMIT = true: also ranks the halo row and column, writes the vertices of
+//     plane k at their final offsets and the quads of plane k-1.
+// Active cells are compacted per plane in output order and processed 32 at a
+// time, one per lane, so that all lanes share the per-cell work.
+template <class T, bool VEC, bool EMIT>
+__global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vol, Geom g,
                                                         const DeviceTables *__restrict__ tabp,
-                                                        uint2 *__restrict__ seg_cnt, uint32_t *ticket,
-                                                        unsigned long long *counters)
-{
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const DeviceTables &tab = stage_tables(tabp, reinterpret_cast<DeviceTables *>(smem_raw));
-    WarpSmem &S = reinterpret_cast<WarpSmem *>(smem_raw + sizeof(DeviceTables))[warp];
-    uint32_t n_act = 0, n_l2 = 0, n_drop = 0;
-    S.rowv[lane] = 0;
-
-    for (;;) {
-        const uint32_t b = claim_brick(ticket, lane);
-        if (b >= g.nbricks) break;
-        const uint32_t xs = b % g.nxs, yb = (b / g.nxs) % g.nyb, zb = b / (g.nxs * g.nyb);
-        const uint32_t x0 = xs * W, y0 = yb * ROWS, z0 = zb * g.zc;
-        const uint32_t z1 = min(z0 + g.zc, g.cells.z);
-        const uint64_t rowmask = ((1ull << min((uint32_t)ROWS, g.cells.y - y0)) - 1ull);
-        load_plane<T, VEC>(vol, g, x0, y0, z0, S.mask[z0 & 1], lane);
-        for (uint32_t k = z0; k < z1; ++k) {
-            load_plane<T, VEC>(vol, g, x0, y0, k + 1, S.mask[(k + 1) & 1], lane);
-            __syncwarp();
-            const uint64_t *mk = S.mask[k & 1].lt, *mk1 = S.mask[(k + 1) & 1].lt;
-            const uint64_t *ek = S.mask[k & 1].le, *ek1 = S.mask[(k + 1) & 1].le;
-#pragma unroll 1
-            for (int j = 0; j < CPL; ++j) {
-                const int c = CPL * lane + j;
-                const uint32_t x = x0 + c;
-                const uint64_t A = mk[c], B = mk[c + 1], C = mk1[c], D = mk1[c + 1];
-                uint64_t a = x < g.cells.x ? active_rows(A, B, C, D) & rowmask : 0ull;
-                if (!a) continue;
-                const uint64_t EB = ek[c + 1], EC = ek1[c], ED = ek1[c + 1];
-                do {
-                    const int r = __ffsll((long long)a) - 1;
-                    a &= a - 1;
-                    const uint32_t y = y0 + r;
-                    const uint32_t cfg = cfg_from_masks(A, B, C, D, r);
-                    const bool l2 = needs_lut2(vol, g, tab, cfg, mk, mk1, c, r, x, y, k);
-                    const uint32_t info = info_from_bits(cfg, le4_from_masks(EB, EC, ED, r));
-                    const uint32_t nv = nvert_of(tab, cfg, l2) + __popc(info & 7u);
-                    const uint32_t nq = quad_count(info, cfg, x, y, k, g.cells, n_drop);
-                    atomicAdd(&S.rowv[r], nv | (nq << 16));
-                    ++n_act; n_l2 += l2;
-                } while (a);
-            }
-            __syncwarp();
-            if (y0 + lane < g.cells.y) {
-                const uint32_t t = S.rowv[lane];
-                seg_cnt[seg_index(g, k, y0 + lane, xs)] = make_uint2(t & 0xffffu, t >> 16);
-            }
-            S.rowv[lane] = 0;
-            __syncwarp();
-        }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        n_act += __shfl_xor_sync(0xffffffffu, n_act, o);
-        n_l2 += __shfl_xor_sync(0xffffffffu, n_l2, o);
-        n_drop += __shfl_xor_sync(0xffffffffu, n_drop, o);
-    }
-    if (lane == 0) {
-        if (n_act) atomicAdd(&counters[0], (unsigned long long)n_act);
-        if (n_l2) atomicAdd(&counters[1], (unsigned long long)n_l2);
-        if (n_drop) atomicAdd(&counters[2], (unsigned long long)n_drop);
-    }
-}
-
-// Emit sweep: ranks active cells, writes vertices of plane k and quads of plane k-1.
-template <class T, bool VEC>
-__global__ void __launch_bounds__(32 * NWB) brick_emit(const T *__restrict__ vol, Geom g,
-                                                       const DeviceTables *__restrict__ tabp, EmitOut out,
-                                                       Spill *__restrict__ spill, uint32_t *ticket, uint32_t *err)
+                                                        uint2 *__restrict__ seg_cnt, EmitOut out,
+                                                        Spill *__restrict__ spill, uint32_t *ticket,
+                                                        unsigned long long *counters, uint32_t *err)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const DeviceTables &tab = stage_tables(tabp, reinterpret_cast<DeviceTables *>(smem_raw));
     WarpSmem &S = reinterpret_cast<WarpSmem *>(smem_raw + sizeof(DeviceTables))[warp];
     WarpMem M{&S, spill + (uint64_t)blockIdx.x * NWB + warp};
+    const PlaneArgs pa{g.pts, g.iso, g.iso_u16, g.isole_u16};
+    constexpr uint32_t NR = EMIT ? HROWS : ROWS;   // ranked rows
+    uint32_t n_act = 0, n_l2 = 0, n_drop = 0;
 
     for (;;) {
         const uint32_t b = claim_brick(ticket, lane);
@@ -486,25 +440,27 @@ __global__ void __launch_bounds__(32 * NWB) brick_emit(const T *__restrict__ vol
         const uint32_t xs = b % g.nxs, yb = (b / g.nxs) % g.nyb, zb = b / (g.nxs * g.nyb);
         const uint32_t x0 = xs * W, y0 = yb * ROWS, z0 = zb * g.zc;
         const uint32_t z1 = min(z0 + g.zc, g.cells.z);
-        const uint64_t rowmask = ((1ull << min((uint32_t)HROWS, g.cells.y - y0)) - 1ull);
+        const uint64_t rowmask = ((1ull << min(NR, g.cells.y - y0)) - 1ull);
+        // the emit sweep also visits plane z1: quads of plane z1-1 reference it
+        const uint32_t kend = EMIT ? z1 : z1 - 1;
 
-        load_plane<T, VEC>(vol, g, x0, y0, z0, S.mask[z0 & 1], lane);
-        // planes z0..z1: plane z1 (when inside the volume) is ranked only so
-        // that the quads of plane z1-1 can reference it
-        for (uint32_t k = z0; k <= z1; ++k) {
+        load_plane<T, VEC>(vol, pa, x0, y0, z0, S.mask[z0 & 1], lane);
+        for (uint32_t k = z0; k <= kend; ++k) {
             const int cur = k & 1, prv = cur ^ 1;
             const bool have_plane = k < g.cells.z;
             uint32_t L = 0;
             if (have_plane) {
-                load_plane<T, VEC>(vol, g, x0, y0, k + 1, S.mask[(k + 1) & 1], lane);
-                for (uint32_t r = lane; r < HROWS; r += 32) {
-                    const uint32_t yy = y0 + r;
-                    uint2 own = make_uint2(0, 0), nxt = make_uint2(0, 0);
-                    if (yy < g.cells.y) {
-                        own = out.seg_off[seg_index(g, k, yy, xs)];
-                        if (xs + 1 < g.nxs) nxt = out.seg_off[seg_index(g, k, yy, xs + 1)];
+                load_plane<T, VEC>(vol, pa, x0, y0, k + 1, S.mask[(k + 1) & 1], lane);
+                if (EMIT) {
+                    for (uint32_t r = lane; r < HROWS; r += 32) {
+                        const uint32_t yy = y0 + r;
+                        uint2 own = make_uint2(0, 0), nxt = make_uint2(0, 0);
+                        if (yy < g.cells.y) {
+                            own = out.seg_off[seg_index(g, k, yy, xs)];
+                            if (xs + 1 < g.nxs) nxt = out.seg_off[seg_index(g, k, yy, xs + 1)];
+                        }
+                        S.segv[cur][r][0] = own.x; S.segv[cur][r][1] = nxt.x; S.segq[cur][r] = own.y;
                     }
-                    S.segv[cur][r][0] = own.x; S.segv[cur][r][1] = nxt.x; S.segq[cur][r] = own.y;
                 }
                 __syncwarp();
                 const uint64_t *mk = S.mask[cur].lt, *mk1 = S.mask[(k + 1) & 1].lt;
@@ -515,22 +471,26 @@ __global__ void __launch_bounds__(32 * NWB) brick_emit(const T *__restrict__ vol
                     act[j] = (x0 + c < g.cells.x) ? active_rows(mk[c], mk[c + 1], mk1[c], mk1[c + 1]) & rowmask : 0ull;
                 }
                 uint64_t hact = 0;
-                if (lane == 0 && x0 + W < g.cells.x) hact = active_rows(mk[W], mk[W + 1], mk1[W], mk1[W + 1]) & rowmask;
-                // rows 0..31: bit transpose gives each lane its row's active
-                // lanes per column-in-lane; row 32 by ballots
+                if (EMIT && lane == 0 && x0 + W < g.cells.x) hact = active_rows(mk[W], mk[W + 1], mk1[W], mk1[W + 1]) & rowmask;
+                // rows 0..31: a bit transpose gives each lane its row's active
+                // lanes per column-in-lane; row 32 (emit only) by ballots
                 uint32_t cnt = 0, cnt32 = 0;
 #pragma unroll
                 for (int j = 0; j < CPL; ++j) {
                     const uint32_t rowbits = warp_transpose32((uint32_t)act[j], lane);
                     S.ball[cur][lane][j] = rowbits;
                     cnt += __popc(rowbits);
-                    const uint32_t b32 = __ballot_sync(0xffffffffu, (act[j] >> 32) & 1ull);
-                    if (lane == 0) S.ball[cur][32][j] = b32;
-                    cnt32 += __popc(b32);
+                    if (EMIT) {
+                        const uint32_t b32 = __ballot_sync(0xffffffffu, (act[j] >> 32) & 1ull);
+                        if (lane == 0) S.ball[cur][32][j] = b32;
+                        cnt32 += __popc(b32);
+                    }
                 }
-                hact = __shfl_sync(0xffffffffu, hact, 0);
-                cnt += (uint32_t)((hact >> lane) & 1ull);
-                cnt32 += (uint32_t)((hact >> 32) & 1ull);
+                if (EMIT) {
+                    hact = __shfl_sync(0xffffffffu, hact, 0);
+                    cnt += (uint32_t)((hact >> lane) & 1ull);
+                    cnt32 += (uint32_t)((hact >> 32) & 1ull);
+                }
                 const uint32_t inc = warp_incl_scan(cnt, lane);
                 const uint32_t tot32 = __shfl_sync(0xffffffffu, inc, 31);
                 S.rowstart[cur][lane] = (uint16_t)(inc - cnt);
@@ -546,7 +506,7 @@ __global__ void __launch_bounds__(32 * NWB) brick_emit(const T *__restrict__ vol
                         M.lst(cur, entry_of(S, cur, r, CPL * lane + j)) = (uint16_t)((r << 8) | (CPL * lane + j));
                     }
                 }
-                if (lane == 0) {
+                if (EMIT && lane == 0) {
                     uint64_t h = hact;
                     while (h) {
                         const int r = __ffsll((long long)h) - 1;
@@ -556,7 +516,7 @@ __global__ void __launch_bounds__(32 * NWB) brick_emit(const T *__restrict__ vol
                 }
                 __syncwarp();
             }
-            // ranked active cells: counts, offsets inside their segment, vertices
+            // ranked active cells, 32 at a time
             const uint64_t *mk = S.mask[cur].lt, *mk1 = S.mask[(k + 1) & 1].lt;
             const uint64_t *ek = S.mask[cur].le, *ek1 = S.mask[(k + 1) & 1].le;
             uint32_t run = 0;
@@ -576,16 +536,19 @@ __global__ void __launch_bounds__(32 * NWB) brick_emit(const T *__restrict__ vol
                     l2 = needs_lut2(vol, g, tab, cfg, mk, mk1, c, r, x, y, k);
                     info = info_from_bits(cfg, le4_from_masks(ek[c + 1], ek1[c], ek1[c + 1], r));
                     nv = nvert_of(tab, cfg, l2) + __popc(info & 7u);
-                    uint32_t nq = 0, dummy = 0;
-                    if (own) nq = quad_count(info, cfg, x, y, k, g.cells, dummy);
+                    uint32_t nq = 0;
+                    if (own) nq = quad_count(info, cfg, x, y, k, g.cells, n_drop);
                     packed = nv | (nq << 16);
+                    n_l2 += l2;
                 }
                 const uint32_t incl = warp_incl_scan(packed, lane);
                 const uint32_t ex = run + incl - packed;
                 run += __shfl_sync(0xffffffffu, incl, 31);
                 if (valid && i == S.rowstart[cur][r]) S.rowbase[r] = ex;
                 __syncwarp();
-                if (valid) {
+                if (!EMIT) {
+                    if (valid && i + 1 == S.rowstart[cur][r + 1]) S.rowtot[r] = ex + packed - S.rowbase[r];
+                } else if (valid) {
                     const uint32_t rb = S.rowbase[r];
                     const uint32_t vrel = c == W ? 0u : (ex & 0xffffu) - (rb & 0xffffu);
                     const uint32_t qrel = (ex >> 16) - (rb >> 16);
@@ -609,12 +572,19 @@ __global__ void __launch_bounds__(32 * NWB) brick_emit(const T *__restrict__ vol
                 }
                 __syncwarp();
             }
+            if (!EMIT) {
+                if (y0 + lane < g.cells.y) {
+                    const uint32_t t = S.rowstart[cur][lane] == S.rowstart[cur][lane + 1] ? 0u : S.rowtot[lane];
+                    seg_cnt[seg_index(g, k, y0 + lane, xs)] = make_uint2(t & 0xffffu, t >> 16);
+                }
+                n_act += L;
+            }
             // quads of own cells of plane k-1: their +z ring cells are in plane k.
             // Ring cells (dmc.cu:653-664): e6 -> (c,r) (c+1,r) (c+1,r+1) (c,r+1) in
             // plane k-1; e9 -> (c,r,k-1) (c,r,k) (c+1,r,k) (c+1,r,k-1); e10 ->
-            // (c,r,k-1) (c,r+1,k-1) (c,r+1,k) (c,r,k).  A +x neighbour of an active
-            // cell that is itself active is the next entry of the same row.
-            if (k > z0) {
+            // (c,r,k-1) (c,r+1,k-1) (c,r+1,k) (c,r,k).  An active +x neighbour of an
+            // active cell is the next entry of the same row.
+            if (EMIT && k > z0) {
                 const uint32_t kp = k - 1;
                 const uint32_t Lp = S.rowstart[prv][HROWS];
                 for (uint32_t i = lane; i < Lp; i += 32) {
@@ -631,7 +601,6 @@ __global__ void __launch_bounds__(32 * NWB) brick_emit(const T *__restrict__ vol
                         if ((info & (1u << s)) && owned_quad_in_volume(s, x, y, kp, g.cells) && owned_sign_change(cfg, s)) want |= 1u << s;
                     if (!want) continue;
                     uint64_t q = (uint64_t)S.segq[prv][r] + cell_qrel(d);
-                    // entries of the ring cells: (plane, row, col) -> list index
                     const uint32_t e_up = (want & 5u) ? entry_of(S, prv, r + 1, c) : 0u;    // (c, r+1, k-1)
                     const uint32_t e_z = (want & 6u) ? entry_of(S, cur, r, c) : 0u;        // (c, r, k)
                     const uint32_t e_zup = (want & 4u) ? entry_of(S, cur, r + 1, c) : 0u;  // (c, r+1, k)
@@ -639,35 +608,34 @@ __global__ void __launch_bounds__(32 * NWB) brick_emit(const T *__restrict__ vol
                     for (int s = 0; s < 3; ++s) {
                         if (!(want & (1u << s))) continue;
                         if (q >= out.qcap) { atomicOr(err, DEV_ERR_OVERFLOW); break; }
-                        // ccw ring order: ring slots 0..3 = (plane, list index, ring edge)
-                        uint32_t ri[4]; int rp[4], rr[4], rc[4];
-                        const int E[3][4] = {{6, 7, 4, 5}, {9, 1, 3, 11}, {10, 8, 0, 2}};
+                        uint32_t ri[4]; int rp[4], rr[4], rc[4], re[4];
                         if (s == 0) {
-                            rp[0] = prv; ri[0] = i;        rr[0] = r;     rc[0] = c;
-                            rp[1] = prv; ri[1] = i + 1;    rr[1] = r;     rc[1] = c + 1;
-                            rp[2] = prv; ri[2] = e_up + 1; rr[2] = r + 1; rc[2] = c + 1;
-                            rp[3] = prv; ri[3] = e_up;     rr[3] = r + 1; rc[3] = c;
+                            rp[0] = prv; ri[0] = i;        rr[0] = r;     rc[0] = c;     re[0] = 6;
+                            rp[1] = prv; ri[1] = i + 1;    rr[1] = r;     rc[1] = c + 1; re[1] = 7;
+                            rp[2] = prv; ri[2] = e_up + 1; rr[2] = r + 1; rc[2] = c + 1; re[2] = 4;
+                            rp[3] = prv; ri[3] = e_up;     rr[3] = r + 1; rc[3] = c;     re[3] = 5;
                         } else if (s == 1) {
-                            rp[0] = prv; ri[0] = i;        rr[0] = r;     rc[0] = c;
-                            rp[1] = cur; ri[1] = e_z;      rr[1] = r;     rc[1] = c;
-                            rp[2] = cur; ri[2] = e_z + 1;  rr[2] = r;     rc[2] = c + 1;
-                            rp[3] = prv; ri[3] = i + 1;    rr[3] = r;     rc[3] = c + 1;
+                            rp[0] = prv; ri[0] = i;        rr[0] = r;     rc[0] = c;     re[0] = 9;
+                            rp[1] = cur; ri[1] = e_z;      rr[1] = r;     rc[1] = c;     re[1] = 1;
+                            rp[2] = cur; ri[2] = e_z + 1;  rr[2] = r;     rc[2] = c + 1; re[2] = 3;
+                            rp[3] = prv; ri[3] = i + 1;    rr[3] = r;     rc[3] = c + 1; re[3] = 11;
                         } else {
-                            rp[0] = prv; ri[0] = i;        rr[0] = r;     rc[0] = c;
-                            rp[1] = prv; ri[1] = e_up;     rr[1] = r + 1; rc[1] = c;
-                            rp[2] = cur; ri[2] = e_zup;    rr[2] = r + 1; rc[2] = c;
-                            rp[3] = cur; ri[3] = e_z;      rr[3] = r;     rc[3] = c;
+                            rp[0] = prv; ri[0] = i;        rr[0] = r;     rc[0] = c;     re[0] = 10;
+                            rp[1] = prv; ri[1] = e_up;     rr[1] = r + 1; rc[1] = c;     re[1] = 8;
+                            rp[2] = cur; ri[2] = e_zup;    rr[2] = r + 1; rc[2] = c;     re[2] = 0;
+                            rp[3] = cur; ri[3] = e_z;      rr[3] = r;     rc[3] = c;     re[3] = 2;
                         }
                         const bool ccw = (info >> (s + 3)) & 1u;
                         uint32_t idx[4];
 #pragma unroll
                         for (int it = 0; it < 4; ++it) {
+                            // ccw visits ring slots 0,1,2,3, cw 0,3,2,1 (dmc.cu:1636-1645)
                             const int kk = ccw ? it : (4 - it) & 3;
                             const int pl = rp[kk];
                             const uint32_t li = ri[kk];
                             if (li >= S.rowstart[pl][HROWS]) { atomicOr(err, DEV_ERR_BOUNDS); idx[it] = 0; continue; }
                             const uint32_t rd = M.ent(pl, li);
-                            uint32_t m = lut_m(tab, cell_cfg(rd), cell_l2(rd), E[s][kk]);
+                            uint32_t m = lut_m(tab, cell_cfg(rd), cell_l2(rd), re[kk]);
                             if (m == 0xffu) { atomicOr(err, DEV_ERR_BOUNDS); m = 0; }
                             idx[it] = S.segv[pl][rr[kk]][rc[kk] == W ? 1 : 0] + cell_vrel(rd) + m;
                         }
@@ -682,6 +650,18 @@ __global__ void __launch_bounds__(32 * NWB) brick_emit(const T *__restrict__ vol
                 }
             }
             __syncwarp();
+        }
+    }
+    if (!EMIT) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            n_l2 += __shfl_xor_sync(0xffffffffu, n_l2, o);
+            n_drop += __shfl_xor_sync(0xffffffffu, n_drop, o);
+        }
+        if (lane == 0) {
+            if (n_act) atomicAdd(&counters[0], (unsigned long long)n_act);
+            if (n_l2) atomicAdd(&counters[1], (unsigned long long)n_l2);
+            if (n_drop) atomicAdd(&counters[2], (unsigned long long)n_drop);
         }
     }
 }
@@ -744,11 +724,11 @@ template <class T, bool VEC>
 static int sweep_grid(Ctx *ctx)
 {
     using namespace brick;
-    cudaFuncSetAttribute(brick_emit<T, VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSweepSmem);
-    cudaFuncSetAttribute(brick_count<T, VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSweepSmem);
+    cudaFuncSetAttribute(brick_sweep<T, VEC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSweepSmem);
+    cudaFuncSetAttribute(brick_sweep<T, VEC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSweepSmem);
     int b0 = 0, b1 = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, brick_emit<T, VEC>, 32 * NWB, kSweepSmem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, brick_count<T, VEC>, 32 * NWB, kSweepSmem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, brick_sweep<T, VEC, true>, 32 * NWB, kSweepSmem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, brick_sweep<T, VEC, false>, 32 * NWB, kSweepSmem);
     int b = b0 < b1 ? b0 : b1;
     if (b < 1) b = 1;
     return b * ctx->num_sms;
@@ -813,8 +793,8 @@ static dmc_status brick_run_v(Ctx *ctx, const T *vol, const ExtractArgs &a, cuda
     coord_table<<<(unsigned)((n_coord + 255) / 256), 256, 0, st>>>(coord, a.pts, a.cells, a.rng, a.mn);
     ctx->evk_used = false;
     CUDA_TRY(cudaEventRecord(ctx->evk[0], st));
-    brick_count<T, VEC><<<grid, 32 * NWB, kSweepSmem, st>>>(vol, g, ctx->d_tab, seg_cnt, &tickets[0],
-                                                             ctx->d_ctl->counters);
+    brick_sweep<T, VEC, false><<<grid, 32 * NWB, kSweepSmem, st>>>(vol, g, ctx->d_tab, seg_cnt, EmitOut{}, spill,
+                                                                    &tickets[0], ctx->d_ctl->counters, &ctx->d_ctl->err);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaEventRecord(ctx->evk[1], st));
     ScanCtl ctl;
@@ -837,7 +817,8 @@ static dmc_status brick_run_v(Ctx *ctx, const T *vol, const ExtractArgs &a, cuda
     EmitOut eo;
     eo.seg_off = seg_off; eo.verts = a.verts; eo.vcap = a.vcap; eo.quads = a.quads; eo.qcap = a.qcap; eo.tris = a.tris;
     CUDA_TRY(cudaEventRecord(ctx->evk[3], st));
-    brick_emit<T, VEC><<<grid, 32 * NWB, kSweepSmem, st>>>(vol, g, ctx->d_tab, eo, spill, &tickets[1], &ctx->d_ctl->err);
+    brick_sweep<T, VEC, true><<<grid, 32 * NWB, kSweepSmem, st>>>(vol, g, ctx->d_tab, nullptr, eo, spill, &tickets[1],
+                                                                   ctx->d_ctl->counters, &ctx->d_ctl->err);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaEventRecord(ctx->evk[4], st));
     ctx->evk_used = true;

@@ -262,9 +262,9 @@ __device__ __forceinline__ void store3(float *p, float3 c) { p[0] = c.x; p[1] = 
 // Dual vertices of a cell with several patches (rare): crossings of the
 // owner-inside edges accumulated per patch in edge order; a patch with none
 // of them takes all its crossings.
-static __device__ __noinline__ void multi_patch_vertices(const DeviceTables &tab, const float v[8], const Geo &g, float iso,
-                                                  uint32_t cfg, bool lut2, uint32_t niso, uint32_t cm, uint32_t om,
-                                                  float *out, uint32_t &have, float3 &c6, float3 &c9, float3 &c10)
+static __device__ __noinline__ void multi_patch_vertices(const DeviceTables &tab, const float *v, Geo g, float iso,
+                                                         uint32_t cfg, bool lut2, uint32_t niso, uint32_t cm, uint32_t om,
+                                                         float *out)
 {
     float3 acc[4];
     uint32_t cnt[4] = {0, 0, 0, 0};
@@ -273,7 +273,6 @@ static __device__ __noinline__ void multi_patch_vertices(const DeviceTables &tab
         const int e = __ffs(mm) - 1;
         mm &= mm - 1;
         const float3 c = crossing_any(e, v, g, iso);
-        if (e == 6) { c6 = c; have |= 1u; } else if (e == 9) { c9 = c; have |= 2u; } else if (e == 10) { c10 = c; have |= 4u; }
         const uint32_t m = lut_m(tab, cfg, lut2, e);
         acc[m] = cnt[m] ? add3(acc[m], c) : c;
         cnt[m]++;
@@ -323,7 +322,7 @@ __device__ __forceinline__ void cell_vertices(const DeviceTables &tab, const flo
         }
         store3(out, div3(acc, n));
     } else {
-        multi_patch_vertices(tab, v, g, iso, cfg, lut2, niso, cm, om, out, have, c6, c9, c10);
+        multi_patch_vertices(tab, v, g, iso, cfg, lut2, niso, cm, om, out);
     }
     uint32_t k = niso;
     if (info & 1u) { store3(out + 3 * k, (have & 1u) ? c6 : crossing_any(6, v, g, iso)); ++k; }
