@@ -135,7 +135,7 @@ __device__ __noinline__ void load_plane(const T *vol, const PlaneArgs ga, uint32
                 const float4 *q = reinterpret_cast<const float4 *>(base);
                 const uint64_t step = sx / 4;
                 uint32_t a0 = 0, a1 = 0, a2 = 0, a3 = 0, b0 = 0, b1 = 0, b2 = 0, b3 = 0;
-#pragma unroll 8
+#pragma unroll 4
                 for (int r = 0; r < 32; ++r) {
                     const float4 v = __ldg(q + r * step);
                     const uint32_t bit = 1u << r;
@@ -171,7 +171,7 @@ __device__ __noinline__ void load_plane(const T *vol, const PlaneArgs ga, uint32
                 for (int h = 0; h < 3; ++h) {
                     acc[h][0] = acc[h][1] = acc[h][2] = acc[h][3] = 0;
                     const int r0 = 16 * h, n = h < 2 ? 16 : 2;
-#pragma unroll 8
+#pragma unroll 4
                     for (int i = 0; i < n; ++i) {
                         const uint2 w = __ldg(q + (r0 + i) * step);
                         const uint32_t c0 = all_lt ? 0x00010001u : (__vcmpltu2(w.x, tl) & 0x00010001u);
@@ -192,8 +192,9 @@ __device__ __noinline__ void load_plane(const T *vol, const PlaneArgs ga, uint32
                 }
             }
         } else {
+#pragma unroll 1
             for (uint32_t r = 0; r < nrow; ++r) {
-#pragma unroll
+#pragma unroll 1
                 for (int j = 0; j < CPL; ++j) {
                     if (xb + j >= g.pts.x) continue;
                     const float v = load_sample(base, (uint64_t)r * sx + j);
@@ -313,7 +314,7 @@ __device__ __forceinline__ uint32_t cell_cfg(uint32_t p) { return (p >> 21) & 0x
 __device__ __forceinline__ bool cell_l2(uint32_t p) { return (p >> 29) & 1u; }
 
 // List index of active cell (c, r) of the plane stored at parity p.
-__device__ __forceinline__ uint32_t entry_of(const WarpSmem &s, int p, int r, int c)
+__device__ __noinline__ uint32_t entry_of(const WarpSmem &s, int p, int r, int c)
 {
     if (c == W) return s.rowstart[p][r + 1] - 1u;
     const int l = c >> 2, j = c & 3;
@@ -409,6 +410,17 @@ __device__ __forceinline__ uint32_t warp_transpose32(uint32_t x, int lane)
         x = (lane & s) ? ((x & ~lo[i]) | ((y & ~lo[i]) >> s)) : ((x & lo[i]) | ((y & lo[i]) << s));
     }
     return x;
+}
+
+// Quad rings of owned edges 6, 9, 10 (dmc.cu:653-664), one byte per ring slot:
+// bit 0 plane (0: k-1, 1: k), bits 1-2 base entry (0 own, 1 (c,r+1,k-1),
+// 2 (c,r,k), 3 (c,r+1,k)), bit 3 next entry (+x neighbour), bit 4 row + 1.
+constexpr uint32_t kRing6 = 0x121a0800u, kRing9 = 0x080d0500u, kRing10 = 0x05171200u;
+// ring edges: e6 ring 6,7,4,5; e9 ring 9,1,3,11; e10 ring 10,8,0,2
+__device__ __forceinline__ uint32_t ring_edge(int s, int kk)
+{
+    const unsigned long long E = 0x208ab3195476ull;   // 12 nibbles: s*4 + kk
+    return (uint32_t)((E >> (4 * (4 * s + kk))) & 0xfull);
 }
 
 // One sweep kernel for both passes.
@@ -604,40 +616,28 @@ __global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vo
                     const uint32_t e_up = (want & 5u) ? entry_of(S, prv, r + 1, c) : 0u;    // (c, r+1, k-1)
                     const uint32_t e_z = (want & 6u) ? entry_of(S, cur, r, c) : 0u;        // (c, r, k)
                     const uint32_t e_zup = (want & 4u) ? entry_of(S, cur, r + 1, c) : 0u;  // (c, r+1, k)
-#pragma unroll
+                    // ring slot = plane (0 k-1, 1 k) | base (0 own entry, 1 (c,r+1,k-1),
+                    // 2 (c,r,k), 3 (c,r+1,k)) | +1 (next entry: c+1) | dr | ring edge
                     for (int s = 0; s < 3; ++s) {
                         if (!(want & (1u << s))) continue;
                         if (q >= out.qcap) { atomicOr(err, DEV_ERR_OVERFLOW); break; }
-                        uint32_t ri[4]; int rp[4], rr[4], rc[4], re[4];
-                        if (s == 0) {
-                            rp[0] = prv; ri[0] = i;        rr[0] = r;     rc[0] = c;     re[0] = 6;
-                            rp[1] = prv; ri[1] = i + 1;    rr[1] = r;     rc[1] = c + 1; re[1] = 7;
-                            rp[2] = prv; ri[2] = e_up + 1; rr[2] = r + 1; rc[2] = c + 1; re[2] = 4;
-                            rp[3] = prv; ri[3] = e_up;     rr[3] = r + 1; rc[3] = c;     re[3] = 5;
-                        } else if (s == 1) {
-                            rp[0] = prv; ri[0] = i;        rr[0] = r;     rc[0] = c;     re[0] = 9;
-                            rp[1] = cur; ri[1] = e_z;      rr[1] = r;     rc[1] = c;     re[1] = 1;
-                            rp[2] = cur; ri[2] = e_z + 1;  rr[2] = r;     rc[2] = c + 1; re[2] = 3;
-                            rp[3] = prv; ri[3] = i + 1;    rr[3] = r;     rc[3] = c + 1; re[3] = 11;
-                        } else {
-                            rp[0] = prv; ri[0] = i;        rr[0] = r;     rc[0] = c;     re[0] = 10;
-                            rp[1] = prv; ri[1] = e_up;     rr[1] = r + 1; rc[1] = c;     re[1] = 8;
-                            rp[2] = cur; ri[2] = e_zup;    rr[2] = r + 1; rc[2] = c;     re[2] = 0;
-                            rp[3] = cur; ri[3] = e_z;      rr[3] = r;     rc[3] = c;     re[3] = 2;
-                        }
+                        const uint32_t ring = s == 0 ? kRing6 : (s == 1 ? kRing9 : kRing10);
                         const bool ccw = (info >> (s + 3)) & 1u;
                         uint32_t idx[4];
-#pragma unroll
+#pragma unroll 1
                         for (int it = 0; it < 4; ++it) {
-                            // ccw visits ring slots 0,1,2,3, cw 0,3,2,1 (dmc.cu:1636-1645)
-                            const int kk = ccw ? it : (4 - it) & 3;
-                            const int pl = rp[kk];
-                            const uint32_t li = ri[kk];
+                            const int kk = ccw ? it : (4 - it) & 3;    // ccw 0,1,2,3; cw 0,3,2,1 (dmc.cu:1636-1645)
+                            const uint32_t sl = (ring >> (8 * kk)) & 0xffu;
+                            const int pl = (sl & 1u) ? cur : prv;
+                            const uint32_t bsel = (sl >> 1) & 3u;
+                            const uint32_t plus = (sl >> 3) & 1u, dr = (sl >> 4) & 1u;
+                            const uint32_t li = (bsel == 0 ? i : bsel == 1 ? e_up : bsel == 2 ? e_z : e_zup) + plus;
+                            const uint32_t re = ring_edge(s, kk);
                             if (li >= S.rowstart[pl][HROWS]) { atomicOr(err, DEV_ERR_BOUNDS); idx[it] = 0; continue; }
                             const uint32_t rd = M.ent(pl, li);
-                            uint32_t m = lut_m(tab, cell_cfg(rd), cell_l2(rd), re[kk]);
+                            uint32_t m = lut_m(tab, cell_cfg(rd), cell_l2(rd), (int)re);
                             if (m == 0xffu) { atomicOr(err, DEV_ERR_BOUNDS); m = 0; }
-                            idx[it] = S.segv[pl][rr[kk]][rc[kk] == W ? 1 : 0] + cell_vrel(rd) + m;
+                            idx[it] = S.segv[pl][r + dr][(c + (int)plus) == W ? 1 : 0] + cell_vrel(rd) + m;
                         }
                         reinterpret_cast<uint4 *>(out.quads)[q] = make_uint4(idx[0], idx[1], idx[2], idx[3]);
                         if (out.tris) {

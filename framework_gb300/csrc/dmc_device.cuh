@@ -295,8 +295,8 @@ static __device__ __noinline__ void multi_patch_vertices(const DeviceTables &tab
 
 // All vertices of an active cell, written to out: the niso dual vertices,
 // then the crossings of its own edges 6, 9, 10 flagged in info (bits 0-2).
-// Same values as dual_vertices + owned_edge_vertices, but only the crossed
-// edges are evaluated, each once.
+// Same values as dual_vertices + owned_edge_vertices; each needed crossing
+// is evaluated once, at a single call site (keeps the kernel small).
 __device__ __forceinline__ void cell_vertices(const DeviceTables &tab, const float v[8], const Geo &g, float iso,
                                               uint32_t cfg, bool lut2, uint32_t niso, uint32_t info,
                                               uint32_t x, uint32_t y, uint32_t z, float *out)
@@ -306,28 +306,27 @@ __device__ __forceinline__ void cell_vertices(const DeviceTables &tab, const flo
     if (x == 0) om &= ~0x898u;             // edges 3, 4, 7, 11 are owned at -x
     if (y == 0) om &= ~0x131u;             // edges 0, 4, 5, 8 are owned at -y
     if (z == 0) om &= ~0x00fu;             // edges 0, 1, 2, 3 are owned at -z
-    float3 c6 = make_float3(0.f, 0.f, 0.f), c9 = c6, c10 = c6;
-    uint32_t have = 0;                     // bit 0/1/2: c6/c9/c10 computed
-    if (niso == 1) {
-        uint32_t mm = om ? om : cm;
-        float3 acc = make_float3(0.f, 0.f, 0.f);
-        uint32_t n = 0;
-        while (mm) {
-            const int e = __ffs(mm) - 1;
-            mm &= mm - 1;
-            const float3 c = crossing_any(e, v, g, iso);
-            if (e == 6) { c6 = c; have |= 1u; } else if (e == 9) { c9 = c; have |= 2u; } else if (e == 10) { c10 = c; have |= 4u; }
-            acc = n ? add3(acc, c) : c;
-            ++n;
-        }
-        store3(out, div3(acc, n));
-    } else {
-        multi_patch_vertices(tab, v, g, iso, cfg, lut2, niso, cm, om, out);
+    // edges of the single patch that enter the mean, and owned edges whose
+    // crossing is emitted
+    const uint32_t dual = niso == 1 ? (om ? om : cm) : 0u;
+    const uint32_t owned = ((info & 1u) << 6) | ((info & 2u) << 8) | ((info & 4u) << 8);
+    float3 acc = make_float3(0.f, 0.f, 0.f), c6 = acc, c9 = acc, c10 = acc;
+    uint32_t n = 0, mm = dual | owned;
+    while (mm) {
+        const int e = __ffs(mm) - 1;
+        mm &= mm - 1;
+        const float3 c = crossing_any(e, v, g, iso);
+        if ((dual >> e) & 1u) { acc = n ? add3(acc, c) : c; ++n; }
+        if (e == 6) c6 = c;
+        if (e == 9) c9 = c;
+        if (e == 10) c10 = c;
     }
+    if (niso == 1) store3(out, div3(acc, n));
+    else multi_patch_vertices(tab, v, g, iso, cfg, lut2, niso, cm, om, out);
     uint32_t k = niso;
-    if (info & 1u) { store3(out + 3 * k, (have & 1u) ? c6 : crossing_any(6, v, g, iso)); ++k; }
-    if (info & 2u) { store3(out + 3 * k, (have & 2u) ? c9 : crossing_any(9, v, g, iso)); ++k; }
-    if (info & 4u) { store3(out + 3 * k, (have & 4u) ? c10 : crossing_any(10, v, g, iso)); ++k; }
+    if (info & 1u) { store3(out + 3 * k, c6); ++k; }
+    if (info & 2u) { store3(out + 3 * k, c9); ++k; }
+    if (info & 4u) { store3(out + 3 * k, c10); ++k; }
 }
 
 // Device-side error codes (written with atomicOr to ctx error word).
