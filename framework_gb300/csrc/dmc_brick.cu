@@ -181,15 +181,14 @@ __device__ __noinline__ void load_plane(const T *vol, const PlaneArgs ga, uint32
                         acc[h][0] |= c0 << i; acc[h][1] |= c1 << i; acc[h][2] |= d0 << i; acc[h][3] |= d1 << i;
                     }
                 }
-#pragma unroll
-                for (int t = 0; t < 2; ++t) {        // t = 0: lt, 1: le
-                    uint64_t *dst = t ? le : lt;
-                    const uint32_t *a = &acc[0][2 * t], *b = &acc[1][2 * t], *hh = &acc[2][2 * t];
-                    dst[0] = spread16(a[0], b[0], false) | ((uint64_t)(hh[0] & 3u) << 32);
-                    dst[1] = spread16(a[0], b[0], true) | ((uint64_t)((hh[0] >> 16) & 3u) << 32);
-                    dst[2] = spread16(a[1], b[1], false) | ((uint64_t)(hh[1] & 3u) << 32);
-                    dst[3] = spread16(a[1], b[1], true) | ((uint64_t)((hh[1] >> 16) & 3u) << 32);
-                }
+                lt[0] = spread16(acc[0][0], acc[1][0], false) | ((uint64_t)(acc[2][0] & 3u) << 32);
+                lt[1] = spread16(acc[0][0], acc[1][0], true) | ((uint64_t)((acc[2][0] >> 16) & 3u) << 32);
+                lt[2] = spread16(acc[0][1], acc[1][1], false) | ((uint64_t)(acc[2][1] & 3u) << 32);
+                lt[3] = spread16(acc[0][1], acc[1][1], true) | ((uint64_t)((acc[2][1] >> 16) & 3u) << 32);
+                le[0] = spread16(acc[0][2], acc[1][2], false) | ((uint64_t)(acc[2][2] & 3u) << 32);
+                le[1] = spread16(acc[0][2], acc[1][2], true) | ((uint64_t)((acc[2][2] >> 16) & 3u) << 32);
+                le[2] = spread16(acc[0][3], acc[1][3], false) | ((uint64_t)(acc[2][3] & 3u) << 32);
+                le[3] = spread16(acc[0][3], acc[1][3], true) | ((uint64_t)((acc[2][3] >> 16) & 3u) << 32);
             }
         } else {
 #pragma unroll 1
@@ -624,7 +623,7 @@ __global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vo
                         const uint32_t ring = s == 0 ? kRing6 : (s == 1 ? kRing9 : kRing10);
                         const bool ccw = (info >> (s + 3)) & 1u;
                         uint32_t idx[4];
-#pragma unroll 1
+#pragma unroll
                         for (int it = 0; it < 4; ++it) {
                             const int kk = ccw ? it : (4 - it) & 3;    // ccw 0,1,2,3; cw 0,3,2,1 (dmc.cu:1636-1645)
                             const uint32_t sl = (ring >> (8 * kk)) & 0xffu;

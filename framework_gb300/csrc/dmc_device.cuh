@@ -262,10 +262,13 @@ __device__ __forceinline__ void store3(float *p, float3 c) { p[0] = c.x; p[1] = 
 // Dual vertices of a cell with several patches (rare): crossings of the
 // owner-inside edges accumulated per patch in edge order; a patch with none
 // of them takes all its crossings.
-static __device__ __noinline__ void multi_patch_vertices(const DeviceTables &tab, const float *v, Geo g, float iso,
+struct Corners { float v[8]; };
+
+static __device__ __noinline__ void multi_patch_vertices(const DeviceTables &tab, const Corners cv, Geo g, float iso,
                                                          uint32_t cfg, bool lut2, uint32_t niso, uint32_t cm, uint32_t om,
                                                          float *out)
 {
+    const float *v = cv.v;
     float3 acc[4];
     uint32_t cnt[4] = {0, 0, 0, 0};
     uint32_t mm = om;
@@ -322,7 +325,12 @@ __device__ __forceinline__ void cell_vertices(const DeviceTables &tab, const flo
         if (e == 10) c10 = c;
     }
     if (niso == 1) store3(out, div3(acc, n));
-    else multi_patch_vertices(tab, v, g, iso, cfg, lut2, niso, cm, om, out);
+    else {
+        Corners cv;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) cv.v[i] = v[i];
+        multi_patch_vertices(tab, cv, g, iso, cfg, lut2, niso, cm, om, out);
+    }
     uint32_t k = niso;
     if (info & 1u) { store3(out + 3 * k, c6); ++k; }
     if (info & 2u) { store3(out + 3 * k, c9); ++k; }
