@@ -79,9 +79,21 @@ struct Spill {                          // per warp slot, global memory
 struct WarpMem {
     WarpSmem *s;
     Spill *g;
-    __device__ __forceinline__ uint32_t &ent(int p, uint32_t i) { return i < CAP ? s->ent[p][i] : g->ent[p][i - CAP]; }
-    __device__ __forceinline__ uint16_t &lst(int p, uint32_t i) { return i < CAP ? s->lst[p][i] : g->lst[p][i - CAP]; }
-    __device__ __forceinline__ uint8_t &info(int p, uint32_t i) { return i < CAP ? s->info[p][i] : g->info[p][i - CAP]; }
+    __device__ __forceinline__ uint32_t &ent(int p, uint32_t i)
+    {
+        uint32_t *b = i < CAP ? s->ent[p] : g->ent[p] - CAP;
+        return b[i];
+    }
+    __device__ __forceinline__ uint16_t &lst(int p, uint32_t i)
+    {
+        uint16_t *b = i < CAP ? s->lst[p] : g->lst[p] - CAP;
+        return b[i];
+    }
+    __device__ __forceinline__ uint8_t &info(int p, uint32_t i)
+    {
+        uint8_t *b = i < CAP ? s->info[p] : g->info[p] - CAP;
+        return b[i];
+    }
 };
 
 __device__ __forceinline__ uint64_t seg_index(const Geom &g, uint32_t k, uint32_t j, uint32_t xs)
@@ -118,6 +130,21 @@ __device__ __forceinline__ float sample_p(const T *vol, uint3 pts, uint32_t x, u
     return load_sample(vol, ((uint64_t)z * pts.y + y) * pts.x + x);
 }
 
+// Masks of a lane's columns one sample at a time: the volume's right edge,
+// or rows that are not aligned for vector loads.
+template <class T>
+__device__ __noinline__ void load_columns_scalar(const T *base, uint64_t sx, uint32_t nrow, uint32_t ncol, float iso,
+                                                 uint64_t *lt, uint64_t *le)
+{
+    for (uint32_t r = 0; r < nrow; ++r) {
+        for (uint32_t j = 0; j < CPL && j < ncol; ++j) {
+            const float v = load_sample(base, (uint64_t)r * sx + j);
+            if (v < iso) lt[j] |= 1ull << r;
+            if (v <= iso) le[j] |= 1ull << r;
+        }
+    }
+}
+
 template <class T, bool VEC>
 __device__ __noinline__ void load_plane(const T *vol, const PlaneArgs ga, uint32_t x0, uint32_t y0, uint32_t p,
                                         PlaneMasks &m, int lane)
@@ -135,7 +162,7 @@ __device__ __noinline__ void load_plane(const T *vol, const PlaneArgs ga, uint32
                 const float4 *q = reinterpret_cast<const float4 *>(base);
                 const uint64_t step = sx / 4;
                 uint32_t a0 = 0, a1 = 0, a2 = 0, a3 = 0, b0 = 0, b1 = 0, b2 = 0, b3 = 0;
-#pragma unroll 4
+#pragma unroll 2
                 for (int r = 0; r < 32; ++r) {
                     const float4 v = __ldg(q + r * step);
                     const uint32_t bit = 1u << r;
@@ -171,7 +198,7 @@ __device__ __noinline__ void load_plane(const T *vol, const PlaneArgs ga, uint32
                 for (int h = 0; h < 3; ++h) {
                     acc[h][0] = acc[h][1] = acc[h][2] = acc[h][3] = 0;
                     const int r0 = 16 * h, n = h < 2 ? 16 : 2;
-#pragma unroll 4
+#pragma unroll 2
                     for (int i = 0; i < n; ++i) {
                         const uint2 w = __ldg(q + (r0 + i) * step);
                         const uint32_t c0 = all_lt ? 0x00010001u : (__vcmpltu2(w.x, tl) & 0x00010001u);
@@ -191,16 +218,7 @@ __device__ __noinline__ void load_plane(const T *vol, const PlaneArgs ga, uint32
                 le[3] = spread16(acc[0][3], acc[1][3], true) | ((uint64_t)((acc[2][3] >> 16) & 3u) << 32);
             }
         } else {
-#pragma unroll 1
-            for (uint32_t r = 0; r < nrow; ++r) {
-#pragma unroll 1
-                for (int j = 0; j < CPL; ++j) {
-                    if (xb + j >= g.pts.x) continue;
-                    const float v = load_sample(base, (uint64_t)r * sx + j);
-                    if (v < g.iso) lt[j] |= 1ull << r;
-                    if (v <= g.iso) le[j] |= 1ull << r;
-                }
-            }
+            load_columns_scalar(base, sx, nrow, g.pts.x - xb, g.iso, lt, le);
         }
     }
 #pragma unroll
@@ -617,6 +635,7 @@ __global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vo
                     const uint32_t e_zup = (want & 4u) ? entry_of(S, cur, r + 1, c) : 0u;  // (c, r+1, k)
                     // ring slot = plane (0 k-1, 1 k) | base (0 own entry, 1 (c,r+1,k-1),
                     // 2 (c,r,k), 3 (c,r+1,k)) | +1 (next entry: c+1) | dr | ring edge
+#pragma unroll 1
                     for (int s = 0; s < 3; ++s) {
                         if (!(want & (1u << s))) continue;
                         if (q >= out.qcap) { atomicOr(err, DEV_ERR_OVERFLOW); break; }

@@ -249,12 +249,15 @@ __device__ __forceinline__ float3 add3(float3 a, float3 b)
 // for n = 1, 2, 4, 8 (same rounded result).
 __device__ __forceinline__ float3 div3(float3 a, uint32_t n)
 {
-    if ((n & (n - 1)) == 0) {
+    if (n == 1 || n == 2 || n == 4 || n == 8) {
         const float r = n == 1 ? 1.f : (n == 2 ? 0.5f : (n == 4 ? 0.25f : 0.125f));
-        if (n <= 8) return make_float3(__fmul_rn(a.x, r), __fmul_rn(a.y, r), __fmul_rn(a.z, r));
+        return make_float3(__fmul_rn(a.x, r), __fmul_rn(a.y, r), __fmul_rn(a.z, r));
     }
     const float d = __uint2float_rn(n);
-    return make_float3(__fdiv_rn(a.x, d), __fdiv_rn(a.y, d), __fdiv_rn(a.z, d));
+    float c[3] = {a.x, a.y, a.z};
+#pragma unroll 1
+    for (int i = 0; i < 3; ++i) c[i] = __fdiv_rn(c[i], d);
+    return make_float3(c[0], c[1], c[2]);
 }
 
 __device__ __forceinline__ void store3(float *p, float3 c) { p[0] = c.x; p[1] = c.y; p[2] = c.z; }
