@@ -119,12 +119,12 @@ static dmc_status finish(dmc_ctx *ctx, cudaStream_t st)
     float ms = 0.f;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
     c->stats.device_ms = ms;
-    if (c->evk_used) {
+    if (c->evk_used >= 1) {
         cudaEventElapsedTime(&c->stats.count_ms, c->evk[0], c->evk[1]);
         cudaEventElapsedTime(&c->stats.scan_ms, c->evk[1], c->evk[2]);
-        cudaEventElapsedTime(&c->stats.emit_ms, c->evk[3], c->evk[4]);
-        c->evk_used = false;
     }
+    if (c->evk_used >= 2) cudaEventElapsedTime(&c->stats.emit_ms, c->evk[3], c->evk[4]);
+    c->evk_used = 0;
     uint32_t err = c->h_ctl->err;
     if (err & DEV_ERR_TIMEOUT) return DMC_ERR_TIMEOUT;
     if (err & DEV_ERR_OVERFLOW) return DMC_ERR_OUTPUT_OVERFLOW;

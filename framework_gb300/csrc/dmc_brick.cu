@@ -809,7 +809,7 @@ static dmc_status brick_run_v(Ctx *ctx, const T *vol, const ExtractArgs &a, cuda
     CUDA_TRY(cudaMemsetAsync(tickets, 0, 256, st));
     CUDA_TRY(cudaMemsetAsync(ctx->d_ctl, 0, sizeof(DevCtl), st));
     coord_table<<<(unsigned)((n_coord + 255) / 256), 256, 0, st>>>(coord, a.pts, a.cells, a.rng, a.mn);
-    ctx->evk_used = false;
+    ctx->evk_used = 0;
     CUDA_TRY(cudaEventRecord(ctx->evk[0], st));
     brick_sweep<T, VEC, false><<<grid, 32 * NWB, kSweepSmem, st>>>(vol, g, ctx->d_tab, seg_cnt, EmitOut{}, spill,
                                                                     &tickets[0], ctx->d_ctl->counters, &ctx->d_ctl->err);
@@ -821,6 +821,7 @@ static dmc_status brick_run_v(Ctx *ctx, const T *vol, const ExtractArgs &a, cuda
     seg_scan<<<n_tiles, SCAN_NT, 0, st>>>(seg_cnt, nseg, ctl, seg_off);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaEventRecord(ctx->evk[2], st));
+    ctx->evk_used = 1;
     CUDA_TRY(cudaMemcpyAsync(ctx->h_ctl, ctx->d_ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
     if (ctx->h_ctl->err & DEV_ERR_TIMEOUT) return DMC_ERR_TIMEOUT;
@@ -839,7 +840,7 @@ static dmc_status brick_run_v(Ctx *ctx, const T *vol, const ExtractArgs &a, cuda
                                                                    ctx->d_ctl->counters, &ctx->d_ctl->err);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaEventRecord(ctx->evk[4], st));
-    ctx->evk_used = true;
+    ctx->evk_used = 2;
     return DMC_OK;
 }
 

@@ -34,7 +34,7 @@ struct Ctx {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t evk[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};   // per-kernel timing (brick path)
-    bool evk_used = false;
+    int evk_used = 0;                   // 1: count and scan timed, 2: emit timed too
     void *scratch = nullptr;           // grow-only device scratch
     size_t scratch_bytes = 0;
     DevCtl *d_ctl = nullptr;
