@@ -1,22 +1,23 @@
 // Brick path: persistent warps sweep bricks of the volume along z.
 //
-// A brick is 128 cell columns x 32 cell rows x ZC planes and belongs to one
-// warp; each lane owns 4 consecutive columns and reads them with one vector
-// load per row (float4 / 4 x uint16), so every warp load is a contiguous,
-// coalesced run.  For every point plane a lane keeps one bit per sample,
-// "below the isovalue", in a 64-bit mask per column (rows 0..33).  A cell's
+// A brick is 128 cell columns x 32 cell rows x a run of z planes and belongs
+// to one warp.  Lane l owns columns l, l+32, l+64, l+96: every warp load is a
+// contiguous 32-sample run of one row, and loads are issued 32 at a time per
+// lane.  For every point plane a lane keeps one bit per sample, "below the
+// isovalue", in a 64-bit mask per column (rows 0..33).  A cell's
 // configuration is a few shifts on the masks of two columns in two planes,
-// and activity for all rows of a column is ~12 bitwise operations, so only
-// active cells (a few percent) take the per-cell path.  Warps never wait for
-// each other: there is no block-level barrier anywhere.
+// and activity for all rows of a column takes ~12 bitwise operations, so only
+// active cells (a few percent) take the per-cell path.  A 32x32 bit transpose
+// turns the column masks into each row's active cells in x order.  Warps never
+// wait for each other: there is no block-level barrier in the sweep.
 //
 // Output order is the reference's (ascending cell index, x fastest,
 // utils.hpp:72), so the active cells of one plane, row and 128-column
 // segment form one contiguous output range, a "segment" (k, j, xs).
 //   count sweep : per segment (vertices, quads)
 //   scan        : decoupled look-back over segments -> offsets
-//   emit sweep  : ranks the active cells of each row (4 ballots per row),
-//                 writes vertex positions and quads at their final places.
+//   emit sweep  : ranks the active cells of each row, writes vertex positions
+//                 and quads at their final places.
 // Quads reference the dual vertices of the +x, +y, +z neighbours
 // (dmc.cu:1636-1664): the emit sweep also ranks the first cell column of the
 // next segment (its vertices start at that segment's offset) and the first
@@ -30,14 +31,15 @@ namespace dmc {
 
 namespace brick {
 
-constexpr int CPL = 4;                    // columns per lane
-constexpr int W = 32 * CPL;               // cell columns per brick (= segment width)
+constexpr int GROUPS = 4;                 // columns per lane, 32 apart
+constexpr int W = 32 * GROUPS;            // cell columns per brick (= segment width)
 constexpr int ROWS = 32;                  // own cell rows
 constexpr int HROWS = ROWS + 1;           // with the halo row
 constexpr int MAXL = HROWS * (W + 1);     // most active cells one plane of a brick can hold
 constexpr int CAP = 320;                  // entries kept in shared memory per plane
 constexpr int OVF = MAXL - CAP;           // entries per plane that spill to global scratch
 constexpr int NWB = 8;                    // warps per block (independent)
+constexpr int QBUF = 96;                  // quads of one round of owner cells (3 per cell)
 constexpr int SCAN_NT = 256, SCAN_ITEMS = 8, SCAN_TILE = SCAN_NT * SCAN_ITEMS;
 
 struct Geom {
@@ -46,29 +48,29 @@ struct Geom {
     uint64_t nbricks;
     float iso;
     uint32_t iso_u16;      // uint16 samples: v < iso  <=>  v < iso_u16 (65536: always)
-    uint32_t isole_u16;    // uint16 samples: v <= iso <=>  v < isole_u16
     float3 mn, rng;
     const float *coord;    // point coordinates: x[0..cx], y[0..cy], z[0..cz]
 };
 
-struct PlaneMasks {
-    uint64_t lt[W + 2];                // bit r: sample (x0+c, y0+r) < iso
-    uint64_t le[W + 2];                // bit r: sample <= iso
-};
-
 struct WarpSmem {
-    PlaneMasks mask[2];                // point planes by parity
-    uint32_t ball[2][HROWS][CPL];      // per row, per column-in-lane: active lanes
+    uint64_t mask[2][W + 2];           // column masks of point planes (by parity): bit r = row r below iso
+    uint32_t xrow[2][HROWS][GROUPS];   // per row: active cells in x order, word q = columns 32q..32q+31
     uint64_t hact[2];                  // halo column activity (bit = row)
     uint16_t rowstart[2][HROWS + 1];   // first list entry of each row
     uint32_t rowbase[HROWS];           // running (v | q << 16) prefix at each row start
+    uint32_t rowtot[ROWS];             // count sweep: per-row (v | q << 16)
     uint32_t segv[2][HROWS][2];        // vertex offset of (row, own / next segment)
     uint32_t segq[2][HROWS];           // quad offset of (row, own segment)
-    uint32_t rowtot[ROWS];             // count sweep: per-row (v | q << 16)
+    uint32_t qwork[QBUF];              // quads of one round: entry | edge << 16 | wanted edges << 18
     uint32_t ent[2][CAP];              // packed cell: vrel 11 | qrel 10 | cfg 8 | lut2 1
     uint16_t lst[2][CAP];              // row << 8 | col
     uint8_t info[2][CAP];              // own-edge bipolar/ccw bits
 };
+
+static_assert(sizeof(WarpSmem) % 16 == 0, "per-warp shared memory must keep 16-byte alignment");
+
+// shared memory layout of a sweep block: tables, then one WarpSmem per warp
+constexpr size_t kTablesBytes = (sizeof(DeviceTables) + 127) & ~(size_t)127;
 
 struct Spill {                          // per warp slot, global memory
     uint32_t ent[2][OVF];
@@ -107,138 +109,89 @@ __device__ __forceinline__ float sample_at(const T *vol, const Geom &g, uint32_t
     return load_sample(vol, ((uint64_t)z * g.pts.y + y) * g.pts.x + x);
 }
 
-__device__ __forceinline__ bool below_u16(uint32_t v, uint32_t thr) { return v < thr; }
-
-// Column masks of point plane p: bit r of column c = sample (x0+c, y0+r, p)
-// below (lt) / at or below (le) the isovalue, rows 0..33, columns 0..W+1.
-// Samples outside the volume read as 0; cells touching them are never active.
-__device__ __forceinline__ uint32_t spread16(uint32_t a, uint32_t b, bool upper)
-{
-    // a holds rows 0..15 of two columns (low/high halfword), b rows 16..31
-    return upper ? ((a >> 16) | (b & 0xffff0000u)) : ((a & 0xffffu) | (b << 16));
-}
-
-struct PlaneArgs {
-    uint3 pts;
-    float iso;
-    uint32_t thr_lt, thr_le;   // uint16 thresholds (see Geom)
-};
-
 template <class T>
 __device__ __forceinline__ float sample_p(const T *vol, uint3 pts, uint32_t x, uint32_t y, uint32_t z)
 {
     return load_sample(vol, ((uint64_t)z * pts.y + y) * pts.x + x);
 }
 
-// Masks of a lane's columns one sample at a time: the volume's right edge,
-// or rows that are not aligned for vector loads.
-template <class T>
-__device__ __noinline__ void load_columns_scalar(const T *base, uint64_t sx, uint32_t nrow, uint32_t ncol, float iso,
-                                                 uint64_t *lt, uint64_t *le)
-{
-    for (uint32_t r = 0; r < nrow; ++r) {
-        for (uint32_t j = 0; j < CPL && j < ncol; ++j) {
-            const float v = load_sample(base, (uint64_t)r * sx + j);
-            if (v < iso) lt[j] |= 1ull << r;
-            if (v <= iso) le[j] |= 1ull << r;
-        }
-    }
-}
+// "below the isovalue" for a raw sample: float compare, or for uint16 the
+// equivalent integer compare against the precomputed threshold
+__device__ __forceinline__ uint32_t below(float v, float iso, uint32_t) { return v < iso ? 1u : 0u; }
+__device__ __forceinline__ uint32_t below(uint16_t v, float, uint32_t thr) { return (uint32_t)v < thr ? 1u : 0u; }
 
-template <class T, bool VEC>
-__device__ __noinline__ void load_plane(const T *vol, const PlaneArgs ga, uint32_t x0, uint32_t y0, uint32_t p,
-                                        PlaneMasks &m, int lane)
+template <class T>
+__device__ __forceinline__ T raw_load(const T *p) { return __ldg(p); }
+
+// Column masks of point plane p for the lane's columns x0+lane+32j and the two
+// halo columns x0+W, x0+W+1: bit r = sample (x, y0+r, p) below the isovalue,
+// rows 0..33.  Samples outside the volume read as 0 (their cells are never
+// active).  Loads go out 32 per lane before their results are used, and the
+// next plane's rows are prefetched into L2.
+template <class T>
+__device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint32_t thr, uint32_t x0, uint32_t y0,
+                                        uint32_t p, uint64_t *m, int lane)
 {
-    struct { uint3 pts; float iso; uint32_t iso_u16, isole_u16; } g = {ga.pts, ga.iso, ga.thr_lt, ga.thr_le};
-    uint64_t lt[CPL] = {0, 0, 0, 0}, le[CPL] = {0, 0, 0, 0};
-    const uint32_t xb = x0 + CPL * lane;
-    const bool pz = p < g.pts.z;
-    if (pz && xb < g.pts.x) {
-        const uint64_t sx = g.pts.x;
-        const T *base = vol + ((uint64_t)p * g.pts.y + y0) * sx + xb;
-        const uint32_t nrow = min(34u, g.pts.y - y0);
-        if (VEC && nrow == 34 && xb + CPL <= g.pts.x) {
-            if constexpr (sizeof(T) == 4) {
-                const float4 *q = reinterpret_cast<const float4 *>(base);
-                const uint64_t step = sx / 4;
-                uint32_t a0 = 0, a1 = 0, a2 = 0, a3 = 0, b0 = 0, b1 = 0, b2 = 0, b3 = 0;
-#pragma unroll 2
-                for (int r = 0; r < 32; ++r) {
-                    const float4 v = __ldg(q + r * step);
-                    const uint32_t bit = 1u << r;
-                    a0 |= v.x < g.iso ? bit : 0u; a1 |= v.y < g.iso ? bit : 0u;
-                    a2 |= v.z < g.iso ? bit : 0u; a3 |= v.w < g.iso ? bit : 0u;
-                    b0 |= v.x <= g.iso ? bit : 0u; b1 |= v.y <= g.iso ? bit : 0u;
-                    b2 |= v.z <= g.iso ? bit : 0u; b3 |= v.w <= g.iso ? bit : 0u;
-                }
-                uint32_t h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    uint32_t lo[GROUPS] = {0, 0, 0, 0}, hi[GROUPS] = {0, 0, 0, 0};
+    const bool pz = p < pts.z;
+    const uint32_t nrow = pz ? min(34u, pts.y - y0) : 0u;
+    const uint64_t sx = pts.x;
+    const uint64_t plane0 = (uint64_t)p * pts.y;
+    const T *base = vol + (plane0 + y0) * sx + x0 + lane;
+    if (p + 1 < pts.z && (uint32_t)lane < nrow) {
+        // next plane, this lane's row: every line of the brick's columns
+        const char *nxt = reinterpret_cast<const char *>(vol + (plane0 + pts.y + y0 + lane) * sx + x0);
+        const uint32_t bytes = min((uint32_t)(W + 2), pts.x - x0) * (uint32_t)sizeof(T);
+        for (uint32_t o = 0; o < bytes; o += 128) asm volatile("prefetch.global.L2 [%0];" ::"l"(nxt + o));
+    }
+    bool cok[GROUPS];
 #pragma unroll
-                for (int r = 0; r < 2; ++r) {
-                    const float4 v = __ldg(q + (32 + r) * step);
-                    const uint32_t bit = 1u << r;
-                    h[0] |= v.x < g.iso ? bit : 0u; h[1] |= v.y < g.iso ? bit : 0u;
-                    h[2] |= v.z < g.iso ? bit : 0u; h[3] |= v.w < g.iso ? bit : 0u;
-                    h[4] |= v.x <= g.iso ? bit : 0u; h[5] |= v.y <= g.iso ? bit : 0u;
-                    h[6] |= v.z <= g.iso ? bit : 0u; h[7] |= v.w <= g.iso ? bit : 0u;
-                }
-                lt[0] = a0 | ((uint64_t)h[0] << 32); lt[1] = a1 | ((uint64_t)h[1] << 32);
-                lt[2] = a2 | ((uint64_t)h[2] << 32); lt[3] = a3 | ((uint64_t)h[3] << 32);
-                le[0] = b0 | ((uint64_t)h[4] << 32); le[1] = b1 | ((uint64_t)h[5] << 32);
-                le[2] = b2 | ((uint64_t)h[6] << 32); le[3] = b3 | ((uint64_t)h[7] << 32);
-            } else {
-                // two samples per 32-bit word, per-halfword compares: rows
-                // 0..15 of columns (0,1) accumulate in one word, (2,3) in another
-                const bool all_lt = g.iso_u16 > 0xffffu, all_le = g.isole_u16 > 0xffffu;
-                const uint32_t tl = all_lt ? 0u : (g.iso_u16 | (g.iso_u16 << 16));
-                const uint32_t te = all_le ? 0u : (g.isole_u16 | (g.isole_u16 << 16));
-                const uint2 *q = reinterpret_cast<const uint2 *>(base);
-                const uint64_t step = sx / 4;
-                uint32_t acc[3][4];   // [rows 0-15, 16-31, 32-33][lt01, lt23, le01, le23]
+    for (int j = 0; j < GROUPS; ++j) cok[j] = x0 + lane + 32 * j < pts.x;
+    const bool full = cok[GROUPS - 1] && nrow == 34;
+    if (full) {
+#pragma unroll 1
+        for (int r0 = 0; r0 < 32; r0 += 8) {
+            T v[8][GROUPS];
 #pragma unroll
-                for (int h = 0; h < 3; ++h) {
-                    acc[h][0] = acc[h][1] = acc[h][2] = acc[h][3] = 0;
-                    const int r0 = 16 * h, n = h < 2 ? 16 : 2;
-#pragma unroll 2
-                    for (int i = 0; i < n; ++i) {
-                        const uint2 w = __ldg(q + (r0 + i) * step);
-                        const uint32_t c0 = all_lt ? 0x00010001u : (__vcmpltu2(w.x, tl) & 0x00010001u);
-                        const uint32_t c1 = all_lt ? 0x00010001u : (__vcmpltu2(w.y, tl) & 0x00010001u);
-                        const uint32_t d0 = all_le ? 0x00010001u : (__vcmpltu2(w.x, te) & 0x00010001u);
-                        const uint32_t d1 = all_le ? 0x00010001u : (__vcmpltu2(w.y, te) & 0x00010001u);
-                        acc[h][0] |= c0 << i; acc[h][1] |= c1 << i; acc[h][2] |= d0 << i; acc[h][3] |= d1 << i;
-                    }
-                }
-                lt[0] = spread16(acc[0][0], acc[1][0], false) | ((uint64_t)(acc[2][0] & 3u) << 32);
-                lt[1] = spread16(acc[0][0], acc[1][0], true) | ((uint64_t)((acc[2][0] >> 16) & 3u) << 32);
-                lt[2] = spread16(acc[0][1], acc[1][1], false) | ((uint64_t)(acc[2][1] & 3u) << 32);
-                lt[3] = spread16(acc[0][1], acc[1][1], true) | ((uint64_t)((acc[2][1] >> 16) & 3u) << 32);
-                le[0] = spread16(acc[0][2], acc[1][2], false) | ((uint64_t)(acc[2][2] & 3u) << 32);
-                le[1] = spread16(acc[0][2], acc[1][2], true) | ((uint64_t)((acc[2][2] >> 16) & 3u) << 32);
-                le[2] = spread16(acc[0][3], acc[1][3], false) | ((uint64_t)(acc[2][3] & 3u) << 32);
-                le[3] = spread16(acc[0][3], acc[1][3], true) | ((uint64_t)((acc[2][3] >> 16) & 3u) << 32);
+            for (int i = 0; i < 8; ++i) {
+                const T *row = base + (uint64_t)(r0 + i) * sx;
+#pragma unroll
+                for (int j = 0; j < GROUPS; ++j) v[i][j] = raw_load(row + 32 * j);
             }
-        } else {
-            load_columns_scalar(base, sx, nrow, g.pts.x - xb, g.iso, lt, le);
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+#pragma unroll
+                for (int j = 0; j < GROUPS; ++j) lo[j] |= below(v[i][j], iso, thr) << (r0 + i);
+        }
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            const T *row = base + (uint64_t)(32 + i) * sx;
+#pragma unroll
+            for (int j = 0; j < GROUPS; ++j) hi[j] |= below(raw_load(row + 32 * j), iso, thr) << i;
+        }
+    } else {
+        for (uint32_t r = 0; r < nrow; ++r) {
+            const T *row = base + (uint64_t)r * sx;
+            for (int j = 0; j < GROUPS; ++j) {
+                if (!cok[j]) continue;
+                const uint32_t b = below(raw_load(row + 32 * j), iso, thr);
+                if (r < 32) lo[j] |= b << r; else hi[j] |= b << (r - 32);
+            }
         }
     }
 #pragma unroll
-    for (int j = 0; j < CPL; ++j) { m.lt[CPL * lane + j] = lt[j]; m.le[CPL * lane + j] = le[j]; }
+    for (int j = 0; j < GROUPS; ++j) m[lane + 32 * j] = (uint64_t)lo[j] | ((uint64_t)hi[j] << 32);
 #pragma unroll 1
     for (int hc = 0; hc < 2; ++hc) {
         const uint32_t x = x0 + W + hc;
-        const bool okx = pz && x < g.pts.x;
+        const bool okx = pz && x < pts.x;
         const uint32_t y = y0 + lane, y2 = y0 + 32 + lane;
-        const bool in1 = okx && y < g.pts.y, in2 = okx && lane < 2 && y2 < g.pts.y;
-        const float v = in1 ? sample_p(vol, g.pts, x, y, p) : 0.f;
-        const float v2 = in2 ? sample_p(vol, g.pts, x, y2, p) : 0.f;
-        const uint32_t l32 = __ballot_sync(0xffffffffu, in1 && v < g.iso);
-        const uint32_t h2 = __ballot_sync(0xffffffffu, in2 && v2 < g.iso) & 3u;
-        const uint32_t e32 = __ballot_sync(0xffffffffu, in1 && v <= g.iso);
-        const uint32_t eh2 = __ballot_sync(0xffffffffu, in2 && v2 <= g.iso) & 3u;
-        if (lane == 0) {
-            m.lt[W + hc] = (uint64_t)l32 | ((uint64_t)h2 << 32);
-            m.le[W + hc] = (uint64_t)e32 | ((uint64_t)eh2 << 32);
-        }
+        const bool in1 = okx && y < pts.y, in2 = okx && lane < 2 && y2 < pts.y;
+        const float v = in1 ? sample_p(vol, pts, x, y, p) : 0.f;
+        const float v2 = in2 ? sample_p(vol, pts, x, y2, p) : 0.f;
+        const uint32_t l32 = __ballot_sync(0xffffffffu, in1 && v < iso);
+        const uint32_t h2 = __ballot_sync(0xffffffffu, in2 && v2 < iso) & 3u;
+        if (lane == 0) m[W + hc] = (uint64_t)l32 | ((uint64_t)h2 << 32);
     }
 }
 
@@ -295,20 +248,6 @@ __device__ __forceinline__ bool needs_lut2(const T *vol, const Geom &g, const De
     return tab.amb_face[ncfg] != 0xffu;
 }
 
-// Reference bipolarity and ccw bits of the cell's own edges 6, 9, 10 from
-// corners 2, 5, 6, 7 (dmc.cu:1199-1216).
-template <class T>
-__device__ __forceinline__ uint32_t owned_info_global(const T *vol, const Geom &g, uint32_t x, uint32_t y, uint32_t z)
-{
-    const float v2 = sample_at(vol, g, x + 1, y + 1, z), v5 = sample_at(vol, g, x + 1, y, z + 1);
-    const float v6 = sample_at(vol, g, x + 1, y + 1, z + 1), v7 = sample_at(vol, g, x, y + 1, z + 1);
-    uint32_t info = 0;
-    if (ref_bipolar(v2, v6, g.iso)) info |= 1u | (v2 <= g.iso ? 8u : 0u);
-    if (ref_bipolar(v5, v6, g.iso)) info |= 2u | (v5 <= g.iso ? 16u : 0u);
-    if (ref_bipolar(v7, v6, g.iso)) info |= 4u | (v7 <= g.iso ? 32u : 0u);
-    return info;
-}
-
 __device__ __forceinline__ uint32_t quad_count(uint32_t info, uint32_t cfg, uint32_t x, uint32_t y, uint32_t z,
                                                uint3 cells, uint32_t &dropped)
 {
@@ -331,17 +270,16 @@ __device__ __forceinline__ uint32_t cell_cfg(uint32_t p) { return (p >> 21) & 0x
 __device__ __forceinline__ bool cell_l2(uint32_t p) { return (p >> 29) & 1u; }
 
 // List index of active cell (c, r) of the plane stored at parity p.
-__device__ __noinline__ uint32_t entry_of(const WarpSmem &s, int p, int r, int c)
+__device__ __forceinline__ uint32_t entry_of(const WarpSmem &s, int p, int r, int c)
 {
     if (c == W) return s.rowstart[p][r + 1] - 1u;
-    const int l = c >> 2, j = c & 3;
-    const uint32_t lt = (1u << l) - 1u;
+    const uint4 w = *reinterpret_cast<const uint4 *>(s.xrow[p][r]);
+    const uint32_t q = (uint32_t)c >> 5, below_mask = (1u << (c & 31)) - 1u;
     uint32_t idx = s.rowstart[p][r];
-#pragma unroll
-    for (int jj = 0; jj < CPL; ++jj) {
-        const uint32_t b = s.ball[p][r][jj];
-        idx += __popc(b & lt) + ((jj < j) ? ((b >> l) & 1u) : 0u);
-    }
+    idx += q > 0 ? __popc(w.x) : __popc(w.x & below_mask);
+    if (q >= 1) idx += q > 1 ? __popc(w.y) : __popc(w.y & below_mask);
+    if (q >= 2) idx += q > 2 ? __popc(w.z) : __popc(w.z & below_mask);
+    if (q >= 3) idx += __popc(w.w & below_mask);
     return idx;
 }
 
@@ -353,6 +291,20 @@ __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane)
         if (lane >= o) v += y;
     }
     return v;
+}
+
+// 32x32 bit transpose across the warp: on entry lane l holds column l (bit r
+// = row r); on exit lane r holds row r (bit l = column l).
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x, int lane)
+{
+    const uint32_t lo[5] = {0x0000ffffu, 0x00ff00ffu, 0x0f0f0f0fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        const int s = 16 >> i;
+        const uint32_t y = __shfl_xor_sync(0xffffffffu, x, s);
+        x = (lane & s) ? ((x & ~lo[i]) | ((y & ~lo[i]) >> s)) : ((x & lo[i]) | ((y & lo[i]) << s));
+    }
+    return x;
 }
 
 struct EmitOut {
@@ -379,54 +331,19 @@ __device__ __forceinline__ uint32_t claim_brick(uint32_t *ticket, int lane)
     return __shfl_sync(0xffffffffu, b, 0);
 }
 
-// The eight corner samples of cell (x, y, z), with one 64-bit index.
+// Corner samples 2, 5, 6, 7 (the cell's own edges) or all eight.
 template <class T>
-__device__ __forceinline__ void load_cell(const T *vol, const Geom &g, uint32_t x, uint32_t y, uint32_t z, float v[8])
+__device__ __forceinline__ void load_cell(const T *vol, const Geom &g, uint32_t x, uint32_t y, uint32_t z, float v[8],
+                                          bool all)
 {
     const uint64_t sy = g.pts.x, sz = (uint64_t)g.pts.x * g.pts.y;
     const T *p = vol + (uint64_t)z * sz + (uint64_t)y * sy + x;
-    v[0] = load_sample(p, 0);           v[1] = load_sample(p, 1);
-    v[2] = load_sample(p, sy + 1);      v[3] = load_sample(p, sy);
-    v[4] = load_sample(p, sz);          v[5] = load_sample(p, sz + 1);
+    v[2] = load_sample(p, sy + 1);      v[5] = load_sample(p, sz + 1);
     v[6] = load_sample(p, sz + sy + 1); v[7] = load_sample(p, sz + sy);
-}
-
-// Reference bipolarity and ccw bits of the cell's own edges (dmc.cu:1199-1216)
-// from the "below" (lt) and "at or below" (le) bits of corners 2, 5, 6, 7:
-// ref_bipolar(a,b) = not both below, not both above, not both equal.
-__device__ __forceinline__ uint32_t info_from_bits(uint32_t cfg, uint32_t le4)
-{
-    // le4: bit 0 corner 2, bit 1 corner 5, bit 2 corner 6, bit 3 corner 7
-    const uint32_t l2 = (cfg >> 2) & 1u, l5 = (cfg >> 5) & 1u, l6 = (cfg >> 6) & 1u, l7 = (cfg >> 7) & 1u;
-    const uint32_t e2 = le4 & 1u, e5 = (le4 >> 1) & 1u, e6 = (le4 >> 2) & 1u, e7 = (le4 >> 3) & 1u;
-    auto bip = [](uint32_t la, uint32_t ea, uint32_t lb, uint32_t eb) -> uint32_t {
-        const uint32_t qa = ea & ~la, qb = eb & ~lb;          // exactly at the isovalue
-        return ~(la & lb) & (ea | eb) & ~(qa & qb) & 1u;
-    };
-    const uint32_t b6 = bip(l2, e2, l6, e6), b9 = bip(l5, e5, l6, e6), b10 = bip(l7, e7, l6, e6);
-    return b6 | (b9 << 1) | (b10 << 2) | ((b6 & e2) << 3) | ((b9 & e5) << 4) | ((b10 & e7) << 5);
-}
-
-// le bits of corners 2, 5, 6, 7 of the cell in row r (masks of columns c, c+1
-// in planes k (A,B) and k+1 (C,D)).
-__device__ __forceinline__ uint32_t le4_from_masks(uint64_t B, uint64_t C, uint64_t D, int r)
-{
-    return (uint32_t)((B >> (r + 1)) & 1u) | ((uint32_t)((D >> r) & 1u) << 1) |
-           ((uint32_t)((D >> (r + 1)) & 1u) << 2) | ((uint32_t)((C >> (r + 1)) & 1u) << 3);
-}
-
-// 32x32 bit transpose across the warp: on entry lane l holds column l (bit r
-// = row r); on exit lane r holds row r (bit l = column l).
-__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x, int lane)
-{
-    const uint32_t lo[5] = {0x0000ffffu, 0x00ff00ffu, 0x0f0f0f0fu, 0x33333333u, 0x55555555u};
-#pragma unroll
-    for (int i = 0; i < 5; ++i) {
-        const int s = 16 >> i;
-        const uint32_t y = __shfl_xor_sync(0xffffffffu, x, s);
-        x = (lane & s) ? ((x & ~lo[i]) | ((y & ~lo[i]) >> s)) : ((x & lo[i]) | ((y & lo[i]) << s));
+    if (all) {
+        v[0] = load_sample(p, 0);  v[1] = load_sample(p, 1);
+        v[3] = load_sample(p, sy); v[4] = load_sample(p, sz);
     }
-    return x;
 }
 
 // Quad rings of owned edges 6, 9, 10 (dmc.cu:653-664), one byte per ring slot:
@@ -446,8 +363,8 @@ __device__ __forceinline__ uint32_t ring_edge(int s, int kk)
 //   EMIT = true: also ranks the halo row and column, writes the vertices of
 //     plane k at their final offsets and the quads of plane k-1.
 // Active cells are compacted per plane in output order and processed 32 at a
-// time, one per lane, so that all lanes share the per-cell work.
-template <class T, bool VEC, bool EMIT>
+// time, one per lane; quads are compacted the same way.
+template <class T, bool EMIT>
 __global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vol, Geom g,
                                                         const DeviceTables *__restrict__ tabp,
                                                         uint2 *__restrict__ seg_cnt, EmitOut out,
@@ -457,9 +374,8 @@ __global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vo
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const DeviceTables &tab = stage_tables(tabp, reinterpret_cast<DeviceTables *>(smem_raw));
-    WarpSmem &S = reinterpret_cast<WarpSmem *>(smem_raw + sizeof(DeviceTables))[warp];
+    WarpSmem &S = reinterpret_cast<WarpSmem *>(smem_raw + kTablesBytes)[warp];
     WarpMem M{&S, spill + (uint64_t)blockIdx.x * NWB + warp};
-    const PlaneArgs pa{g.pts, g.iso, g.iso_u16, g.isole_u16};
     constexpr uint32_t NR = EMIT ? HROWS : ROWS;   // ranked rows
     uint32_t n_act = 0, n_l2 = 0, n_drop = 0;
 
@@ -473,13 +389,13 @@ __global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vo
         // the emit sweep also visits plane z1: quads of plane z1-1 reference it
         const uint32_t kend = EMIT ? z1 : z1 - 1;
 
-        load_plane<T, VEC>(vol, pa, x0, y0, z0, S.mask[z0 & 1], lane);
+        load_plane<T>(vol, g.pts, g.iso, g.iso_u16, x0, y0, z0, S.mask[z0 & 1], lane);
         for (uint32_t k = z0; k <= kend; ++k) {
             const int cur = k & 1, prv = cur ^ 1;
             const bool have_plane = k < g.cells.z;
             uint32_t L = 0;
             if (have_plane) {
-                load_plane<T, VEC>(vol, pa, x0, y0, k + 1, S.mask[(k + 1) & 1], lane);
+                load_plane<T>(vol, g.pts, g.iso, g.iso_u16, x0, y0, k + 1, S.mask[(k + 1) & 1], lane);
                 if (EMIT) {
                     for (uint32_t r = lane; r < HROWS; r += 32) {
                         const uint32_t yy = y0 + r;
@@ -492,62 +408,69 @@ __global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vo
                     }
                 }
                 __syncwarp();
-                const uint64_t *mk = S.mask[cur].lt, *mk1 = S.mask[(k + 1) & 1].lt;
-                uint64_t act[CPL];
+                const uint64_t *mk = S.mask[cur], *mk1 = S.mask[(k + 1) & 1];
+                uint64_t act[GROUPS];
 #pragma unroll
-                for (int j = 0; j < CPL; ++j) {
-                    const int c = CPL * lane + j;
+                for (int j = 0; j < GROUPS; ++j) {
+                    const int c = lane + 32 * j;
                     act[j] = (x0 + c < g.cells.x) ? active_rows(mk[c], mk[c + 1], mk1[c], mk1[c + 1]) & rowmask : 0ull;
                 }
                 uint64_t hact = 0;
                 if (EMIT && lane == 0 && x0 + W < g.cells.x) hact = active_rows(mk[W], mk[W + 1], mk1[W], mk1[W + 1]) & rowmask;
-                // rows 0..31: a bit transpose gives each lane its row's active
-                // lanes per column-in-lane; row 32 (emit only) by ballots
+                // bit transpose: lane r gets row r's active cells in x order
+                uint32_t xr[GROUPS], x32[GROUPS];
                 uint32_t cnt = 0, cnt32 = 0;
 #pragma unroll
-                for (int j = 0; j < CPL; ++j) {
-                    const uint32_t rowbits = warp_transpose32((uint32_t)act[j], lane);
-                    S.ball[cur][lane][j] = rowbits;
-                    cnt += __popc(rowbits);
-                    if (EMIT) {
-                        const uint32_t b32 = __ballot_sync(0xffffffffu, (act[j] >> 32) & 1ull);
-                        if (lane == 0) S.ball[cur][32][j] = b32;
-                        cnt32 += __popc(b32);
-                    }
+                for (int j = 0; j < GROUPS; ++j) {
+                    xr[j] = warp_transpose32((uint32_t)act[j], lane);
+                    cnt += __popc(xr[j]);
+                    x32[j] = EMIT ? __ballot_sync(0xffffffffu, (act[j] >> 32) & 1ull) : 0u;
+                    cnt32 += __popc(x32[j]);
                 }
                 if (EMIT) {
                     hact = __shfl_sync(0xffffffffu, hact, 0);
                     cnt += (uint32_t)((hact >> lane) & 1ull);
                     cnt32 += (uint32_t)((hact >> 32) & 1ull);
                 }
+                *reinterpret_cast<uint4 *>(S.xrow[cur][lane]) = make_uint4(xr[0], xr[1], xr[2], xr[3]);
+                if (EMIT && lane == 0) *reinterpret_cast<uint4 *>(S.xrow[cur][32]) = make_uint4(x32[0], x32[1], x32[2], x32[3]);
                 const uint32_t inc = warp_incl_scan(cnt, lane);
                 const uint32_t tot32 = __shfl_sync(0xffffffffu, inc, 31);
-                S.rowstart[cur][lane] = (uint16_t)(inc - cnt);
+                const uint32_t start = inc - cnt;
+                S.rowstart[cur][lane] = (uint16_t)start;
                 if (lane == 0) { S.rowstart[cur][32] = (uint16_t)tot32; S.rowstart[cur][33] = (uint16_t)(tot32 + cnt32); S.hact[cur] = hact; }
                 L = tot32 + cnt32;
-                __syncwarp();
+                // lane r lists row r in x order (lane 0 also row 32)
+                {
+                    uint32_t pos = start;
 #pragma unroll
-                for (int j = 0; j < CPL; ++j) {
-                    uint64_t a = act[j];
-                    while (a) {
-                        const int r = __ffsll((long long)a) - 1;
-                        a &= a - 1;
-                        M.lst(cur, entry_of(S, cur, r, CPL * lane + j)) = (uint16_t)((r << 8) | (CPL * lane + j));
+                    for (int j = 0; j < GROUPS; ++j) {
+                        uint32_t w = xr[j];
+                        while (w) {
+                            const int l = __ffs(w) - 1;
+                            w &= w - 1;
+                            M.lst(cur, pos++) = (uint16_t)((lane << 8) | (32 * j + l));
+                        }
                     }
-                }
-                if (EMIT && lane == 0) {
-                    uint64_t h = hact;
-                    while (h) {
-                        const int r = __ffsll((long long)h) - 1;
-                        h &= h - 1;
-                        M.lst(cur, S.rowstart[cur][r + 1] - 1u) = (uint16_t)((r << 8) | W);
+                    if (EMIT && ((hact >> lane) & 1ull)) M.lst(cur, pos++) = (uint16_t)((lane << 8) | W);
+                    if (EMIT && lane == 0) {
+                        pos = tot32;
+#pragma unroll
+                        for (int j = 0; j < GROUPS; ++j) {
+                            uint32_t w = x32[j];
+                            while (w) {
+                                const int l = __ffs(w) - 1;
+                                w &= w - 1;
+                                M.lst(cur, pos++) = (uint16_t)((32 << 8) | (32 * j + l));
+                            }
+                        }
+                        if ((hact >> 32) & 1ull) M.lst(cur, pos++) = (uint16_t)((32 << 8) | W);
                     }
                 }
                 __syncwarp();
             }
             // ranked active cells, 32 at a time
-            const uint64_t *mk = S.mask[cur].lt, *mk1 = S.mask[(k + 1) & 1].lt;
-            const uint64_t *ek = S.mask[cur].le, *ek1 = S.mask[(k + 1) & 1].le;
+            const uint64_t *mk = S.mask[cur], *mk1 = S.mask[(k + 1) & 1];
             uint32_t run = 0;
             for (uint32_t base = 0; base < L; base += 32) {
                 const uint32_t i = base + lane;
@@ -556,14 +479,16 @@ __global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vo
                 int r = 0, c = 0;
                 bool l2 = false, own = false;
                 uint32_t x = 0, y = 0;
+                float v[8];
                 if (valid) {
                     const uint32_t e = M.lst(cur, i);
                     r = e >> 8; c = e & 0xff;
                     x = x0 + c; y = y0 + r;
                     own = r < ROWS && c < W;
                     cfg = cfg_from_masks(mk[c], mk[c + 1], mk1[c], mk1[c + 1], r);
+                    load_cell(vol, g, x, y, k, v, EMIT && own && k < z1);
                     l2 = needs_lut2(vol, g, tab, cfg, mk, mk1, c, r, x, y, k);
-                    info = info_from_bits(cfg, le4_from_masks(ek[c + 1], ek1[c], ek1[c + 1], r));
+                    info = owned_edge_info(v, g.iso);
                     nv = nvert_of(tab, cfg, l2) + __popc(info & 7u);
                     uint32_t nq = 0;
                     if (own) nq = quad_count(info, cfg, x, y, k, g.cells, n_drop);
@@ -588,8 +513,6 @@ __global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vo
                         if (vb + nv > out.vcap) {
                             atomicOr(err, DEV_ERR_OVERFLOW);
                         } else {
-                            float v[8];
-                            load_cell(vol, g, x, y, k, v);
                             Geo geo;
                             geo.x0 = g.coord[x]; geo.x1 = g.coord[x + 1];
                             geo.y0 = g.coord[g.pts.x + y]; geo.y1 = g.coord[g.pts.x + y + 1];
@@ -608,63 +531,84 @@ __global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vo
                 }
                 n_act += L;
             }
-            // quads of own cells of plane k-1: their +z ring cells are in plane k.
-            // Ring cells (dmc.cu:653-664): e6 -> (c,r) (c+1,r) (c+1,r+1) (c,r+1) in
-            // plane k-1; e9 -> (c,r,k-1) (c,r,k) (c+1,r,k) (c+1,r,k-1); e10 ->
-            // (c,r,k-1) (c,r+1,k-1) (c,r+1,k) (c,r,k).  An active +x neighbour of an
-            // active cell is the next entry of the same row.
+            // quads of own cells of plane k-1: their +z ring cells are in plane
+            // k.  Owners are taken 32 at a time; their quads are compacted into
+            // qwork and written one per lane.
             if (EMIT && k > z0) {
                 const uint32_t kp = k - 1;
                 const uint32_t Lp = S.rowstart[prv][HROWS];
-                for (uint32_t i = lane; i < Lp; i += 32) {
-                    const uint32_t e = M.lst(prv, i);
-                    const int r = e >> 8, c = e & 0xff;
-                    if (r >= ROWS || c >= W) continue;
-                    const uint32_t x = x0 + c, y = y0 + r;
-                    const uint32_t d = M.ent(prv, i);
-                    const uint32_t cfg = cell_cfg(d);
-                    const uint32_t info = M.info(prv, i);
+                for (uint32_t base = 0; base < Lp; base += 32) {
+                    const uint32_t i = base + lane;
                     uint32_t want = 0;
+                    if (i < Lp) {
+                        const uint32_t e = M.lst(prv, i);
+                        const int r = e >> 8, c = e & 0xff;
+                        if (r < ROWS && c < W) {
+                            const uint32_t x = x0 + c, y = y0 + r;
+                            const uint32_t cfg = cell_cfg(M.ent(prv, i));
+                            const uint32_t info = M.info(prv, i);
 #pragma unroll
-                    for (int s = 0; s < 3; ++s)
-                        if ((info & (1u << s)) && owned_quad_in_volume(s, x, y, kp, g.cells) && owned_sign_change(cfg, s)) want |= 1u << s;
-                    if (!want) continue;
-                    uint64_t q = (uint64_t)S.segq[prv][r] + cell_qrel(d);
-                    const uint32_t e_up = (want & 5u) ? entry_of(S, prv, r + 1, c) : 0u;    // (c, r+1, k-1)
-                    const uint32_t e_z = (want & 6u) ? entry_of(S, cur, r, c) : 0u;        // (c, r, k)
-                    const uint32_t e_zup = (want & 4u) ? entry_of(S, cur, r + 1, c) : 0u;  // (c, r+1, k)
-                    // ring slot = plane (0 k-1, 1 k) | base (0 own entry, 1 (c,r+1,k-1),
-                    // 2 (c,r,k), 3 (c,r+1,k)) | +1 (next entry: c+1) | dr | ring edge
-#pragma unroll 1
-                    for (int s = 0; s < 3; ++s) {
-                        if (!(want & (1u << s))) continue;
-                        if (q >= out.qcap) { atomicOr(err, DEV_ERR_OVERFLOW); break; }
-                        const uint32_t ring = s == 0 ? kRing6 : (s == 1 ? kRing9 : kRing10);
-                        const bool ccw = (info >> (s + 3)) & 1u;
-                        uint32_t idx[4];
-#pragma unroll
-                        for (int it = 0; it < 4; ++it) {
-                            const int kk = ccw ? it : (4 - it) & 3;    // ccw 0,1,2,3; cw 0,3,2,1 (dmc.cu:1636-1645)
-                            const uint32_t sl = (ring >> (8 * kk)) & 0xffu;
-                            const int pl = (sl & 1u) ? cur : prv;
-                            const uint32_t bsel = (sl >> 1) & 3u;
-                            const uint32_t plus = (sl >> 3) & 1u, dr = (sl >> 4) & 1u;
-                            const uint32_t li = (bsel == 0 ? i : bsel == 1 ? e_up : bsel == 2 ? e_z : e_zup) + plus;
-                            const uint32_t re = ring_edge(s, kk);
-                            if (li >= S.rowstart[pl][HROWS]) { atomicOr(err, DEV_ERR_BOUNDS); idx[it] = 0; continue; }
-                            const uint32_t rd = M.ent(pl, li);
-                            uint32_t m = lut_m(tab, cell_cfg(rd), cell_l2(rd), (int)re);
-                            if (m == 0xffu) { atomicOr(err, DEV_ERR_BOUNDS); m = 0; }
-                            idx[it] = S.segv[pl][r + dr][(c + (int)plus) == W ? 1 : 0] + cell_vrel(rd) + m;
+                            for (int s = 0; s < 3; ++s)
+                                if ((info & (1u << s)) && owned_quad_in_volume(s, x, y, kp, g.cells) && owned_sign_change(cfg, s))
+                                    want |= 1u << s;
                         }
-                        reinterpret_cast<uint4 *>(out.quads)[q] = make_uint4(idx[0], idx[1], idx[2], idx[3]);
-                        if (out.tris) {
-                            uint32_t *tp = out.tris + 6 * q;
-                            tp[0] = idx[0]; tp[1] = idx[1]; tp[2] = idx[2];
-                            tp[3] = idx[2]; tp[4] = idx[3]; tp[5] = idx[0];
-                        }
-                        ++q;
                     }
+                    const uint32_t nq = __popc(want);
+                    const uint32_t qinc = warp_incl_scan(nq, lane);
+                    const uint32_t qtot = __shfl_sync(0xffffffffu, qinc, 31);
+                    {
+                        uint32_t pos = qinc - nq, w = want;
+                        while (w) {
+                            const int s = __ffs(w) - 1;
+                            w &= w - 1;
+                            S.qwork[pos++] = i | ((uint32_t)s << 16) | (want << 18);
+                        }
+                    }
+                    __syncwarp();
+                    for (uint32_t qb = 0; qb < qtot; qb += 32) {
+                        if (qb + lane < qtot) {
+                            const uint32_t item = S.qwork[qb + lane];
+                            const uint32_t oi = item & 0xffffu;
+                            const int s = (int)((item >> 16) & 3u);
+                            const uint32_t owant = item >> 18;
+                            const uint32_t e = M.lst(prv, oi);
+                            const int r = e >> 8, c = e & 0xff;
+                            const uint32_t d = M.ent(prv, oi);
+                            const uint32_t info = M.info(prv, oi);
+                            const uint64_t q = (uint64_t)S.segq[prv][r] + cell_qrel(d) + __popc(owant & ((1u << s) - 1u));
+                            if (q >= out.qcap) {
+                                atomicOr(err, DEV_ERR_OVERFLOW);
+                            } else {
+                                const uint32_t e_up = s != 1 ? entry_of(S, prv, r + 1, c) : 0u;    // (c, r+1, k-1)
+                                const uint32_t e_z = s != 0 ? entry_of(S, cur, r, c) : 0u;         // (c, r, k)
+                                const uint32_t e_zup = s == 2 ? entry_of(S, cur, r + 1, c) : 0u;   // (c, r+1, k)
+                                const uint32_t ring = s == 0 ? kRing6 : (s == 1 ? kRing9 : kRing10);
+                                const bool ccw = (info >> (s + 3)) & 1u;
+                                uint32_t idx[4];
+#pragma unroll
+                                for (int it = 0; it < 4; ++it) {
+                                    const int kk = ccw ? it : (4 - it) & 3;    // ccw 0,1,2,3; cw 0,3,2,1 (dmc.cu:1636-1645)
+                                    const uint32_t sl = (ring >> (8 * kk)) & 0xffu;
+                                    const int pl = (sl & 1u) ? cur : prv;
+                                    const uint32_t bsel = (sl >> 1) & 3u;
+                                    const uint32_t plus = (sl >> 3) & 1u, dr = (sl >> 4) & 1u;
+                                    const uint32_t li = (bsel == 0 ? oi : bsel == 1 ? e_up : bsel == 2 ? e_z : e_zup) + plus;
+                                    if (li >= S.rowstart[pl][HROWS]) { atomicOr(err, DEV_ERR_BOUNDS); idx[it] = 0; continue; }
+                                    const uint32_t rd = M.ent(pl, li);
+                                    uint32_t m = lut_m(tab, cell_cfg(rd), cell_l2(rd), (int)ring_edge(s, kk));
+                                    if (m == 0xffu) { atomicOr(err, DEV_ERR_BOUNDS); m = 0; }
+                                    idx[it] = S.segv[pl][r + dr][(c + (int)plus) == W ? 1 : 0] + cell_vrel(rd) + m;
+                                }
+                                reinterpret_cast<uint4 *>(out.quads)[q] = make_uint4(idx[0], idx[1], idx[2], idx[3]);
+                                if (out.tris) {
+                                    uint32_t *tp = out.tris + 6 * q;
+                                    tp[0] = idx[0]; tp[1] = idx[1]; tp[2] = idx[2];
+                                    tp[3] = idx[2]; tp[4] = idx[3]; tp[5] = idx[0];
+                                }
+                            }
+                        }
+                    }
+                    __syncwarp();
                 }
             }
             __syncwarp();
@@ -736,23 +680,23 @@ bool brick_supports(const ExtractArgs &a)
     return a.cells.x >= 1 && a.cells.y >= 1 && a.cells.z >= 1;
 }
 
-constexpr size_t kSweepSmem = sizeof(DeviceTables) + sizeof(brick::WarpSmem) * brick::NWB;
+constexpr size_t kSweepSmem = brick::kTablesBytes + sizeof(brick::WarpSmem) * brick::NWB;
 
-template <class T, bool VEC>
+template <class T>
 static int sweep_grid(Ctx *ctx)
 {
     using namespace brick;
-    cudaFuncSetAttribute(brick_sweep<T, VEC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSweepSmem);
-    cudaFuncSetAttribute(brick_sweep<T, VEC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSweepSmem);
+    cudaFuncSetAttribute(brick_sweep<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSweepSmem);
+    cudaFuncSetAttribute(brick_sweep<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSweepSmem);
     int b0 = 0, b1 = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, brick_sweep<T, VEC, true>, 32 * NWB, kSweepSmem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, brick_sweep<T, VEC, false>, 32 * NWB, kSweepSmem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, brick_sweep<T, true>, 32 * NWB, kSweepSmem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, brick_sweep<T, false>, 32 * NWB, kSweepSmem);
     int b = b0 < b1 ? b0 : b1;
     if (b < 1) b = 1;
     return b * ctx->num_sms;
 }
 
-template <class T, bool VEC>
+template <class T>
 static dmc_status brick_run_v(Ctx *ctx, const T *vol, const ExtractArgs &a, cudaStream_t st)
 {
     using namespace brick;
@@ -766,16 +710,10 @@ static dmc_status brick_run_v(Ctx *ctx, const T *vol, const ExtractArgs &a, cuda
         else if (f > 65535.f) t = 65536;
         else { uint32_t fl = (uint32_t)f; t = ((float)fl == f) ? fl : fl + 1; }
         g.iso_u16 = t;
-        // v <= iso  <=>  v < floor(iso) + 1
-        uint32_t te;
-        if (!(f >= 0.f)) te = 0;
-        else if (f >= 65535.f) te = 65536;
-        else te = (uint32_t)f + 1;
-        g.isole_u16 = te;
     }
     g.nxs = (a.cells.x + W - 1) / W;
     g.nyb = (a.cells.y + ROWS - 1) / ROWS;
-    const int grid = sweep_grid<T, VEC>(ctx);
+    const int grid = sweep_grid<T>(ctx);
     // planes per brick: long sweeps amortise the z halo, but keep at least
     // three bricks per warp so that the persistent warps stay busy
     g.zc = 32;
@@ -811,7 +749,7 @@ static dmc_status brick_run_v(Ctx *ctx, const T *vol, const ExtractArgs &a, cuda
     coord_table<<<(unsigned)((n_coord + 255) / 256), 256, 0, st>>>(coord, a.pts, a.cells, a.rng, a.mn);
     ctx->evk_used = 0;
     CUDA_TRY(cudaEventRecord(ctx->evk[0], st));
-    brick_sweep<T, VEC, false><<<grid, 32 * NWB, kSweepSmem, st>>>(vol, g, ctx->d_tab, seg_cnt, EmitOut{}, spill,
+    brick_sweep<T, false><<<grid, 32 * NWB, kSweepSmem, st>>>(vol, g, ctx->d_tab, seg_cnt, EmitOut{}, spill,
                                                                     &tickets[0], ctx->d_ctl->counters, &ctx->d_ctl->err);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaEventRecord(ctx->evk[1], st));
@@ -836,7 +774,7 @@ static dmc_status brick_run_v(Ctx *ctx, const T *vol, const ExtractArgs &a, cuda
     EmitOut eo;
     eo.seg_off = seg_off; eo.verts = a.verts; eo.vcap = a.vcap; eo.quads = a.quads; eo.qcap = a.qcap; eo.tris = a.tris;
     CUDA_TRY(cudaEventRecord(ctx->evk[3], st));
-    brick_sweep<T, VEC, true><<<grid, 32 * NWB, kSweepSmem, st>>>(vol, g, ctx->d_tab, nullptr, eo, spill, &tickets[1],
+    brick_sweep<T, true><<<grid, 32 * NWB, kSweepSmem, st>>>(vol, g, ctx->d_tab, nullptr, eo, spill, &tickets[1],
                                                                    ctx->d_ctl->counters, &ctx->d_ctl->err);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaEventRecord(ctx->evk[4], st));
@@ -847,10 +785,7 @@ static dmc_status brick_run_v(Ctx *ctx, const T *vol, const ExtractArgs &a, cuda
 template <class T>
 static dmc_status brick_run_t(Ctx *ctx, const T *vol, const ExtractArgs &a, cudaStream_t st)
 {
-    // vector loads need every row start aligned to the vector size
-    const size_t vb = sizeof(T) * brick::CPL;
-    const bool vec = ((uintptr_t)vol % vb == 0) && (((size_t)a.pts.x * sizeof(T)) % vb == 0);
-    return vec ? brick_run_v<T, true>(ctx, vol, a, st) : brick_run_v<T, false>(ctx, vol, a, st);
+    return brick_run_v<T>(ctx, vol, a, st);
 }
 
 dmc_status brick_run(Ctx *ctx, const ExtractArgs &a, cudaStream_t st)
