@@ -52,7 +52,7 @@ struct Geom {
     const float *coord;    // point coordinates: x[0..cx], y[0..cy], z[0..cz]
 };
 
-struct WarpSmem {
+struct alignas(16) WarpSmem {
     uint64_t mask[2][W + 2];           // column masks of point planes (by parity): bit r = row r below iso
     uint32_t xrow[2][HROWS][GROUPS];   // per row: active cells in x order, word q = columns 32q..32q+31
     uint64_t hact[2];                  // halo column activity (bit = row)
