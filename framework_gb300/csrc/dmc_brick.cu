@@ -48,26 +48,37 @@ struct Geom {
     uint64_t nbricks;
     float iso;
     uint32_t iso_u16;      // uint16 samples: v < iso  <=>  v < iso_u16 (65536: always)
+    uint32_t isole_u16;    // uint16 samples: v <= iso <=>  v < isole_u16
     float3 mn, rng;
     const float *coord;    // point coordinates: x[0..cx], y[0..cy], z[0..cz]
 };
 
-struct alignas(16) WarpSmem {
-    uint64_t mask[2][W + 2];           // column masks of point planes (by parity): bit r = row r below iso
+struct alignas(16) PlaneMasks {
+    uint64_t lt[W + 2];                // bit r: sample (x0+c, y0+r) < iso
+    uint64_t le[W + 2];                // bit r: sample <= iso
+};
+
+// Per-warp state used by both sweeps (the count sweep allocates only this).
+struct alignas(16) SweepSmem {
+    PlaneMasks mask[2];                // point planes by parity
     uint32_t xrow[2][HROWS][GROUPS];   // per row: active cells in x order, word q = columns 32q..32q+31
     uint64_t hact[2];                  // halo column activity (bit = row)
     uint16_t rowstart[2][HROWS + 1];   // first list entry of each row
     uint32_t rowbase[HROWS];           // running (v | q << 16) prefix at each row start
     uint32_t rowtot[ROWS];             // count sweep: per-row (v | q << 16)
+    uint16_t lst[2][CAP];              // row << 8 | col
+};
+
+// Per-warp state of the emit sweep.
+struct alignas(16) WarpSmem : SweepSmem {
     uint32_t segv[2][HROWS][2];        // vertex offset of (row, own / next segment)
     uint32_t segq[2][HROWS];           // quad offset of (row, own segment)
     uint32_t qwork[QBUF];              // quads of one round: entry | edge << 16 | wanted edges << 18
     uint32_t ent[2][CAP];              // packed cell: vrel 11 | qrel 10 | cfg 8 | lut2 1
-    uint16_t lst[2][CAP];              // row << 8 | col
     uint8_t info[2][CAP];              // own-edge bipolar/ccw bits
 };
 
-static_assert(sizeof(WarpSmem) % 16 == 0, "per-warp shared memory must keep 16-byte alignment");
+static_assert(sizeof(WarpSmem) % 16 == 0 && sizeof(SweepSmem) % 16 == 0, "per-warp shared memory must keep 16-byte alignment");
 
 // shared memory layout of a sweep block: tables, then one WarpSmem per warp
 constexpr size_t kTablesBytes = (sizeof(DeviceTables) + 127) & ~(size_t)127;
@@ -119,6 +130,8 @@ __device__ __forceinline__ float sample_p(const T *vol, uint3 pts, uint32_t x, u
 // equivalent integer compare against the precomputed threshold
 __device__ __forceinline__ uint32_t below(float v, float iso, uint32_t) { return v < iso ? 1u : 0u; }
 __device__ __forceinline__ uint32_t below(uint16_t v, float, uint32_t thr) { return (uint32_t)v < thr ? 1u : 0u; }
+__device__ __forceinline__ uint32_t at_or_below(float v, float iso, uint32_t) { return v <= iso ? 1u : 0u; }
+__device__ __forceinline__ uint32_t at_or_below(uint16_t v, float, uint32_t thr) { return (uint32_t)v < thr ? 1u : 0u; }
 
 template <class T>
 __device__ __forceinline__ T raw_load(const T *p) { return __ldg(p); }
@@ -129,10 +142,11 @@ __device__ __forceinline__ T raw_load(const T *p) { return __ldg(p); }
 // active).  Loads go out 32 per lane before their results are used, and the
 // next plane's rows are prefetched into L2.
 template <class T>
-__device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint32_t thr, uint32_t x0, uint32_t y0,
-                                        uint32_t p, uint64_t *m, int lane)
+__device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint32_t thr, uint32_t thr_le, uint32_t x0,
+                                        uint32_t y0, uint32_t p, PlaneMasks &m, int lane)
 {
     uint32_t lo[GROUPS] = {0, 0, 0, 0}, hi[GROUPS] = {0, 0, 0, 0};
+    uint32_t elo[GROUPS] = {0, 0, 0, 0}, ehi[GROUPS] = {0, 0, 0, 0};
     const bool pz = p < pts.z;
     const uint32_t nrow = pz ? min(34u, pts.y - y0) : 0u;
     const uint64_t sx = pts.x;
@@ -161,26 +175,38 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
 #pragma unroll
             for (int i = 0; i < 8; ++i)
 #pragma unroll
-                for (int j = 0; j < GROUPS; ++j) lo[j] |= below(v[i][j], iso, thr) << (r0 + i);
+                for (int j = 0; j < GROUPS; ++j) {
+                    lo[j] |= below(v[i][j], iso, thr) << (r0 + i);
+                    elo[j] |= at_or_below(v[i][j], iso, thr_le) << (r0 + i);
+                }
         }
 #pragma unroll
         for (int i = 0; i < 2; ++i) {
             const T *row = base + (uint64_t)(32 + i) * sx;
 #pragma unroll
-            for (int j = 0; j < GROUPS; ++j) hi[j] |= below(raw_load(row + 32 * j), iso, thr) << i;
+            for (int j = 0; j < GROUPS; ++j) {
+                const T v = raw_load(row + 32 * j);
+                hi[j] |= below(v, iso, thr) << i;
+                ehi[j] |= at_or_below(v, iso, thr_le) << i;
+            }
         }
     } else {
         for (uint32_t r = 0; r < nrow; ++r) {
             const T *row = base + (uint64_t)r * sx;
             for (int j = 0; j < GROUPS; ++j) {
                 if (!cok[j]) continue;
-                const uint32_t b = below(raw_load(row + 32 * j), iso, thr);
-                if (r < 32) lo[j] |= b << r; else hi[j] |= b << (r - 32);
+                const T v = raw_load(row + 32 * j);
+                const uint32_t b = below(v, iso, thr), e = at_or_below(v, iso, thr_le);
+                if (r < 32) { lo[j] |= b << r; elo[j] |= e << r; }
+                else { hi[j] |= b << (r - 32); ehi[j] |= e << (r - 32); }
             }
         }
     }
 #pragma unroll
-    for (int j = 0; j < GROUPS; ++j) m[lane + 32 * j] = (uint64_t)lo[j] | ((uint64_t)hi[j] << 32);
+    for (int j = 0; j < GROUPS; ++j) {
+        m.lt[lane + 32 * j] = (uint64_t)lo[j] | ((uint64_t)hi[j] << 32);
+        m.le[lane + 32 * j] = (uint64_t)elo[j] | ((uint64_t)ehi[j] << 32);
+    }
 #pragma unroll 1
     for (int hc = 0; hc < 2; ++hc) {
         const uint32_t x = x0 + W + hc;
@@ -191,8 +217,36 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
         const float v2 = in2 ? sample_p(vol, pts, x, y2, p) : 0.f;
         const uint32_t l32 = __ballot_sync(0xffffffffu, in1 && v < iso);
         const uint32_t h2 = __ballot_sync(0xffffffffu, in2 && v2 < iso) & 3u;
-        if (lane == 0) m[W + hc] = (uint64_t)l32 | ((uint64_t)h2 << 32);
+        const uint32_t e32 = __ballot_sync(0xffffffffu, in1 && v <= iso);
+        const uint32_t eh2 = __ballot_sync(0xffffffffu, in2 && v2 <= iso) & 3u;
+        if (lane == 0) {
+            m.lt[W + hc] = (uint64_t)l32 | ((uint64_t)h2 << 32);
+            m.le[W + hc] = (uint64_t)e32 | ((uint64_t)eh2 << 32);
+        }
     }
+}
+
+// Reference bipolarity and ccw bits of the cell's own edges (dmc.cu:1199-1216)
+// from the "below" (lt) and "at or below" (le) bits of corners 2, 5, 6, 7:
+// ref_bipolar(a,b) = not both below, not both above, not both equal.
+__device__ __forceinline__ uint32_t info_from_bits(uint32_t cfg, uint32_t le4)
+{
+    // le4: bit 0 corner 2, bit 1 corner 5, bit 2 corner 6, bit 3 corner 7
+    const uint32_t l2 = (cfg >> 2) & 1u, l5 = (cfg >> 5) & 1u, l6 = (cfg >> 6) & 1u, l7 = (cfg >> 7) & 1u;
+    const uint32_t e2 = le4 & 1u, e5 = (le4 >> 1) & 1u, e6 = (le4 >> 2) & 1u, e7 = (le4 >> 3) & 1u;
+    const uint32_t q2 = e2 & ~l2, q5 = e5 & ~l5, q6 = e6 & ~l6, q7 = e7 & ~l7;   // exactly at the isovalue
+    const uint32_t b6 = ~(l2 & l6) & (e2 | e6) & ~(q2 & q6) & 1u;
+    const uint32_t b9 = ~(l5 & l6) & (e5 | e6) & ~(q5 & q6) & 1u;
+    const uint32_t b10 = ~(l7 & l6) & (e7 | e6) & ~(q7 & q6) & 1u;
+    return b6 | (b9 << 1) | (b10 << 2) | ((b6 & e2) << 3) | ((b9 & e5) << 4) | ((b10 & e7) << 5);
+}
+
+// le bits of corners 2, 5, 6, 7 of the cell in row r (masks of columns c, c+1
+// in planes k (B: column c+1) and k+1 (C: column c, D: column c+1)).
+__device__ __forceinline__ uint32_t le4_from_masks(uint64_t B, uint64_t C, uint64_t D, int r)
+{
+    return (uint32_t)((B >> (r + 1)) & 1u) | ((uint32_t)((D >> r) & 1u) << 1) |
+           ((uint32_t)((D >> (r + 1)) & 1u) << 2) | ((uint32_t)((C >> (r + 1)) & 1u) << 3);
 }
 
 // Rows r (bit r) whose cell has corners on both sides (A,B: plane k columns
@@ -270,7 +324,7 @@ __device__ __forceinline__ uint32_t cell_cfg(uint32_t p) { return (p >> 21) & 0x
 __device__ __forceinline__ bool cell_l2(uint32_t p) { return (p >> 29) & 1u; }
 
 // List index of active cell (c, r) of the plane stored at parity p.
-__device__ __forceinline__ uint32_t entry_of(const WarpSmem &s, int p, int r, int c)
+__device__ __forceinline__ uint32_t entry_of(const SweepSmem &s, int p, int r, int c)
 {
     if (c == W) return s.rowstart[p][r + 1] - 1u;
     const uint4 w = *reinterpret_cast<const uint4 *>(s.xrow[p][r]);
@@ -374,7 +428,8 @@ __global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vo
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const DeviceTables &tab = stage_tables(tabp, reinterpret_cast<DeviceTables *>(smem_raw));
-    WarpSmem &S = reinterpret_cast<WarpSmem *>(smem_raw + kTablesBytes)[warp];
+    // the count sweep gives each warp only the SweepSmem part
+    WarpSmem &S = *reinterpret_cast<WarpSmem *>(smem_raw + kTablesBytes + (size_t)warp * (EMIT ? sizeof(WarpSmem) : sizeof(SweepSmem)));
     WarpMem M{&S, spill + (uint64_t)blockIdx.x * NWB + warp};
     constexpr uint32_t NR = EMIT ? HROWS : ROWS;   // ranked rows
     uint32_t n_act = 0, n_l2 = 0, n_drop = 0;
@@ -389,13 +444,13 @@ __global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vo
         // the emit sweep also visits plane z1: quads of plane z1-1 reference it
         const uint32_t kend = EMIT ? z1 : z1 - 1;
 
-        load_plane<T>(vol, g.pts, g.iso, g.iso_u16, x0, y0, z0, S.mask[z0 & 1], lane);
+        load_plane<T>(vol, g.pts, g.iso, g.iso_u16, g.isole_u16, x0, y0, z0, S.mask[z0 & 1], lane);
         for (uint32_t k = z0; k <= kend; ++k) {
             const int cur = k & 1, prv = cur ^ 1;
             const bool have_plane = k < g.cells.z;
             uint32_t L = 0;
             if (have_plane) {
-                load_plane<T>(vol, g.pts, g.iso, g.iso_u16, x0, y0, k + 1, S.mask[(k + 1) & 1], lane);
+                load_plane<T>(vol, g.pts, g.iso, g.iso_u16, g.isole_u16, x0, y0, k + 1, S.mask[(k + 1) & 1], lane);
                 if (EMIT) {
                     for (uint32_t r = lane; r < HROWS; r += 32) {
                         const uint32_t yy = y0 + r;
@@ -408,7 +463,7 @@ __global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vo
                     }
                 }
                 __syncwarp();
-                const uint64_t *mk = S.mask[cur], *mk1 = S.mask[(k + 1) & 1];
+                const uint64_t *mk = S.mask[cur].lt, *mk1 = S.mask[(k + 1) & 1].lt;
                 uint64_t act[GROUPS];
 #pragma unroll
                 for (int j = 0; j < GROUPS; ++j) {
@@ -470,7 +525,8 @@ __global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vo
                 __syncwarp();
             }
             // ranked active cells, 32 at a time
-            const uint64_t *mk = S.mask[cur], *mk1 = S.mask[(k + 1) & 1];
+            const uint64_t *mk = S.mask[cur].lt, *mk1 = S.mask[(k + 1) & 1].lt;
+            const uint64_t *ek = S.mask[cur].le, *ek1 = S.mask[(k + 1) & 1].le;
             uint32_t run = 0;
             for (uint32_t base = 0; base < L; base += 32) {
                 const uint32_t i = base + lane;
@@ -486,9 +542,9 @@ __global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vo
                     x = x0 + c; y = y0 + r;
                     own = r < ROWS && c < W;
                     cfg = cfg_from_masks(mk[c], mk[c + 1], mk1[c], mk1[c + 1], r);
-                    load_cell(vol, g, x, y, k, v, EMIT && own && k < z1);
+                    if (EMIT && own && k < z1) load_cell(vol, g, x, y, k, v, true);
                     l2 = needs_lut2(vol, g, tab, cfg, mk, mk1, c, r, x, y, k);
-                    info = owned_edge_info(v, g.iso);
+                    info = info_from_bits(cfg, le4_from_masks(ek[c + 1], ek1[c], ek1[c + 1], r));
                     nv = nvert_of(tab, cfg, l2) + __popc(info & 7u);
                     uint32_t nq = 0;
                     if (own) nq = quad_count(info, cfg, x, y, k, g.cells, n_drop);
@@ -680,18 +736,17 @@ bool brick_supports(const ExtractArgs &a)
     return a.cells.x >= 1 && a.cells.y >= 1 && a.cells.z >= 1;
 }
 
-constexpr size_t kSweepSmem = brick::kTablesBytes + sizeof(brick::WarpSmem) * brick::NWB;
+constexpr size_t kEmitSmem = brick::kTablesBytes + sizeof(brick::WarpSmem) * brick::NWB;
+constexpr size_t kCountSmem = brick::kTablesBytes + sizeof(brick::SweepSmem) * brick::NWB;
 
-template <class T>
+template <class T, bool EMIT>
 static int sweep_grid(Ctx *ctx)
 {
     using namespace brick;
-    cudaFuncSetAttribute(brick_sweep<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSweepSmem);
-    cudaFuncSetAttribute(brick_sweep<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSweepSmem);
-    int b0 = 0, b1 = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, brick_sweep<T, true>, 32 * NWB, kSweepSmem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, brick_sweep<T, false>, 32 * NWB, kSweepSmem);
-    int b = b0 < b1 ? b0 : b1;
+    const size_t smem = EMIT ? kEmitSmem : kCountSmem;
+    cudaFuncSetAttribute(brick_sweep<T, EMIT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, brick_sweep<T, EMIT>, 32 * NWB, smem);
     if (b < 1) b = 1;
     return b * ctx->num_sms;
 }
@@ -710,10 +765,16 @@ static dmc_status brick_run_v(Ctx *ctx, const T *vol, const ExtractArgs &a, cuda
         else if (f > 65535.f) t = 65536;
         else { uint32_t fl = (uint32_t)f; t = ((float)fl == f) ? fl : fl + 1; }
         g.iso_u16 = t;
+        // v <= iso  <=>  v < floor(iso) + 1
+        uint32_t te;
+        if (!(f >= 0.f)) te = 0;
+        else if (f >= 65535.f) te = 65536;
+        else te = (uint32_t)f + 1;
+        g.isole_u16 = te;
     }
     g.nxs = (a.cells.x + W - 1) / W;
     g.nyb = (a.cells.y + ROWS - 1) / ROWS;
-    const int grid = sweep_grid<T>(ctx);
+    const int grid = sweep_grid<T, true>(ctx), cgrid = sweep_grid<T, false>(ctx);
     // planes per brick: long sweeps amortise the z halo, but keep at least
     // three bricks per warp so that the persistent warps stay busy
     g.zc = 32;
@@ -730,7 +791,7 @@ static dmc_status brick_run_v(Ctx *ctx, const T *vol, const ExtractArgs &a, cuda
     size_t off = 0;
     auto carve = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~(size_t)255; return o; };
     const size_t o_cnt = carve(8 * nseg), o_off = carve(8 * nseg), o_tiles = carve(sizeof(TileState) * n_tiles);
-    const size_t o_spill = carve(sizeof(Spill) * (size_t)grid * NWB);
+    const size_t o_spill = carve(sizeof(Spill) * (size_t)(grid > cgrid ? grid : cgrid) * NWB);
     const size_t o_coord = carve(4 * n_coord);
     const size_t o_tk = carve(256);
     dmc_status s = ctx_reserve_scratch(ctx, off);
@@ -749,7 +810,7 @@ static dmc_status brick_run_v(Ctx *ctx, const T *vol, const ExtractArgs &a, cuda
     coord_table<<<(unsigned)((n_coord + 255) / 256), 256, 0, st>>>(coord, a.pts, a.cells, a.rng, a.mn);
     ctx->evk_used = 0;
     CUDA_TRY(cudaEventRecord(ctx->evk[0], st));
-    brick_sweep<T, false><<<grid, 32 * NWB, kSweepSmem, st>>>(vol, g, ctx->d_tab, seg_cnt, EmitOut{}, spill,
+    brick_sweep<T, false><<<cgrid, 32 * NWB, kCountSmem, st>>>(vol, g, ctx->d_tab, seg_cnt, EmitOut{}, spill,
                                                                     &tickets[0], ctx->d_ctl->counters, &ctx->d_ctl->err);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaEventRecord(ctx->evk[1], st));
@@ -774,7 +835,7 @@ static dmc_status brick_run_v(Ctx *ctx, const T *vol, const ExtractArgs &a, cuda
     EmitOut eo;
     eo.seg_off = seg_off; eo.verts = a.verts; eo.vcap = a.vcap; eo.quads = a.quads; eo.qcap = a.qcap; eo.tris = a.tris;
     CUDA_TRY(cudaEventRecord(ctx->evk[3], st));
-    brick_sweep<T, true><<<grid, 32 * NWB, kSweepSmem, st>>>(vol, g, ctx->d_tab, nullptr, eo, spill, &tickets[1],
+    brick_sweep<T, true><<<grid, 32 * NWB, kEmitSmem, st>>>(vol, g, ctx->d_tab, nullptr, eo, spill, &tickets[1],
                                                                    ctx->d_ctl->counters, &ctx->d_ctl->err);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaEventRecord(ctx->evk[4], st));
