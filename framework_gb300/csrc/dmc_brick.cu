@@ -36,7 +36,7 @@ constexpr int W = 32 * GROUPS;            // cell columns per brick (= segment w
 constexpr int ROWS = 32;                  // own cell rows
 constexpr int HROWS = ROWS + 1;           // with the halo row
 constexpr int MAXL = HROWS * (W + 1);     // most active cells one plane of a brick can hold
-constexpr int CAP = 320;                  // entries kept in shared memory per plane
+constexpr int CAP = 256;                  // entries kept in shared memory per plane
 constexpr int OVF = MAXL - CAP;           // entries per plane that spill to global scratch
 constexpr int NWB = 8;                    // warps per block (independent)
 constexpr int QBUF = 96;                  // quads of one round of owner cells (3 per cell)
@@ -66,11 +66,12 @@ struct alignas(16) SweepSmem {
     uint16_t rowstart[2][HROWS + 1];   // first list entry of each row
     uint32_t rowbase[HROWS];           // running (v | q << 16) prefix at each row start
     uint32_t rowtot[ROWS];             // count sweep: per-row (v | q << 16)
-    uint16_t lst[2][CAP];              // row << 8 | col
+    uint16_t lst0[CAP];                // list of plane slot 0: row << 8 | col (the count sweep uses only this)
 };
 
 // Per-warp state of the emit sweep.
 struct alignas(16) WarpSmem : SweepSmem {
+    uint16_t lst1[CAP];                // list of plane slot 1
     uint32_t segv[2][HROWS][2];        // vertex offset of (row, own / next segment)
     uint32_t segq[2][HROWS];           // quad offset of (row, own segment)
     uint32_t qwork[QBUF];              // quads of one round: entry | edge << 16 | wanted edges << 18
@@ -99,7 +100,7 @@ struct WarpMem {
     }
     __device__ __forceinline__ uint16_t &lst(int p, uint32_t i)
     {
-        uint16_t *b = i < CAP ? s->lst[p] : g->lst[p] - CAP;
+        uint16_t *b = i < CAP ? (p ? s->lst1 : s->lst0) : g->lst[p] - CAP;
         return b[i];
     }
     __device__ __forceinline__ uint8_t &info(int p, uint32_t i)
@@ -419,7 +420,7 @@ __device__ __forceinline__ uint32_t ring_edge(int s, int kk)
 // Active cells are compacted per plane in output order and processed 32 at a
 // time, one per lane; quads are compacted the same way.
 template <class T, bool EMIT>
-__global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vol, Geom g,
+__global__ void __launch_bounds__(32 * NWB, EMIT ? 2 : 4) brick_sweep(const T *__restrict__ vol, Geom g,
                                                         const DeviceTables *__restrict__ tabp,
                                                         uint2 *__restrict__ seg_cnt, EmitOut out,
                                                         Spill *__restrict__ spill, uint32_t *ticket,
@@ -447,6 +448,7 @@ __global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vo
         load_plane<T>(vol, g.pts, g.iso, g.iso_u16, g.isole_u16, x0, y0, z0, S.mask[z0 & 1], lane);
         for (uint32_t k = z0; k <= kend; ++k) {
             const int cur = k & 1, prv = cur ^ 1;
+            const int lp = EMIT ? cur : 0;                 // list slot of this plane
             const bool have_plane = k < g.cells.z;
             uint32_t L = 0;
             if (have_plane) {
@@ -504,10 +506,10 @@ __global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vo
                         while (w) {
                             const int l = __ffs(w) - 1;
                             w &= w - 1;
-                            M.lst(cur, pos++) = (uint16_t)((lane << 8) | (32 * j + l));
+                            M.lst(lp, pos++) = (uint16_t)((lane << 8) | (32 * j + l));
                         }
                     }
-                    if (EMIT && ((hact >> lane) & 1ull)) M.lst(cur, pos++) = (uint16_t)((lane << 8) | W);
+                    if (EMIT && ((hact >> lane) & 1ull)) M.lst(lp, pos++) = (uint16_t)((lane << 8) | W);
                     if (EMIT && lane == 0) {
                         pos = tot32;
 #pragma unroll
@@ -516,10 +518,10 @@ __global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vo
                             while (w) {
                                 const int l = __ffs(w) - 1;
                                 w &= w - 1;
-                                M.lst(cur, pos++) = (uint16_t)((32 << 8) | (32 * j + l));
+                                M.lst(lp, pos++) = (uint16_t)((32 << 8) | (32 * j + l));
                             }
                         }
-                        if ((hact >> 32) & 1ull) M.lst(cur, pos++) = (uint16_t)((32 << 8) | W);
+                        if ((hact >> 32) & 1ull) M.lst(lp, pos++) = (uint16_t)((32 << 8) | W);
                     }
                 }
                 __syncwarp();
@@ -537,7 +539,7 @@ __global__ void __launch_bounds__(32 * NWB) brick_sweep(const T *__restrict__ vo
                 uint32_t x = 0, y = 0;
                 float v[8];
                 if (valid) {
-                    const uint32_t e = M.lst(cur, i);
+                    const uint32_t e = M.lst(lp, i);
                     r = e >> 8; c = e & 0xff;
                     x = x0 + c; y = y0 + r;
                     own = r < ROWS && c < W;
