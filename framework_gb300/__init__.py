@@ -33,7 +33,10 @@ ALGO = {"auto": 0, "simple": 1, "brick": 2}
 ABI_SYMBOLS = [
     "dmc_version", "dmc_tables_sha256", "dmc_status_string", "dmc_create", "dmc_destroy",
     "dmc_set_algo", "dmc_run", "dmc_mesh_free", "dmc_extract_device", "dmc_get_stats",
+    "dmc_extract_batch", "dmc_batch_wait", "dmc_set_option",
 ]
+BATCH_ASYNC, BATCH_GRAPH = 0x1, 0x2
+OPT_BRICK_PLANES = 1
 
 
 class DMCError(RuntimeError):
@@ -45,6 +48,16 @@ class DMCError(RuntimeError):
 
 class _Volume(ctypes.Structure):
     _fields_ = [("data", ctypes.c_void_p), ("dtype", ctypes.c_int), ("dims", ctypes.c_uint32 * 3)]
+
+
+class _BatchItem(ctypes.Structure):
+    _fields_ = [("vol", _Volume), ("iso", ctypes.c_float), ("xyz_min", ctypes.c_float * 3),
+                ("xyz_max", ctypes.c_float * 3)]
+
+
+class _BatchResult(ctypes.Structure):
+    _fields_ = [("vertex_offset", ctypes.c_uint64), ("n_vertices", ctypes.c_uint64),
+                ("quad_offset", ctypes.c_uint64), ("n_quads", ctypes.c_uint64)]
 
 
 class _Mesh(ctypes.Structure):
@@ -98,6 +111,12 @@ def load_library(build_if_missing=True):
                                      ctypes.c_uint64, ctypes.c_void_p, P(ctypes.c_uint64), P(ctypes.c_uint64),
                                      ctypes.c_void_p]
     L.dmc_get_stats.argtypes = [ctypes.c_void_p, P(Stats)]
+    L.dmc_extract_batch.argtypes = [ctypes.c_void_p, P(_BatchItem), ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64,
+                                    ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
+                                    P(_BatchResult), P(ctypes.c_uint64), P(ctypes.c_uint64), ctypes.c_uint32,
+                                    ctypes.c_void_p]
+    L.dmc_batch_wait.argtypes = [ctypes.c_void_p, P(_BatchResult), P(ctypes.c_uint64), P(ctypes.c_uint64)]
+    L.dmc_set_option.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int64]
     for name in ABI_SYMBOLS:
         if name not in ("dmc_version", "dmc_tables_sha256", "dmc_status_string", "dmc_mesh_free"):
             getattr(L, name).restype = ctypes.c_int
@@ -225,7 +244,8 @@ class Extractor:
         bit patterns) or a raw device pointer with ``dims``/``dtype``.  Output
         buffers are CUDA tensors (float32 [V,3], int32/uint32 [Q,4]); returns
         (n_vertices, n_quads).  Raises DMCError(OUTPUT_OVERFLOW) carrying the
-        needed counts in ``.counts`` when the buffers are too small."""
+        needed counts in ``.counts`` when the buffers are too small; with no
+        output buffers at all it only counts."""
         if isinstance(volume, int):
             ptr, dims_xyz, dt = volume, dims, DTYPE[dtype]
         else:
@@ -248,11 +268,7 @@ class Extractor:
         if triangles is not None:
             qcap = min(qcap, triangles.numel() // 6)
         nv, nq = ctypes.c_uint64(), ctypes.c_uint64()
-        if stream is None:
-            # order the work after whatever torch queued on the current stream
-            import torch
-            stream = torch.cuda.current_stream()
-        st = stream.cuda_stream if hasattr(stream, "cuda_stream") else stream
+        st = _stream_handle(stream)
         rc = self._lib.dmc_extract_device(self._h, ctypes.byref(vol), _f3(mn), _f3(mx), ctypes.c_float(iso), 0,
                                           vptr, vcap, qptr, qcap, tptr, ctypes.byref(nv), ctypes.byref(nq), st)
         if rc != 0:
@@ -260,6 +276,98 @@ class Extractor:
             e.counts = (int(nv.value), int(nq.value))
             raise e
         return int(nv.value), int(nq.value)
+
+    def set_option(self, option, value):
+        """``dmc_set_option``: e.g. ``set_option(OPT_BRICK_PLANES, 16)``; 0 restores the automatic choice."""
+        _check(self._lib.dmc_set_option(self._h, int(option), int(value)), "dmc_set_option")
+
+    def extract_batch(self, volumes, vertices=None, quads=None, triangles=None, results=None, mode="sync",
+                      stream=None):
+        """Batched device-memory extraction (``dmc_extract_batch``).
+
+        ``volumes`` is a list of dicts with ``volume`` (CUDA tensor [z,y,x],
+        float32 or (u)int16 holding uint16 bits), ``iso`` and optional
+        ``xyz_min`` / ``xyz_max``.  ``results`` is an optional CUDA int64
+        tensor [n, 4] that receives (vertex_offset, n_vertices, quad_offset,
+        n_quads) per volume on the device.  ``mode`` "sync" returns
+        (n_vertices, n_quads, host results as an (n, 4) uint64 array);
+        "async" and "graph" enqueue on ``stream`` and return None:
+        ``batch_wait()`` then returns the same triple."""
+        n = len(volumes)
+        items = (_BatchItem * n)()
+        self._batch_keep = []
+        for i, d in enumerate(volumes):
+            t = d["volume"]
+            if not t.is_cuda or not t.is_contiguous() or t.dim() != 3:
+                raise DMCError(1, "batch volume %d must be a contiguous 3-D CUDA tensor" % i)
+            dt = {"float32": 0, "int16": 1, "uint16": 1}.get(str(t.dtype).replace("torch.", ""))
+            if dt is None:
+                raise DMCError(1, "batch volume %d dtype must be float32 or (u)int16" % i)
+            dims = (t.shape[2], t.shape[1], t.shape[0])
+            mn, mx = _default_extent(dims, d.get("xyz_min"), d.get("xyz_max"))
+            items[i].vol = _volume_struct(t.data_ptr(), dt, dims)
+            items[i].iso = float(d.get("iso", 0.0))
+            for k in range(3):
+                items[i].xyz_min[k] = float(mn[k])
+                items[i].xyz_max[k] = float(mx[k])
+        vptr = vertices.data_ptr() if vertices is not None else None
+        vcap = vertices.numel() // 3 if vertices is not None else 0
+        qptr = quads.data_ptr() if quads is not None else None
+        qcap = quads.numel() // 4 if quads is not None else 0
+        tptr = triangles.data_ptr() if triangles is not None else None
+        if triangles is not None:
+            qcap = min(qcap, triangles.numel() // 6)
+        rptr = None
+        if results is not None:
+            if not results.is_cuda or results.numel() < 4 * n or results.element_size() != 8:
+                raise DMCError(1, "results must be a CUDA 64-bit tensor with 4 entries per volume")
+            rptr = results.data_ptr()
+        st = _stream_handle(stream)
+        flags = {"sync": 0, "async": BATCH_ASYNC, "graph": BATCH_GRAPH}[mode]
+        hres = (_BatchResult * n)()
+        nv, nq = ctypes.c_uint64(), ctypes.c_uint64()
+        rc = self._lib.dmc_extract_batch(self._h, items, n, vptr, vcap, qptr, qcap, tptr, rptr, hres,
+                                         ctypes.byref(nv), ctypes.byref(nq), flags, st)
+        self._batch_n = n
+        if rc != 0:
+            e = DMCError(rc, "dmc_extract_batch")
+            e.counts = (int(nv.value), int(nq.value))
+            raise e
+        if flags:
+            return None
+        return int(nv.value), int(nq.value), _results_array(hres)
+
+    def batch_wait(self):
+        """``dmc_batch_wait``: completes an async/graph batch; returns (n_vertices, n_quads, results)."""
+        n = getattr(self, "_batch_n", 0)
+        hres = (_BatchResult * max(n, 1))()
+        nv, nq = ctypes.c_uint64(), ctypes.c_uint64()
+        rc = self._lib.dmc_batch_wait(self._h, hres, ctypes.byref(nv), ctypes.byref(nq))
+        if rc != 0:
+            e = DMCError(rc, "dmc_batch_wait")
+            e.counts = (int(nv.value), int(nq.value))
+            raise e
+        return int(nv.value), int(nq.value), _results_array(hres)[:n]
+
+
+_CUDA_STREAM_LEGACY = 0x1   # cudaStreamLegacy: the legacy default stream
+
+
+def _stream_handle(stream):
+    """cudaStream_t for the C ABI.  None: torch's current stream, so the work
+    is ordered after whatever torch queued there.  The C ABI reads a NULL
+    handle as the context's own stream, so torch's legacy default stream
+    (handle 0) is passed as cudaStreamLegacy."""
+    if stream is None:
+        import torch
+        stream = torch.cuda.current_stream()
+    st = stream.cuda_stream if hasattr(stream, "cuda_stream") else stream
+    st = int(st or 0)
+    return st if st else _CUDA_STREAM_LEGACY
+
+
+def _results_array(hres):
+    return np.array([[r.vertex_offset, r.n_vertices, r.quad_offset, r.n_quads] for r in hres], dtype=np.uint64).reshape(-1, 4)
 
 
 # ---------------------------------------------------------------------------

@@ -4,6 +4,7 @@
 #include <string.h>
 #include <new>
 #include "dmc_internal.h"
+#include <vector>
 
 namespace dmc {
 
@@ -17,6 +18,7 @@ dmc_status ctx_reserve_scratch(Ctx *ctx, size_t bytes)
     size_t want = bytes + bytes / 8;   // headroom: fewer re-allocations across calls
     CUDA_TRY(cudaMalloc(&ctx->scratch, want));
     ctx->scratch_bytes = want;
+    ++ctx->scratch_gen;
     return DMC_OK;
 }
 
@@ -190,6 +192,7 @@ dmc_status dmc_destroy(dmc_ctx *ctx)
     cudaFree(c->scratch); cudaFree(c->d_ctl); cudaFree(c->d_tab); cudaFree(c->d_vol);
     cudaFree(ctx->out.v); cudaFree(ctx->out.q); cudaFree(ctx->out.t);
     if (c->h_ctl) cudaFreeHost(c->h_ctl);
+    batch_state_free(c);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     for (int i = 0; i < 5; ++i)
@@ -232,12 +235,14 @@ dmc_status dmc_extract_device(dmc_ctx *ctx, const dmc_volume *vol, const float x
     if (s != DMC_OK) return s;
     if ((vertex_capacity && !d_vertices) || (quad_capacity && !d_quads)) return DMC_ERR_INVALID_ARG;
     Ctx *c = &ctx->c;
+    if (c->batch_pending) return DMC_ERR_INVALID_ARG;   // an asynchronous batch holds the scratch
     if (cudaSetDevice(c->device) != cudaSuccess) return DMC_ERR_CUDA;
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
     a.verts = d_vertices; a.vcap = vertex_capacity;
     a.quads = d_quads; a.qcap = quad_capacity;
     a.tris = d_triangles;
     a.n_vertices = n_vertices; a.n_quads = n_quads;
+    a.sizing_only = !d_vertices && !d_quads && !d_triangles;
     *n_vertices = 0; *n_quads = 0;
     c->stats = dmc_stats{};
     CUDA_TRY(cudaEventRecord(c->ev0, st));
@@ -250,6 +255,86 @@ dmc_status dmc_extract_device(dmc_ctx *ctx, const dmc_volume *vol, const float x
     return s;
 }
 
+dmc_status dmc_extract_batch(dmc_ctx *ctx, const dmc_batch_item *items, uint32_t n_items, float *d_vertices,
+                             uint64_t vertex_capacity, uint32_t *d_quads, uint64_t quad_capacity, uint32_t *d_triangles,
+                             dmc_batch_result *d_results, dmc_batch_result *results, uint64_t *n_vertices,
+                             uint64_t *n_quads, uint32_t flags, void *stream)
+{
+    if (!ctx || !items || n_items == 0) return DMC_ERR_INVALID_ARG;
+    if (flags & ~(DMC_BATCH_ASYNC | DMC_BATCH_GRAPH)) return DMC_ERR_INVALID_ARG;
+    if ((vertex_capacity && !d_vertices) || (quad_capacity && !d_quads)) return DMC_ERR_INVALID_ARG;
+    const bool async = flags != 0;
+    if (!async && (!n_vertices || !n_quads)) return DMC_ERR_INVALID_ARG;
+    Ctx *c = &ctx->c;
+    if (c->batch_pending) return DMC_ERR_INVALID_ARG;   // dmc_batch_wait first
+    std::vector<BrickItem> bi(n_items);
+    for (uint32_t i = 0; i < n_items; ++i) {
+        ExtractArgs a;
+        dmc_status s = make_args(&items[i].vol, items[i].xyz_min, items[i].xyz_max, items[i].iso, a);
+        if (s != DMC_OK) return s;
+        BrickItem &it = bi[i];
+        it.data = a.vol; it.dtype = a.dtype; it.pts = a.pts; it.cells = a.cells; it.iso = a.iso; it.mn = a.mn; it.rng = a.rng;
+    }
+    if (cudaSetDevice(c->device) != cudaSuccess) return DMC_ERR_CUDA;
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    BrickOut o{};
+    o.verts = d_vertices; o.vcap = vertex_capacity;
+    o.quads = d_quads; o.qcap = quad_capacity;
+    o.tris = d_triangles;
+    o.d_results = d_results;
+    o.h_results = async ? nullptr : results;
+    o.n_vertices = async ? nullptr : n_vertices;
+    o.n_quads = async ? nullptr : n_quads;
+    o.mode = (flags & DMC_BATCH_GRAPH) ? BATCH_GRAPH : async ? BATCH_ASYNC : BATCH_SYNC;
+    o.sizing_only = !async && !d_vertices && !d_quads && !d_triangles;
+    if (!async) { *n_vertices = 0; *n_quads = 0; }
+    c->stats = dmc_stats{};
+    c->stats.algo = DMC_ALGO_BRICK;
+    c->evk_used = 0;
+    CUDA_TRY(cudaEventRecord(c->ev0, st));
+    dmc_status s = brick_extract(c, bi.data(), n_items, o, st);
+    if (s != DMC_OK) return s;
+    CUDA_TRY(cudaEventRecord(c->ev1, st));
+    if (async) {
+        c->batch_pending = true;
+        return DMC_OK;
+    }
+    cudaEventSynchronize(c->ev1);
+    cudaEventElapsedTime(&c->stats.device_ms, c->ev0, c->ev1);
+    if (c->evk_used >= 2) {
+        cudaEventElapsedTime(&c->stats.count_ms, c->evk[0], c->evk[1]);
+        cudaEventElapsedTime(&c->stats.scan_ms, c->evk[1], c->evk[2]);
+        cudaEventElapsedTime(&c->stats.emit_ms, c->evk[3], c->evk[4]);
+    }
+    c->evk_used = 0;
+    return DMC_OK;
+}
+
+dmc_status dmc_batch_wait(dmc_ctx *ctx, dmc_batch_result *results, uint64_t *n_vertices, uint64_t *n_quads)
+{
+    if (!ctx) return DMC_ERR_INVALID_ARG;
+    Ctx *c = &ctx->c;
+    if (!c->batch_pending) return DMC_ERR_INVALID_ARG;
+    c->batch_pending = false;
+    if (cudaSetDevice(c->device) != cudaSuccess) return DMC_ERR_CUDA;
+    dmc_status s = brick_wait(c, results, n_vertices, n_quads);
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess) c->stats.device_ms = ms;
+    return s;
+}
+
+dmc_status dmc_set_option(dmc_ctx *ctx, dmc_option opt, int64_t value)
+{
+    if (!ctx) return DMC_ERR_INVALID_ARG;
+    switch (opt) {
+    case DMC_OPT_BRICK_PLANES:
+        if (value < 0 || value > 256) return DMC_ERR_INVALID_ARG;
+        ctx->c.brick_zc = (uint32_t)value;
+        return DMC_OK;
+    }
+    return DMC_ERR_INVALID_ARG;
+}
+
 dmc_status dmc_run(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min[3], const float xyz_max[3],
                    float iso, uint32_t num_smooth, int want_triangles, dmc_mesh *out)
 {
@@ -260,6 +345,7 @@ dmc_status dmc_run(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min[3], 
     dmc_status s = make_args(vol, xyz_min, xyz_max, iso, a);
     if (s != DMC_OK) return s;
     Ctx *c = &ctx->c;
+    if (c->batch_pending) return DMC_ERR_INVALID_ARG;   // an asynchronous batch holds the scratch
     if (cudaSetDevice(c->device) != cudaSuccess) return DMC_ERR_CUDA;
     cudaStream_t st = c->stream;
     c->stats = dmc_stats{};

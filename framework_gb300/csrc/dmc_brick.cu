@@ -26,6 +26,9 @@
 #include "dmc_device.cuh"
 #include "dmc_scan.cuh"
 #include "dmc_internal.h"
+#include <algorithm>
+#include <new>
+#include <vector>
 
 namespace dmc {
 
@@ -42,15 +45,21 @@ constexpr int NWB = 8;                    // warps per block (independent)
 constexpr int QBUF = 96;                  // quads of one round of owner cells (3 per cell)
 constexpr int SCAN_NT = 256, SCAN_ITEMS = 8, SCAN_TILE = SCAN_NT * SCAN_ITEMS;
 
+// One volume of an extraction (a plain call has one, a batch many).
 struct Geom {
+    const void *data;
     uint3 pts, cells;
     uint32_t nxs, nyb, nzb, zc;
-    uint64_t nbricks;
+    uint64_t brick_base;   // first brick of this volume in the launch's brick numbering
+    uint64_t seg_base;     // first segment of this volume in the shared segment arrays
+    uint64_t nseg;
     float iso;
     uint32_t iso_u16;      // uint16 samples: v < iso  <=>  v < iso_u16 (65536: always)
     uint32_t isole_u16;    // uint16 samples: v <= iso <=>  v < isole_u16
     float3 mn, rng;
     const float *coord;    // point coordinates: x[0..cx], y[0..cy], z[0..cz]
+    uint32_t vbase, qbase; // first vertex / quad of this volume in the output (set after the scan)
+    uint32_t item;         // position of the volume in the caller's list
 };
 
 struct alignas(16) PlaneMasks {
@@ -95,24 +104,21 @@ struct WarpMem {
     Spill *g;
     __device__ __forceinline__ uint32_t &ent(int p, uint32_t i)
     {
-        uint32_t *b = i < CAP ? s->ent[p] : g->ent[p] - CAP;
-        return b[i];
+        return i < CAP ? s->ent[p][i] : g->ent[p][i - CAP];
     }
     __device__ __forceinline__ uint16_t &lst(int p, uint32_t i)
     {
-        uint16_t *b = i < CAP ? (p ? s->lst1 : s->lst0) : g->lst[p] - CAP;
-        return b[i];
+        return i < CAP ? (p ? s->lst1 : s->lst0)[i] : g->lst[p][i - CAP];
     }
     __device__ __forceinline__ uint8_t &info(int p, uint32_t i)
     {
-        uint8_t *b = i < CAP ? s->info[p] : g->info[p] - CAP;
-        return b[i];
+        return i < CAP ? s->info[p][i] : g->info[p][i - CAP];
     }
 };
 
 __device__ __forceinline__ uint64_t seg_index(const Geom &g, uint32_t k, uint32_t j, uint32_t xs)
 {
-    return ((uint64_t)k * g.cells.y + j) * g.nxs + xs;
+    return g.seg_base + ((uint64_t)k * g.cells.y + j) * g.nxs + xs;
 }
 
 template <class T>
@@ -369,6 +375,23 @@ struct EmitOut {
     uint32_t *tris;
 };
 
+// Device-resident plan of one pipeline launch (a plain call is a batch of
+// one).  The host writes it to pinned memory and one copy moves it to the
+// device, so the kernels take every batch-dependent size from here and a
+// captured graph replays any batch that fits the scratch layout.
+struct alignas(64) BatchHead {
+    unsigned long long nbricks[2];   // bricks of the f32 / u16 volumes
+    unsigned long long nseg;         // segments of all volumes
+    uint32_t nvol[2];                // geoms[]: the f32 volumes, then the u16 ones
+    uint32_t n;                      // volumes
+    uint32_t n_tiles;                // scan tiles over nseg
+};
+
+__device__ __forceinline__ const Geom *batch_geoms(const BatchHead *h)
+{
+    return reinterpret_cast<const Geom *>(h + 1);
+}
+
 // Stage the lookup tables in shared memory (once per block; warps are persistent).
 __device__ __forceinline__ const DeviceTables &stage_tables(const DeviceTables *g, DeviceTables *s)
 {
@@ -420,13 +443,14 @@ __device__ __forceinline__ uint32_t ring_edge(int s, int kk)
 // Active cells are compacted per plane in output order and processed 32 at a
 // time, one per lane; quads are compacted the same way.
 template <class T, bool EMIT>
-__global__ void __launch_bounds__(32 * NWB, EMIT ? 2 : 4) brick_sweep(const T *__restrict__ vol, Geom g,
+__global__ void __launch_bounds__(32 * NWB, EMIT ? 2 : 4) brick_sweep(const BatchHead *__restrict__ head, uint32_t group,
                                                         const DeviceTables *__restrict__ tabp,
                                                         uint2 *__restrict__ seg_cnt, EmitOut out,
                                                         Spill *__restrict__ spill, uint32_t *ticket,
                                                         unsigned long long *counters, uint32_t *err)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    if (head->nbricks[group] == 0) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const DeviceTables &tab = stage_tables(tabp, reinterpret_cast<DeviceTables *>(smem_raw));
     // the count sweep gives each warp only the SweepSmem part
@@ -434,10 +458,22 @@ __global__ void __launch_bounds__(32 * NWB, EMIT ? 2 : 4) brick_sweep(const T *_
     WarpMem M{&S, spill + (uint64_t)blockIdx.x * NWB + warp};
     constexpr uint32_t NR = EMIT ? HROWS : ROWS;   // ranked rows
     uint32_t n_act = 0, n_l2 = 0, n_drop = 0;
+    const uint32_t nvols = head->nvol[group];
+    const uint64_t nbricks = head->nbricks[group];
+    const Geom *__restrict__ vols = batch_geoms(head) + (group ? head->nvol[0] : 0u);
 
     for (;;) {
-        const uint32_t b = claim_brick(ticket, lane);
-        if (b >= g.nbricks) break;
+        const uint32_t bg = claim_brick(ticket, lane);
+        if (bg >= nbricks) break;
+        // volume of this brick: last one whose first brick is <= bg
+        uint32_t lo = 0, hi = nvols - 1;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) >> 1;
+            if (vols[mid].brick_base <= bg) lo = mid; else hi = mid - 1;
+        }
+        const Geom g = vols[lo];
+        const T *__restrict__ vol = reinterpret_cast<const T *>(g.data);
+        const uint32_t b = (uint32_t)(bg - g.brick_base);
         const uint32_t xs = b % g.nxs, yb = (b / g.nxs) % g.nyb, zb = b / (g.nxs * g.nyb);
         const uint32_t x0 = xs * W, y0 = yb * ROWS, z0 = zb * g.zc;
         const uint32_t z1 = min(z0 + g.zc, g.cells.z);
@@ -655,7 +691,7 @@ __global__ void __launch_bounds__(32 * NWB, EMIT ? 2 : 4) brick_sweep(const T *_
                                     const uint32_t rd = M.ent(pl, li);
                                     uint32_t m = lut_m(tab, cell_cfg(rd), cell_l2(rd), (int)ring_edge(s, kk));
                                     if (m == 0xffu) { atomicOr(err, DEV_ERR_BOUNDS); m = 0; }
-                                    idx[it] = S.segv[pl][r + dr][(c + (int)plus) == W ? 1 : 0] + cell_vrel(rd) + m;
+                                    idx[it] = S.segv[pl][r + dr][(c + (int)plus) == W ? 1 : 0] + cell_vrel(rd) + m - g.vbase;
                                 }
                                 reinterpret_cast<uint4 *>(out.quads)[q] = make_uint4(idx[0], idx[1], idx[2], idx[3]);
                                 if (out.tris) {
@@ -686,45 +722,84 @@ __global__ void __launch_bounds__(32 * NWB, EMIT ? 2 : 4) brick_sweep(const T *_
     }
 }
 
-// point coordinates x(i) = ijk_to_xyz(i, cells.x, ...) etc. (utils.hpp:118-122)
-__global__ void coord_table(float *coord, uint3 pts, uint3 cells, float3 rng, float3 mn)
+// Start of a pipeline launch: zero the scan tiles, tickets and control block
+// and fill each volume's point coordinates x(i) = ijk_to_xyz(i, cells.x, ...)
+// (utils.hpp:118-122).  Blocks stride over volumes, threads over points.
+__global__ void batch_prep(const BatchHead *__restrict__ head, TileState *tiles, uint32_t *tickets, DevCtl *ctl)
 {
-    const uint32_t n = pts.x + pts.y + pts.z;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float v;
-        if (i < pts.x) v = ijk_to_xyz(i, cells.x, rng.x, mn.x);
-        else if (i < pts.x + pts.y) v = ijk_to_xyz(i - pts.x, cells.y, rng.y, mn.y);
-        else v = ijk_to_xyz(i - pts.x - pts.y, cells.z, rng.z, mn.z);
-        coord[i] = v;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    for (uint32_t t = tid; t < head->n_tiles; t += nth) tiles[t] = TileState{};
+    if (tid < 64) tickets[tid] = 0;
+    if (tid < sizeof(DevCtl) / 4) reinterpret_cast<uint32_t *>(ctl)[tid] = 0;
+    const Geom *vols = batch_geoms(head);
+    for (uint32_t v = blockIdx.x; v < head->n; v += gridDim.x) {
+        const Geom &g = vols[v];
+        float *coord = const_cast<float *>(g.coord);
+        const uint32_t n = g.pts.x + g.pts.y + g.pts.z;
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+            float c;
+            if (i < g.pts.x) c = ijk_to_xyz(i, g.cells.x, g.rng.x, g.mn.x);
+            else if (i < g.pts.x + g.pts.y) c = ijk_to_xyz(i - g.pts.x, g.cells.y, g.rng.y, g.mn.y);
+            else c = ijk_to_xyz(i - g.pts.x - g.pts.y, g.cells.z, g.rng.z, g.mn.z);
+            coord[i] = c;
+        }
+    }
+}
+
+// After the scan: each volume's first vertex / quad and its counts.
+__global__ void volume_results(BatchHead *head, const uint2 *seg_cnt, const uint2 *seg_off,
+                               const unsigned long long *totals, dmc_batch_result *res)
+{
+    Geom *vols = const_cast<Geom *>(batch_geoms(head));
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < head->n; v += gridDim.x * blockDim.x) {
+        Geom &g = vols[v];
+        dmc_batch_result r{0, 0, 0, 0};
+        if (!g.nseg) {
+            // no cells: an empty slice where the next volume starts
+            if (g.seg_base < head->nseg) { r.vertex_offset = seg_off[g.seg_base].x; r.quad_offset = seg_off[g.seg_base].y; }
+            else { r.vertex_offset = totals[0]; r.quad_offset = totals[1]; }
+        } else {
+            const uint2 f = seg_off[g.seg_base], lo = seg_off[g.seg_base + g.nseg - 1], lc = seg_cnt[g.seg_base + g.nseg - 1];
+            r.vertex_offset = f.x; r.n_vertices = (unsigned long long)lo.x + lc.x - f.x;
+            r.quad_offset = f.y; r.n_quads = (unsigned long long)lo.y + lc.y - f.y;
+            g.vbase = f.x; g.qbase = f.y;
+        }
+        if (res) res[g.item] = r;
     }
 }
 
 // ---------------------------------------------------------------------------
 // segment scan (decoupled look-back)
 
-__global__ void __launch_bounds__(SCAN_NT) seg_scan(const uint2 *__restrict__ cnt, uint64_t n, ScanCtl ctl,
-                                                    uint2 *__restrict__ off)
+__global__ void __launch_bounds__(SCAN_NT) seg_scan(const BatchHead *__restrict__ head, const uint2 *__restrict__ cnt,
+                                                    ScanCtl ctl, uint2 *__restrict__ off)
 {
     __shared__ uint32_t s_slot;
     __shared__ unsigned long long s_warp[SCAN_NT / 32 + 1];
     __shared__ unsigned long long s_ex[2];
-    const uint32_t tile = claim_tile(ctl.ticket, &s_slot);
-    const uint64_t first = (uint64_t)tile * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
-    uint2 c[SCAN_ITEMS];
-    uint32_t sv = 0, sq = 0;
+    const uint64_t n = head->nseg;
+    ctl.n_tiles = head->n_tiles;
+    // tiles are claimed in order, so a tile only waits on tiles whose blocks already run
+    for (;;) {
+        const uint32_t tile = claim_tile(ctl.ticket, &s_slot);
+        if (tile >= ctl.n_tiles) break;
+        const uint64_t first = (uint64_t)tile * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
+        uint2 c[SCAN_ITEMS];
+        uint32_t sv = 0, sq = 0;
 #pragma unroll
-    for (int i = 0; i < SCAN_ITEMS; ++i) {
-        c[i] = first + i < n ? cnt[first + i] : make_uint2(0, 0);
-        sv += c[i].x; sq += c[i].y;
-    }
-    unsigned long long tot;
-    unsigned long long ex = block_exclusive_scan<SCAN_NT>((unsigned long long)sv | ((unsigned long long)sq << 32), s_warp, &tot);
-    tile_prefix(ctl, tile, (uint32_t)tot, (uint32_t)(tot >> 32), s_ex);
-    unsigned long long bv = s_ex[0] + (uint32_t)ex, bq = s_ex[1] + (uint32_t)(ex >> 32);
+        for (int i = 0; i < SCAN_ITEMS; ++i) {
+            c[i] = first + i < n ? cnt[first + i] : make_uint2(0, 0);
+            sv += c[i].x; sq += c[i].y;
+        }
+        unsigned long long tot;
+        unsigned long long ex = block_exclusive_scan<SCAN_NT>((unsigned long long)sv | ((unsigned long long)sq << 32), s_warp, &tot);
+        tile_prefix(ctl, tile, (uint32_t)tot, (uint32_t)(tot >> 32), s_ex);
+        unsigned long long bv = s_ex[0] + (uint32_t)ex, bq = s_ex[1] + (uint32_t)(ex >> 32);
 #pragma unroll
-    for (int i = 0; i < SCAN_ITEMS; ++i) {
-        if (first + i < n) off[first + i] = make_uint2((uint32_t)bv, (uint32_t)bq);
-        bv += c[i].x; bq += c[i].y;
+        for (int i = 0; i < SCAN_ITEMS; ++i) {
+            if (first + i < n) off[first + i] = make_uint2((uint32_t)bv, (uint32_t)bq);
+            bv += c[i].x; bq += c[i].y;
+        }
     }
 }
 
@@ -753,108 +828,418 @@ static int sweep_grid(Ctx *ctx)
     return b * ctx->num_sms;
 }
 
-template <class T>
-static dmc_status brick_run_v(Ctx *ctx, const T *vol, const ExtractArgs &a, cudaStream_t st)
+static void iso_thresholds(float f, uint32_t &lt, uint32_t &le)
 {
-    using namespace brick;
-    Geom g;
-    g.pts = a.pts; g.cells = a.cells; g.iso = a.iso; g.mn = a.mn; g.rng = a.rng;
-    {
-        // uint16 compare threshold: smallest integer t with (v < iso) == (v < t)
-        float f = a.iso;
-        uint32_t t;
-        if (!(f > 0.f)) t = 0;                       // also NaN
-        else if (f > 65535.f) t = 65536;
-        else { uint32_t fl = (uint32_t)f; t = ((float)fl == f) ? fl : fl + 1; }
-        g.iso_u16 = t;
-        // v <= iso  <=>  v < floor(iso) + 1
-        uint32_t te;
-        if (!(f >= 0.f)) te = 0;
-        else if (f >= 65535.f) te = 65536;
-        else te = (uint32_t)f + 1;
-        g.isole_u16 = te;
+    // uint16 samples: v < iso <=> v < lt;  v <= iso <=> v < le (floor(iso) + 1)
+    if (!(f > 0.f)) lt = 0;                       // also NaN
+    else if (f > 65535.f) lt = 65536;
+    else { const uint32_t fl = (uint32_t)f; lt = ((float)fl == f) ? fl : fl + 1; }
+    if (!(f >= 0.f)) le = 0;
+    else if (f >= 65535.f) le = 65536;
+    else le = (uint32_t)f + 1;
+}
+
+// Per-context pipeline state.  Scratch (device) and staging (pinned host) are
+// laid out for capacities that only grow; a captured graph holds the
+// addresses of both, plus the output buffers, and is re-captured when any of
+// them changes.
+struct BatchState {
+    // capacities of the layout
+    uint32_t cap_items = 0;
+    uint64_t cap_seg = 0, cap_coord = 0;
+    uint64_t layout_gen = 0;           // scratch_gen the layout was carved for (0: none)
+    // device layout (inside ctx->scratch)
+    brick::BatchHead *d_plan = nullptr;
+    uint2 *seg_cnt = nullptr, *seg_off = nullptr;
+    TileState *tiles = nullptr;
+    brick::Spill *spill = nullptr;
+    float *coord = nullptr;
+    dmc_batch_result *d_res = nullptr;
+    uint32_t *tickets = nullptr;
+    size_t plan_bytes = 0;
+    // pinned staging: plan, then the per-volume results
+    void *h_stage = nullptr;
+    size_t h_stage_bytes = 0;
+    uint64_t stage_gen = 0;
+    // grids of the persistent sweeps [dtype][emit]
+    int grid[2][2] = {{0, 0}, {0, 0}};
+    // cached graph, the layout it was captured for, and its emit nodes,
+    // whose output arguments are rewritten when a batch targets other buffers
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    uint64_t g_scratch_gen = 0, g_stage_gen = 0;
+    cudaGraphNode_t emit_node[2] = {nullptr, nullptr};
+    cudaKernelNodeParams emit_params[2]{};
+    brick::EmitOut g_out{};
+    // batch in flight
+    bool in_flight = false;
+    uint32_t n_inflight = 0;
+    cudaEvent_t done = nullptr;
+};
+
+void batch_state_free(Ctx *ctx)
+{
+    BatchState *b = ctx->batch;
+    if (!b) return;
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->done) cudaEventDestroy(b->done);
+    if (b->h_stage) cudaFreeHost(b->h_stage);
+    delete b;
+    ctx->batch = nullptr;
+}
+
+static dmc_status batch_state(Ctx *ctx, BatchState **out)
+{
+    if (!ctx->batch) {
+        BatchState *b = new (std::nothrow) BatchState();
+        if (!b) return DMC_ERR_OOM;
+        ctx->batch = b;
+        b->grid[0][0] = sweep_grid<float, false>(ctx);
+        b->grid[0][1] = sweep_grid<float, true>(ctx);
+        b->grid[1][0] = sweep_grid<uint16_t, false>(ctx);
+        b->grid[1][1] = sweep_grid<uint16_t, true>(ctx);
+        CUDA_TRY(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
     }
-    g.nxs = (a.cells.x + W - 1) / W;
-    g.nyb = (a.cells.y + ROWS - 1) / ROWS;
-    const int grid = sweep_grid<T, true>(ctx), cgrid = sweep_grid<T, false>(ctx);
-    // planes per brick: long sweeps amortise the z halo, but keep at least
-    // three bricks per warp so that the persistent warps stay busy
-    g.zc = 32;
-    while (g.zc > 4 && (uint64_t)g.nxs * g.nyb * ((a.cells.z + g.zc - 1) / g.zc) < 3ull * grid * NWB) g.zc >>= 1;
-    g.nzb = (a.cells.z + g.zc - 1) / g.zc;
-    g.nbricks = (uint64_t)g.nxs * g.nyb * g.nzb;
-    if (g.nbricks >= 0xF0000000ull) return DMC_ERR_UNSUPPORTED;
-    const uint64_t nseg = (uint64_t)a.cells.z * a.cells.y * g.nxs;
-    const uint64_t n_tiles64 = (nseg + SCAN_TILE - 1) / SCAN_TILE;
-    if (n_tiles64 >= (1ull << 31)) return DMC_ERR_UNSUPPORTED;
-    const uint32_t n_tiles = (uint32_t)n_tiles64;
-    const uint64_t n_coord = (uint64_t)a.pts.x + a.pts.y + a.pts.z;
-
-    size_t off = 0;
-    auto carve = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~(size_t)255; return o; };
-    const size_t o_cnt = carve(8 * nseg), o_off = carve(8 * nseg), o_tiles = carve(sizeof(TileState) * n_tiles);
-    const size_t o_spill = carve(sizeof(Spill) * (size_t)(grid > cgrid ? grid : cgrid) * NWB);
-    const size_t o_coord = carve(4 * n_coord);
-    const size_t o_tk = carve(256);
-    dmc_status s = ctx_reserve_scratch(ctx, off);
-    if (s != DMC_OK) return s;
-    uint8_t *base = (uint8_t *)ctx->scratch;
-    uint2 *seg_cnt = (uint2 *)(base + o_cnt), *seg_off = (uint2 *)(base + o_off);
-    TileState *tiles = (TileState *)(base + o_tiles);
-    Spill *spill = (Spill *)(base + o_spill);
-    float *coord = (float *)(base + o_coord);
-    uint32_t *tickets = (uint32_t *)(base + o_tk);
-    g.coord = coord;
-
-    CUDA_TRY(cudaMemsetAsync(tiles, 0, sizeof(TileState) * n_tiles, st));
-    CUDA_TRY(cudaMemsetAsync(tickets, 0, 256, st));
-    CUDA_TRY(cudaMemsetAsync(ctx->d_ctl, 0, sizeof(DevCtl), st));
-    coord_table<<<(unsigned)((n_coord + 255) / 256), 256, 0, st>>>(coord, a.pts, a.cells, a.rng, a.mn);
-    ctx->evk_used = 0;
-    CUDA_TRY(cudaEventRecord(ctx->evk[0], st));
-    brick_sweep<T, false><<<cgrid, 32 * NWB, kCountSmem, st>>>(vol, g, ctx->d_tab, seg_cnt, EmitOut{}, spill,
-                                                                    &tickets[0], ctx->d_ctl->counters, &ctx->d_ctl->err);
-    CUDA_TRY(cudaGetLastError());
-    CUDA_TRY(cudaEventRecord(ctx->evk[1], st));
-    ScanCtl ctl;
-    ctl.tiles = tiles; ctl.ticket = &ctx->d_ctl->ticket; ctl.err = &ctx->d_ctl->err;
-    ctl.totals = ctx->d_ctl->totals; ctl.n_tiles = n_tiles;
-    seg_scan<<<n_tiles, SCAN_NT, 0, st>>>(seg_cnt, nseg, ctl, seg_off);
-    CUDA_TRY(cudaGetLastError());
-    CUDA_TRY(cudaEventRecord(ctx->evk[2], st));
-    ctx->evk_used = 1;
-    CUDA_TRY(cudaMemcpyAsync(ctx->h_ctl, ctx->d_ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaStreamSynchronize(st));
-    if (ctx->h_ctl->err & DEV_ERR_TIMEOUT) return DMC_ERR_TIMEOUT;
-    const uint64_t V = ctx->h_ctl->totals[0], Q = ctx->h_ctl->totals[1];
-    *a.n_vertices = V; *a.n_quads = Q;
-    ctx->stats.n_active_cells = ctx->h_ctl->counters[0];
-    ctx->stats.n_lut2_cells = ctx->h_ctl->counters[1];
-    ctx->stats.n_dropped_quads = ctx->h_ctl->counters[2];
-    if (V >= 0xFFFFFFFFull || Q >= 0xFFFFFFFFull) return DMC_ERR_OUTPUT_OVERFLOW;
-    if (a.sizing_only) return DMC_OK;
-    if (V > a.vcap || Q > a.qcap) return DMC_ERR_OUTPUT_OVERFLOW;
-    EmitOut eo;
-    eo.seg_off = seg_off; eo.verts = a.verts; eo.vcap = a.vcap; eo.quads = a.quads; eo.qcap = a.qcap; eo.tris = a.tris;
-    CUDA_TRY(cudaEventRecord(ctx->evk[3], st));
-    brick_sweep<T, true><<<grid, 32 * NWB, kEmitSmem, st>>>(vol, g, ctx->d_tab, nullptr, eo, spill, &tickets[1],
-                                                                   ctx->d_ctl->counters, &ctx->d_ctl->err);
-    CUDA_TRY(cudaGetLastError());
-    CUDA_TRY(cudaEventRecord(ctx->evk[4], st));
-    ctx->evk_used = 2;
+    *out = ctx->batch;
     return DMC_OK;
 }
 
-template <class T>
-static dmc_status brick_run_t(Ctx *ctx, const T *vol, const ExtractArgs &a, cudaStream_t st)
+// Carves the scratch and staging for at least the given capacities.
+static dmc_status batch_layout(Ctx *ctx, BatchState &b, uint32_t items, uint64_t seg, uint64_t ncoord)
 {
-    return brick_run_v<T>(ctx, vol, a, st);
+    using namespace brick;
+    const bool fits = b.layout_gen == ctx->scratch_gen && items <= b.cap_items && seg <= b.cap_seg && ncoord <= b.cap_coord;
+    if (fits) return DMC_OK;
+    // grow with headroom so that a stream of similar batches settles on one layout
+    b.cap_items = std::max<uint32_t>(b.cap_items, items + items / 4 + 1);
+    b.cap_seg = std::max<uint64_t>(b.cap_seg, seg + seg / 4 + SCAN_TILE);
+    b.cap_coord = std::max<uint64_t>(b.cap_coord, ncoord + ncoord / 4 + 64);
+    const uint64_t cap_tiles = (b.cap_seg + SCAN_TILE - 1) / SCAN_TILE;
+    const int gmax = std::max(std::max(b.grid[0][0], b.grid[0][1]), std::max(b.grid[1][0], b.grid[1][1]));
+    b.plan_bytes = sizeof(BatchHead) + sizeof(Geom) * (size_t)b.cap_items;
+    size_t off = 0;
+    auto carve = [&](size_t bytes) { size_t r = off; off += (bytes + 255) & ~(size_t)255; return r; };
+    const size_t o_plan = carve(b.plan_bytes);
+    const size_t o_cnt = carve(8 * b.cap_seg), o_off = carve(8 * b.cap_seg);
+    const size_t o_tiles = carve(sizeof(TileState) * cap_tiles);
+    const size_t o_spill = carve(sizeof(Spill) * (size_t)gmax * NWB);
+    const size_t o_coord = carve(4 * b.cap_coord);
+    const size_t o_res = carve(sizeof(dmc_batch_result) * (size_t)b.cap_items);
+    const size_t o_tk = carve(256);
+    if (b.in_flight) return DMC_ERR_INVALID_ARG;
+    dmc_status s = ctx_reserve_scratch(ctx, off);
+    if (s != DMC_OK) return s;
+    uint8_t *base = (uint8_t *)ctx->scratch;
+    b.d_plan = (BatchHead *)(base + o_plan);
+    b.seg_cnt = (uint2 *)(base + o_cnt);
+    b.seg_off = (uint2 *)(base + o_off);
+    b.tiles = (TileState *)(base + o_tiles);
+    b.spill = (Spill *)(base + o_spill);
+    b.coord = (float *)(base + o_coord);
+    b.d_res = (dmc_batch_result *)(base + o_res);
+    b.tickets = (uint32_t *)(base + o_tk);
+    b.layout_gen = ctx->scratch_gen;
+    const size_t stage = b.plan_bytes + sizeof(dmc_batch_result) * (size_t)b.cap_items;
+    if (stage > b.h_stage_bytes) {
+        if (b.h_stage) { CUDA_TRY(cudaDeviceSynchronize()); cudaFreeHost(b.h_stage); b.h_stage = nullptr; b.h_stage_bytes = 0; }
+        CUDA_TRY(cudaMallocHost(&b.h_stage, stage));
+        b.h_stage_bytes = stage;
+        ++b.stage_gen;
+    }
+    return DMC_OK;
+}
+
+static dmc_batch_result *stage_results(BatchState &b)
+{
+    return (dmc_batch_result *)((uint8_t *)b.h_stage + b.plan_bytes);
+}
+
+// Front half: plan upload, prep, count sweeps, scan, per-volume offsets.
+// Sweeps of a sample type without bricks are skipped unless `all` (a graph
+// must serve any later mix of types).
+static dmc_status enqueue_front(Ctx *ctx, BatchState &b, dmc_batch_result *d_res, bool timed, const uint64_t nb[2],
+                                bool all, cudaStream_t st)
+{
+    using namespace brick;
+    CUDA_TRY(cudaMemcpyAsync(b.d_plan, b.h_stage, b.plan_bytes, cudaMemcpyHostToDevice, st));
+    batch_prep<<<2 * ctx->num_sms, 256, 0, st>>>(b.d_plan, b.tiles, b.tickets, ctx->d_ctl);
+    CUDA_TRY(cudaGetLastError());
+    if (timed) CUDA_TRY(cudaEventRecord(ctx->evk[0], st));
+    if (all || nb[0]) {
+        brick_sweep<float, false><<<b.grid[0][0], 32 * NWB, kCountSmem, st>>>(
+            b.d_plan, 0, ctx->d_tab, b.seg_cnt, EmitOut{}, b.spill, &b.tickets[0], ctx->d_ctl->counters, &ctx->d_ctl->err);
+        CUDA_TRY(cudaGetLastError());
+    }
+    if (all || nb[1]) {
+        brick_sweep<uint16_t, false><<<b.grid[1][0], 32 * NWB, kCountSmem, st>>>(
+            b.d_plan, 1, ctx->d_tab, b.seg_cnt, EmitOut{}, b.spill, &b.tickets[1], ctx->d_ctl->counters, &ctx->d_ctl->err);
+        CUDA_TRY(cudaGetLastError());
+    }
+    if (timed) CUDA_TRY(cudaEventRecord(ctx->evk[1], st));
+    ScanCtl ctl;
+    ctl.tiles = b.tiles; ctl.ticket = &ctx->d_ctl->ticket; ctl.err = &ctx->d_ctl->err;
+    ctl.totals = ctx->d_ctl->totals; ctl.n_tiles = 0;
+    seg_scan<<<2 * ctx->num_sms, SCAN_NT, 0, st>>>(b.d_plan, b.seg_cnt, ctl, b.seg_off);
+    CUDA_TRY(cudaGetLastError());
+    volume_results<<<4, 128, 0, st>>>(b.d_plan, b.seg_cnt, b.seg_off, ctx->d_ctl->totals, d_res);
+    CUDA_TRY(cudaGetLastError());
+    if (timed) CUDA_TRY(cudaEventRecord(ctx->evk[2], st));
+    return DMC_OK;
+}
+
+// Back half: emit sweeps, then the control block and results to pinned memory.
+static dmc_status enqueue_back(Ctx *ctx, BatchState &b, const brick::EmitOut &eo, dmc_batch_result *d_res, bool timed,
+                               const uint64_t nb[2], bool all, cudaStream_t st)
+{
+    using namespace brick;
+    if (timed) CUDA_TRY(cudaEventRecord(ctx->evk[3], st));
+    if (all || nb[0]) {
+        brick_sweep<float, true><<<b.grid[0][1], 32 * NWB, kEmitSmem, st>>>(
+            b.d_plan, 0, ctx->d_tab, nullptr, eo, b.spill, &b.tickets[2], ctx->d_ctl->counters, &ctx->d_ctl->err);
+        CUDA_TRY(cudaGetLastError());
+    }
+    if (all || nb[1]) {
+        brick_sweep<uint16_t, true><<<b.grid[1][1], 32 * NWB, kEmitSmem, st>>>(
+            b.d_plan, 1, ctx->d_tab, nullptr, eo, b.spill, &b.tickets[3], ctx->d_ctl->counters, &ctx->d_ctl->err);
+        CUDA_TRY(cudaGetLastError());
+    }
+    if (timed) CUDA_TRY(cudaEventRecord(ctx->evk[4], st));
+    CUDA_TRY(cudaMemcpyAsync(ctx->h_ctl, ctx->d_ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(stage_results(b), d_res, sizeof(dmc_batch_result) * (size_t)b.cap_items,
+                             cudaMemcpyDeviceToHost, st));
+    return DMC_OK;
+}
+
+static void stats_from_ctl(Ctx *ctx)
+{
+    ctx->stats.n_vertices = ctx->h_ctl->totals[0];
+    ctx->stats.n_quads = ctx->h_ctl->totals[1];
+    ctx->stats.n_active_cells = ctx->h_ctl->counters[0];
+    ctx->stats.n_lut2_cells = ctx->h_ctl->counters[1];
+    ctx->stats.n_dropped_quads = ctx->h_ctl->counters[2];
+}
+
+static dmc_status ctl_status(const DevCtl *c)
+{
+    if (c->err & DEV_ERR_TIMEOUT) return DMC_ERR_TIMEOUT;
+    if (c->err & DEV_ERR_OVERFLOW) return DMC_ERR_OUTPUT_OVERFLOW;
+    if (c->err & DEV_ERR_BOUNDS) return DMC_ERR_DEVICE_CHECK;
+    if (c->totals[0] >= 0xFFFFFFFFull || c->totals[1] >= 0xFFFFFFFFull) return DMC_ERR_OUTPUT_OVERFLOW;
+    return DMC_OK;
+}
+
+static bool same_out(const brick::EmitOut &a, const brick::EmitOut &b)
+{
+    return a.seg_off == b.seg_off && a.verts == b.verts && a.vcap == b.vcap && a.quads == b.quads &&
+           a.qcap == b.qcap && a.tris == b.tris;
+}
+
+// Captures the whole pipeline (both sample types) on the context's own
+// stream; the graph is later launched on the caller's stream.
+static dmc_status capture_graph(Ctx *ctx, BatchState &b, const brick::EmitOut &eo, const uint64_t nb[2])
+{
+    using namespace brick;
+    if (b.gexec) { cudaGraphExecDestroy(b.gexec); b.gexec = nullptr; }
+    if (b.graph) { cudaGraphDestroy(b.graph); b.graph = nullptr; }
+    b.emit_node[0] = b.emit_node[1] = nullptr;
+    cudaGraph_t graph = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    dmc_status cs = enqueue_front(ctx, b, b.d_res, false, nb, true, ctx->stream);
+    if (cs == DMC_OK) cs = enqueue_back(ctx, b, eo, b.d_res, false, nb, true, ctx->stream);
+    cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+    if (cs != DMC_OK) { if (graph) cudaGraphDestroy(graph); return cs; }
+    CUDA_TRY(ce);
+    // the emit nodes, found by kernel
+    size_t nn = 0;
+    CUDA_TRY(cudaGraphGetNodes(graph, nullptr, &nn));
+    std::vector<cudaGraphNode_t> nodes(nn);
+    CUDA_TRY(cudaGraphGetNodes(graph, nodes.data(), &nn));
+    for (cudaGraphNode_t nd : nodes) {
+        cudaGraphNodeType t;
+        CUDA_TRY(cudaGraphNodeGetType(nd, &t));
+        if (t != cudaGraphNodeTypeKernel) continue;
+        cudaKernelNodeParams kp;
+        CUDA_TRY(cudaGraphKernelNodeGetParams(nd, &kp));
+        for (int g = 0; g < 2; ++g) {
+            const void *fn = g ? (const void *)brick_sweep<uint16_t, true> : (const void *)brick_sweep<float, true>;
+            if (kp.func == fn) { b.emit_node[g] = nd; b.emit_params[g] = kp; }
+        }
+    }
+    if (!b.emit_node[0] || !b.emit_node[1]) { cudaGraphDestroy(graph); return DMC_ERR_CUDA; }
+    ce = cudaGraphInstantiate(&b.gexec, graph, 0);
+    if (ce != cudaSuccess) { cudaGraphDestroy(graph); CUDA_TRY(ce); }
+    b.graph = graph;
+    b.g_scratch_gen = ctx->scratch_gen;
+    b.g_stage_gen = b.stage_gen;
+    b.g_out = eo;
+    return DMC_OK;
+}
+
+// Points the graph's emit sweeps at other output buffers (same arguments as
+// the launches in enqueue_back, with a new EmitOut).
+static dmc_status retarget_graph(Ctx *ctx, BatchState &b, const brick::EmitOut &eo)
+{
+    using namespace brick;
+    if (same_out(eo, b.g_out)) return DMC_OK;
+    for (uint32_t g = 0; g < 2; ++g) {
+        const BatchHead *a_head = b.d_plan;
+        uint32_t a_group = g;
+        const DeviceTables *a_tab = ctx->d_tab;
+        uint2 *a_cnt = nullptr;
+        EmitOut a_out = eo;
+        Spill *a_spill = b.spill;
+        uint32_t *a_ticket = &b.tickets[2 + g];
+        unsigned long long *a_counters = ctx->d_ctl->counters;
+        uint32_t *a_err = &ctx->d_ctl->err;
+        void *args[] = {&a_head, &a_group, &a_tab, &a_cnt, &a_out, &a_spill, &a_ticket, &a_counters, &a_err};
+        cudaKernelNodeParams kp = b.emit_params[g];
+        kp.kernelParams = args;
+        kp.extra = nullptr;
+        CUDA_TRY(cudaGraphExecKernelNodeSetParams(b.gexec, b.emit_node[g], &kp));
+    }
+    b.g_out = eo;
+    return DMC_OK;
+}
+
+// Extraction of one or many volumes: count sweep, one segment scan over all
+// volumes, per-volume offsets, emit sweep.  Vertices and quads of volume v
+// land at its offsets in the shared output buffers; quad indices are relative
+// to the volume's first vertex.
+dmc_status brick_extract(Ctx *ctx, const BrickItem *items, uint32_t n, const BrickOut &o, cudaStream_t st)
+{
+    using namespace brick;
+    if (n == 0) return DMC_ERR_INVALID_ARG;
+    BatchState *bp = nullptr;
+    dmc_status s = batch_state(ctx, &bp);
+    if (s != DMC_OK) return s;
+    BatchState &b = *bp;
+    if (b.in_flight) return DMC_ERR_INVALID_ARG;
+    const int gmax = std::max(std::max(b.grid[0][0], b.grid[0][1]), std::max(b.grid[1][0], b.grid[1][1]));
+    // planes per brick: long sweeps amortise the z halo, but keep at least
+    // three bricks per warp so that the persistent warps stay busy
+    uint32_t zc = ctx->brick_zc ? ctx->brick_zc : 32;
+    if (!ctx->brick_zc) {
+        for (;;) {
+            uint64_t nb = 0;
+            for (uint32_t i = 0; i < n; ++i) {
+                const uint3 c = items[i].cells;
+                nb += (uint64_t)((c.x + W - 1) / W) * ((c.y + ROWS - 1) / ROWS) * ((c.z + zc - 1) / zc);
+            }
+            if (zc <= 4 || nb >= 3ull * (uint64_t)gmax * NWB) break;
+            zc >>= 1;
+        }
+    }
+    // descriptors: the f32 volumes, then the u16 ones (one launch per type)
+    uint64_t nseg = 0, ncoord = 0, nb[2] = {0, 0};
+    uint32_t nvol[2] = {0, 0};
+    for (uint32_t i = 0; i < n; ++i) {
+        const BrickItem &it = items[i];
+        nseg += (uint64_t)it.cells.z * it.cells.y * ((it.cells.x + W - 1) / W);
+        ncoord += (uint64_t)it.pts.x + it.pts.y + it.pts.z;
+        nvol[it.dtype == DMC_F32 ? 0 : 1]++;
+    }
+    const uint64_t n_tiles = (nseg + SCAN_TILE - 1) / SCAN_TILE;
+    if (n_tiles >= (1ull << 31)) return DMC_ERR_UNSUPPORTED;
+    if ((s = batch_layout(ctx, b, n, nseg, ncoord)) != DMC_OK) return s;
+    BatchHead *head = (BatchHead *)b.h_stage;
+    Geom *geoms = (Geom *)(head + 1);
+    uint32_t pos[2] = {0, nvol[0]};
+    uint64_t seg_base = 0, coord_base = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const BrickItem &it = items[i];
+        const int grp = it.dtype == DMC_F32 ? 0 : 1;
+        Geom &g = geoms[pos[grp]++];
+        g = Geom{};
+        g.data = it.data; g.pts = it.pts; g.cells = it.cells; g.iso = it.iso; g.mn = it.mn; g.rng = it.rng;
+        iso_thresholds(it.iso, g.iso_u16, g.isole_u16);
+        g.nxs = (it.cells.x + W - 1) / W;
+        g.nyb = (it.cells.y + ROWS - 1) / ROWS;
+        g.zc = zc;
+        g.nzb = (it.cells.z + zc - 1) / zc;
+        g.brick_base = nb[grp];
+        nb[grp] += (uint64_t)g.nxs * g.nyb * g.nzb;
+        g.seg_base = seg_base;
+        g.nseg = (uint64_t)it.cells.z * it.cells.y * g.nxs;
+        seg_base += g.nseg;
+        g.coord = b.coord + coord_base;
+        coord_base += (uint64_t)it.pts.x + it.pts.y + it.pts.z;
+        g.item = i;
+    }
+    if (nb[0] >= 0xF0000000ull || nb[1] >= 0xF0000000ull) return DMC_ERR_UNSUPPORTED;
+    head->nbricks[0] = nb[0]; head->nbricks[1] = nb[1];
+    head->nseg = nseg;
+    head->nvol[0] = nvol[0]; head->nvol[1] = nvol[1];
+    head->n = n;
+    head->n_tiles = (uint32_t)n_tiles;
+
+    EmitOut eo;
+    eo.seg_off = b.seg_off; eo.verts = o.verts; eo.vcap = o.vcap; eo.quads = o.quads; eo.qcap = o.qcap; eo.tris = o.tris;
+    dmc_batch_result *d_res = (o.d_results && o.mode != BATCH_GRAPH) ? o.d_results : b.d_res;
+    if (o.mode == BATCH_GRAPH) {
+        // the graph's per-volume results always go to scratch; a caller's
+        // device results are copied from there after the launch
+        if (!b.gexec || b.g_scratch_gen != ctx->scratch_gen || b.g_stage_gen != b.stage_gen) {
+            if ((s = capture_graph(ctx, b, eo, nb)) != DMC_OK) return s;
+        }
+        if ((s = retarget_graph(ctx, b, eo)) != DMC_OK) return s;
+        CUDA_TRY(cudaGraphLaunch(b.gexec, st));
+        if (o.d_results)
+            CUDA_TRY(cudaMemcpyAsync(o.d_results, b.d_res, sizeof(dmc_batch_result) * (size_t)n, cudaMemcpyDeviceToDevice, st));
+    } else if (o.mode == BATCH_ASYNC) {
+        if ((s = enqueue_front(ctx, b, d_res, false, nb, false, st)) != DMC_OK) return s;
+        if ((s = enqueue_back(ctx, b, eo, d_res, false, nb, false, st)) != DMC_OK) return s;
+    } else {
+        if ((s = enqueue_front(ctx, b, d_res, true, nb, false, st)) != DMC_OK) return s;
+        ctx->evk_used = 1;
+        // totals decide whether the caller's buffers are large enough; the
+        // per-volume offsets are final already
+        CUDA_TRY(cudaMemcpyAsync(ctx->h_ctl, ctx->d_ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(stage_results(b), d_res, sizeof(dmc_batch_result) * (size_t)n, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        stats_from_ctl(ctx);
+        if (ctx->h_ctl->err & DEV_ERR_TIMEOUT) return DMC_ERR_TIMEOUT;
+        const uint64_t V = ctx->h_ctl->totals[0], Q = ctx->h_ctl->totals[1];
+        if (o.n_vertices) *o.n_vertices = V;
+        if (o.n_quads) *o.n_quads = Q;
+        if (V >= 0xFFFFFFFFull || Q >= 0xFFFFFFFFull) return DMC_ERR_OUTPUT_OVERFLOW;
+        if (o.h_results) std::copy(stage_results(b), stage_results(b) + n, o.h_results);
+        if (o.sizing_only) return DMC_OK;
+        if (V > o.vcap || Q > o.qcap) return DMC_ERR_OUTPUT_OVERFLOW;
+        if ((s = enqueue_back(ctx, b, eo, d_res, true, nb, false, st)) != DMC_OK) return s;
+        ctx->evk_used = 2;
+        CUDA_TRY(cudaStreamSynchronize(st));
+        stats_from_ctl(ctx);
+        return ctl_status(ctx->h_ctl);
+    }
+    CUDA_TRY(cudaEventRecord(b.done, st));
+    b.in_flight = true;
+    b.n_inflight = n;
+    return DMC_OK;
+}
+
+dmc_status brick_wait(Ctx *ctx, dmc_batch_result *h_results, uint64_t *n_vertices, uint64_t *n_quads)
+{
+    BatchState *b = ctx->batch;
+    if (!b || !b->in_flight) return DMC_ERR_INVALID_ARG;
+    b->in_flight = false;
+    CUDA_TRY(cudaEventSynchronize(b->done));
+    stats_from_ctl(ctx);
+    if (n_vertices) *n_vertices = ctx->h_ctl->totals[0];
+    if (n_quads) *n_quads = ctx->h_ctl->totals[1];
+    if (h_results) std::copy(stage_results(*b), stage_results(*b) + b->n_inflight, h_results);
+    return ctl_status(ctx->h_ctl);
 }
 
 dmc_status brick_run(Ctx *ctx, const ExtractArgs &a, cudaStream_t st)
 {
-    if (a.dtype == DMC_F32) return brick_run_t<float>(ctx, (const float *)a.vol, a, st);
-    return brick_run_t<uint16_t>(ctx, (const uint16_t *)a.vol, a, st);
+    BrickItem it;
+    it.data = a.vol; it.dtype = a.dtype; it.pts = a.pts; it.cells = a.cells; it.iso = a.iso; it.mn = a.mn; it.rng = a.rng;
+    BrickOut o{};
+    o.verts = a.verts; o.vcap = a.vcap; o.quads = a.quads; o.qcap = a.qcap; o.tris = a.tris;
+    o.mode = BATCH_SYNC; o.sizing_only = a.sizing_only;
+    o.n_vertices = a.n_vertices; o.n_quads = a.n_quads;
+    return brick_extract(ctx, &it, 1, o, st);
 }
 
 }  // namespace dmc

@@ -28,6 +28,8 @@ struct DevCtl {
     uint32_t pad[7];
 };
 
+struct BatchState;
+
 struct Ctx {
     int device = 0;
     int num_sms = 0;
@@ -40,6 +42,10 @@ struct Ctx {
     DevCtl *d_ctl = nullptr;
     DevCtl *h_ctl = nullptr;           // pinned
     void *d_vol = nullptr;             // staging for host volumes (grow-only)
+    uint64_t scratch_gen = 0;          // bumped whenever scratch moves (captured graphs hold its addresses)
+    uint32_t brick_zc = 0;             // planes per brick (0: automatic)
+    BatchState *batch = nullptr;
+    bool batch_pending = false;        // an asynchronous batch awaits dmc_batch_wait
     size_t d_vol_bytes = 0;
     DeviceTables *d_tab = nullptr;     // lookup tables in device memory
     int algo = DMC_ALGO_AUTO;
@@ -61,6 +67,36 @@ struct ExtractArgs {
 };
 
 dmc_status ctx_reserve_scratch(Ctx *ctx, size_t bytes);
+
+// One volume of a brick-path extraction.
+struct BrickItem {
+    const void *data;          // device samples
+    dmc_dtype dtype;
+    uint3 pts, cells;
+    float iso;
+    float3 mn, rng;
+};
+
+enum BatchMode { BATCH_SYNC = 0, BATCH_ASYNC = 1, BATCH_GRAPH = 2 };
+
+struct BrickOut {
+    float *verts; uint64_t vcap;
+    uint32_t *quads; uint64_t qcap;
+    uint32_t *tris;
+    dmc_batch_result *d_results;   // per volume, device (may be NULL)
+    dmc_batch_result *h_results;   // per volume, host (may be NULL; BATCH_SYNC only)
+    uint64_t *n_vertices, *n_quads; // totals (host; BATCH_SYNC only)
+    BatchMode mode;
+    bool sizing_only;              // BATCH_SYNC: stop after the count
+};
+
+// State of the batch pipeline of a context (scratch layout, pinned staging,
+// cached graph, the batch in flight).  Defined with the brick kernels.
+void batch_state_free(Ctx *ctx);
+
+dmc_status brick_extract(Ctx *ctx, const BrickItem *items, uint32_t n, const BrickOut &o, cudaStream_t st);
+// Completes an asynchronous batch: waits for it and checks its status.
+dmc_status brick_wait(Ctx *ctx, dmc_batch_result *h_results, uint64_t *n_vertices, uint64_t *n_quads);
 dmc_status upload_tables(Ctx *ctx);
 
 dmc_status simple_run(Ctx *ctx, const ExtractArgs &a, cudaStream_t st);

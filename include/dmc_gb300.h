@@ -119,7 +119,8 @@ void dmc_mesh_free(dmc_mesh *mesh);
  * buffers are caller-owned device memory with the given capacities (in
  * vertices / quads).  d_triangles may be NULL.  On DMC_ERR_OUTPUT_OVERFLOW the
  * counts are still reported in *n_vertices / *n_quads so the caller can
- * retry.  `stream` is a cudaStream_t (NULL: the context's stream).  The call
+ * retry.  With all three output pointers NULL the call only counts: it
+ * returns DMC_OK with the totals and writes no mesh.  `stream` is a cudaStream_t (NULL: the context's stream).  The call
  * returns after the mesh is complete. */
 dmc_status dmc_extract_device(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min[3], const float xyz_max[3],
                               float iso, uint32_t num_smooth,
@@ -128,8 +129,77 @@ dmc_status dmc_extract_device(dmc_ctx *ctx, const dmc_volume *vol, const float x
                               uint32_t *d_triangles,
                               uint64_t *n_vertices, uint64_t *n_quads, void *stream);
 
-/* Counters of the last call on this context. */
+/* Counters of the last call on this context (for a batch: summed over its
+ * volumes). */
 dmc_status dmc_get_stats(const dmc_ctx *ctx, dmc_stats *stats);
+
+/* ---- batched extraction (no reference counterpart: the reference extracts
+ * one volume per run_dmc call, dmc.cu:2069-2208, with a host round trip per
+ * kernel) ------------------------------------------------------------------ */
+
+/* One volume of a batch.  vol.data is DEVICE memory. */
+typedef struct {
+    dmc_volume vol;
+    float iso;
+    float xyz_min[3];
+    float xyz_max[3];
+} dmc_batch_item;
+
+/* Where the mesh of one volume landed in the shared output buffers: vertices
+ * [vertex_offset, vertex_offset + n_vertices), quads (and triangle pairs)
+ * [quad_offset, quad_offset + n_quads).  Quad and triangle corner indices are
+ * relative to the volume's vertex_offset, so each volume's slice is the mesh
+ * dmc_extract_device returns for it alone. */
+typedef struct {
+    uint64_t vertex_offset;
+    uint64_t n_vertices;
+    uint64_t quad_offset;
+    uint64_t n_quads;
+} dmc_batch_result;
+
+/* dmc_extract_batch flags */
+#define DMC_BATCH_ASYNC 0x1u  /* enqueue and return; dmc_batch_wait completes the call */
+#define DMC_BATCH_GRAPH 0x2u  /* as ASYNC, launched as a CUDA graph cached on the context */
+
+/* Extracts n_items volumes (mixed dtypes and shapes) in one pipeline: one
+ * persistent count sweep per dtype over the bricks of all volumes, one scan,
+ * one persistent emit sweep per dtype.  Meshes are concatenated in item order
+ * into the caller's device buffers; per-volume offsets go to d_results
+ * (device, may be NULL) and, for a synchronous call, to results (host, may be
+ * NULL).
+ *
+ * flags == 0: returns when the meshes are complete, with the totals in
+ * *n_vertices / *n_quads; DMC_ERR_OUTPUT_OVERFLOW (no mesh written, totals
+ * and results still reported) when they exceed the capacities.  With all
+ * three output pointers NULL the call only counts: DMC_OK, totals and
+ * per-volume results, no mesh.  DMC_BATCH_ASYNC / DMC_BATCH_GRAPH: enqueue on
+ * `stream` and return at once; results, n_vertices and n_quads may be NULL and
+ * are ignored.  Capacities are then checked on the device (writes beyond them
+ * are skipped and reported by dmc_batch_wait), so size the buffers by a bound.
+ * One asynchronous batch may be in flight per context: call dmc_batch_wait
+ * before the next call on the context.  The graph is captured on first use and
+ * again whenever the scratch layout changes; later batches of any shape that
+ * fit the scratch replay it, with the output buffers of each call patched
+ * into the graph.  The first call of a context allocates its scratch; a
+ * batch larger than any before grows it. */
+dmc_status dmc_extract_batch(dmc_ctx *ctx, const dmc_batch_item *items, uint32_t n_items,
+                             float *d_vertices, uint64_t vertex_capacity,
+                             uint32_t *d_quads, uint64_t quad_capacity,
+                             uint32_t *d_triangles,
+                             dmc_batch_result *d_results, dmc_batch_result *results,
+                             uint64_t *n_vertices, uint64_t *n_quads,
+                             uint32_t flags, void *stream);
+
+/* Completes the asynchronous batch of the context: waits for it, fills
+ * results (host, may be NULL) and the totals, and returns its status. */
+dmc_status dmc_batch_wait(dmc_ctx *ctx, dmc_batch_result *results, uint64_t *n_vertices, uint64_t *n_quads);
+
+/* Tuning knobs (no reference counterpart). */
+typedef enum {
+    DMC_OPT_BRICK_PLANES = 1   /* z planes per brick, 1..256; 0 chooses from the batch size */
+} dmc_option;
+
+dmc_status dmc_set_option(dmc_ctx *ctx, dmc_option opt, int64_t value);
 
 #ifdef __cplusplus
 }
