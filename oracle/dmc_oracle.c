@@ -24,14 +24,17 @@
  *                 target for the GPU.
  *   precision 1 — FP64: the same topology, positions evaluated in double.
  *
- * Deliberate, documented divergence from the reference (the only one): an
+ * Deliberate, documented divergences from the reference (two).  First, an
  * owned edge whose endpoints are "bipolar" by the reference's test
  * (dmc.cu:1101-1106) but fall on the same side of the config bits (one sample
  * equals the isovalue, the other is above it) gets its edge vertex emitted as
  * in the reference, but no quad: the reference would look up NO_VERTEX (0xff)
  * in the ring cells (or read outside the compact array for an inactive ring
  * cell), producing an invalid index.  Such quads are counted in
- * n_dropped_quads.  Samples that are NaN are not supported.
+ * n_dropped_quads.  Second, a dual vertex whose patch has no owner cell
+ * inside the volume gets the mean of its patch's crossings computed locally,
+ * where the reference leaves it uninitialised (dmc.cu:1584-1592).  Samples
+ * that are NaN are not supported.
  */
 #include <stdint.h>
 #include <stdlib.h>
