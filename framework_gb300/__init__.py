@@ -25,7 +25,9 @@ __all__ = ["DMCError", "Extractor", "Mesh", "setup_device_luts", "run_dmc", "cle
 STATUS = {
     0: "DMC_OK", 1: "DMC_ERR_INVALID_ARG", 2: "DMC_ERR_OOM", 3: "DMC_ERR_OUTPUT_OVERFLOW",
     4: "DMC_ERR_TIMEOUT", 5: "DMC_ERR_CUDA", 6: "DMC_ERR_UNSUPPORTED", 7: "DMC_ERR_DEVICE_CHECK",
+    8: "DMC_ERR_TOO_LARGE",
 }
+NOALLOC_MAX_CELLS = 1048576
 DTYPE = {"float32": 0, "uint16": 1}
 ALGO = {"auto": 0, "simple": 1, "brick": 2}
 
@@ -33,7 +35,7 @@ ALGO = {"auto": 0, "simple": 1, "brick": 2}
 ABI_SYMBOLS = [
     "dmc_version", "dmc_tables_sha256", "dmc_status_string", "dmc_create", "dmc_destroy",
     "dmc_set_algo", "dmc_run", "dmc_mesh_free", "dmc_extract_device", "dmc_get_stats",
-    "dmc_extract_batch", "dmc_batch_wait", "dmc_set_option",
+    "dmc_extract_batch", "dmc_batch_wait", "dmc_set_option", "dmc_extract_device_noalloc",
 ]
 BATCH_ASYNC, BATCH_GRAPH = 0x1, 0x2
 OPT_BRICK_PLANES = 1
@@ -117,6 +119,10 @@ def load_library(build_if_missing=True):
                                     ctypes.c_void_p]
     L.dmc_batch_wait.argtypes = [ctypes.c_void_p, P(_BatchResult), P(ctypes.c_uint64), P(ctypes.c_uint64)]
     L.dmc_set_option.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int64]
+    L.dmc_extract_device_noalloc.argtypes = [P(_Volume), P(ctypes.c_float), P(ctypes.c_float), ctypes.c_float,
+                                             ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
+                                             ctypes.c_void_p, P(ctypes.c_uint64), P(ctypes.c_uint64),
+                                             ctypes.c_void_p]
     for name in ABI_SYMBOLS:
         if name not in ("dmc_version", "dmc_tables_sha256", "dmc_status_string", "dmc_mesh_free"):
             getattr(L, name).restype = ctypes.c_int

@@ -32,9 +32,8 @@ static dmc_status reserve(void **p, size_t *have, size_t bytes)
     return DMC_OK;
 }
 
-dmc_status upload_tables(Ctx *ctx)
+void fill_tables(DeviceTables &h)
 {
-    DeviceTables h;
     memcpy(h.edge_lut[0], DMC_EDGE_LUT1, sizeof(h.edge_lut[0]));
     memcpy(h.edge_lut[1], DMC_EDGE_LUT2, sizeof(h.edge_lut[1]));
     memcpy(h.nvert[0], DMC_NVERT_LUT1, sizeof(h.nvert[0]));
@@ -48,6 +47,12 @@ dmc_status upload_tables(Ctx *ctx)
             if (DMC_EDGE_LUT1[c * 12 + e] != 0xff) m |= (uint16_t)(1u << e);
         h.crossed[c] = m;
     }
+}
+
+dmc_status upload_tables(Ctx *ctx)
+{
+    DeviceTables h;
+    fill_tables(h);
     CUDA_TRY(cudaMalloc(&ctx->d_tab, sizeof(DeviceTables)));
     CUDA_TRY(cudaMemcpy(ctx->d_tab, &h, sizeof(DeviceTables), cudaMemcpyHostToDevice));
     return DMC_OK;
@@ -151,6 +156,7 @@ const char *dmc_status_string(dmc_status s)
     case DMC_ERR_CUDA: return "CUDA error";
     case DMC_ERR_UNSUPPORTED: return "unsupported input for the selected path";
     case DMC_ERR_DEVICE_CHECK: return "device-side bounds check failed";
+    case DMC_ERR_TOO_LARGE: return "volume exceeds the fixed scratch of the no-allocation entry point";
     }
     return "unknown status";
 }

@@ -98,6 +98,7 @@ dmc_status brick_extract(Ctx *ctx, const BrickItem *items, uint32_t n, const Bri
 // Completes an asynchronous batch: waits for it and checks its status.
 dmc_status brick_wait(Ctx *ctx, dmc_batch_result *h_results, uint64_t *n_vertices, uint64_t *n_quads);
 dmc_status upload_tables(Ctx *ctx);
+void fill_tables(DeviceTables &h);   // host copy of the lookup tables
 
 dmc_status simple_run(Ctx *ctx, const ExtractArgs &a, cudaStream_t st);
 dmc_status brick_run(Ctx *ctx, const ExtractArgs &a, cudaStream_t st);

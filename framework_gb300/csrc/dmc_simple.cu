@@ -10,6 +10,7 @@
 #include "dmc_device.cuh"
 #include "dmc_scan.cuh"
 #include "dmc_internal.h"
+#include <mutex>
 
 namespace dmc {
 
@@ -264,4 +265,133 @@ dmc_status simple_run(Ctx *ctx, const ExtractArgs &a, cudaStream_t st)
     return simple_run_t<uint16_t>(ctx, (const uint16_t *)a.vol, a, st);
 }
 
+// ---------------------------------------------------------------------------
+// No-allocation variant of the simple path (dmc_extract_device_noalloc).
+//
+// For callers that must not have a library allocate device memory on their
+// behalf: processes whose device memory is held by a pool allocator that has
+// reserved what is free (a framework's caching allocator, an application heap),
+// so that a cudaMalloc from here would fail or fragment it; and latency-bound
+// loops sharing the GPU with other streams, where cudaMalloc / cudaFree may
+// synchronise the device and stall them.  Everything the pipeline needs --
+// lookup tables, control block, per-cell arrays and scan tile states -- lives
+// in one fixed array in the module's global memory, sized for at most
+// kNoAllocMaxCells cells.  Its address is taken once per device with
+// cudaGetSymbolAddress on the first call, which also uploads the tables; make
+// that first call before any stream capture.  Per call, only the control
+// block and the scan tile states must start at zero (cleared with
+// cudaMemsetAsync on the caller's stream); the per-cell arrays are fully
+// rewritten.  There is one array per device, so calls on the same device must
+// not overlap in time: concurrent calls from several host threads race on it.
+
+constexpr uint64_t kNoAllocMaxCells = DMC_NOALLOC_MAX_CELLS;
+constexpr size_t na_align(size_t b) { return (b + 255) & ~(size_t)255; }
+constexpr uint64_t kNoAllocTiles = (kNoAllocMaxCells + kScanTile - 1) / kScanTile;
+constexpr size_t kNaTab = 0;
+constexpr size_t kNaCtl = kNaTab + na_align(sizeof(DeviceTables));
+constexpr size_t kNaCfg = kNaCtl + na_align(sizeof(DevCtl));
+constexpr size_t kNaCnt = kNaCfg + na_align(kNoAllocMaxCells);
+constexpr size_t kNaVb = kNaCnt + na_align(kNoAllocMaxCells);
+constexpr size_t kNaQb = kNaVb + na_align(4 * kNoAllocMaxCells);
+constexpr size_t kNaTiles = kNaQb + na_align(4 * kNoAllocMaxCells);
+constexpr size_t kNoAllocBytes = kNaTiles + na_align(sizeof(TileState) * kNoAllocTiles);   // ~10.1 MiB
+
+static __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocBytes];
+
+static std::mutex g_noalloc_setup_mu;
+static uint8_t *g_noalloc_base[256];          // per device, set by the first call
+
+static dmc_status noalloc_setup(int device, uint8_t **base)
+{
+    if (device < 0 || device >= 256) return DMC_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(g_noalloc_setup_mu);
+    if (!g_noalloc_base[device]) {
+        void *p = nullptr;
+        CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        DeviceTables h;
+        fill_tables(h);
+        CUDA_TRY(cudaMemcpy((uint8_t *)p + kNaTab, &h, sizeof(DeviceTables), cudaMemcpyHostToDevice));
+        g_noalloc_base[device] = (uint8_t *)p;
+    }
+    *base = g_noalloc_base[device];
+    return DMC_OK;
+}
+
+template <class T>
+static dmc_status noalloc_run_t(uint8_t *base, const T *vol, const ExtractArgs &a, int num_sms, cudaStream_t st)
+{
+    const uint64_t C = a.n_cells;
+    const uint32_t n_tiles = (uint32_t)((C + kScanTile - 1) / kScanTile);
+    const DeviceTables *tab = (const DeviceTables *)(base + kNaTab);
+    DevCtl *ctl_d = (DevCtl *)(base + kNaCtl);
+    uint8_t *cfg = base + kNaCfg, *cnt = base + kNaCnt;
+    uint32_t *vb = (uint32_t *)(base + kNaVb), *qb = (uint32_t *)(base + kNaQb);
+    TileState *tiles = (TileState *)(base + kNaTiles);
+    CUDA_TRY(cudaMemsetAsync(tiles, 0, sizeof(TileState) * n_tiles, st));
+    CUDA_TRY(cudaMemsetAsync(ctl_d, 0, sizeof(DevCtl), st));
+    const int g = grid_for(C, kSimpleThreads, num_sms);
+    simple_classify<T><<<g, kSimpleThreads, 0, st>>>(vol, a.pts, a.cells, a.iso, cfg, C);
+    simple_count<T><<<g, kSimpleThreads, 0, st>>>(vol, a.pts, a.cells, a.iso, cfg, cnt, C, ctl_d->counters, tab);
+    ScanCtl ctl;
+    ctl.tiles = tiles; ctl.ticket = &ctl_d->ticket; ctl.err = &ctl_d->err;
+    ctl.totals = ctl_d->totals; ctl.n_tiles = n_tiles;
+    simple_scan<<<n_tiles, kScanThreads, 0, st>>>(cnt, C, ctl, vb, qb);
+    CUDA_TRY(cudaGetLastError());
+    DevCtl h;   // pageable host copy: no pinned buffer to allocate
+    CUDA_TRY(cudaMemcpyAsync(&h, ctl_d, sizeof(DevCtl), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (h.err & DEV_ERR_TIMEOUT) return DMC_ERR_TIMEOUT;
+    *a.n_vertices = h.totals[0]; *a.n_quads = h.totals[1];
+    if (a.sizing_only) return DMC_OK;
+    if (h.totals[0] > a.vcap || h.totals[1] > a.qcap) return DMC_ERR_OUTPUT_OVERFLOW;
+    simple_emit<T><<<g, kSimpleThreads, 0, st>>>(vol, a.pts, a.cells, a.iso, a.mn, a.rng, cfg, cnt, vb, qb, C,
+                                                  a.verts, a.vcap, a.quads, a.qcap, a.tris, &ctl_d->err, tab);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(&h, ctl_d, sizeof(DevCtl), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (h.err & DEV_ERR_OVERFLOW) return DMC_ERR_OUTPUT_OVERFLOW;
+    if (h.err & DEV_ERR_BOUNDS) return DMC_ERR_DEVICE_CHECK;
+    return DMC_OK;
+}
+
 }  // namespace dmc
+
+extern "C" dmc_status dmc_extract_device_noalloc(const dmc_volume *vol, const float xyz_min[3],
+                                                 const float xyz_max[3], float iso, float *d_vertices,
+                                                 uint64_t vertex_capacity, uint32_t *d_quads, uint64_t quad_capacity,
+                                                 uint32_t *d_triangles, uint64_t *n_vertices, uint64_t *n_quads,
+                                                 void *stream)
+{
+    using namespace dmc;
+    if (!vol || !vol->data || !xyz_min || !xyz_max || !n_vertices || !n_quads) return DMC_ERR_INVALID_ARG;
+    if (vol->dtype != DMC_F32 && vol->dtype != DMC_U16) return DMC_ERR_INVALID_ARG;
+    if ((vertex_capacity && !d_vertices) || (quad_capacity && !d_quads)) return DMC_ERR_INVALID_ARG;
+    *n_vertices = 0; *n_quads = 0;
+    ExtractArgs a{};
+    a.vol = vol->data;
+    a.dtype = vol->dtype;
+    a.pts = make_uint3(vol->dims[0], vol->dims[1], vol->dims[2]);
+    a.cells = make_uint3(vol->dims[0] ? vol->dims[0] - 1 : 0, vol->dims[1] ? vol->dims[1] - 1 : 0,
+                         vol->dims[2] ? vol->dims[2] - 1 : 0);
+    a.n_cells = (uint64_t)a.cells.x * a.cells.y * a.cells.z;
+    if (a.n_cells > kNoAllocMaxCells) return DMC_ERR_TOO_LARGE;
+    a.iso = iso;
+    a.mn = make_float3(xyz_min[0], xyz_min[1], xyz_min[2]);
+    a.rng = make_float3(xyz_max[0] - xyz_min[0], xyz_max[1] - xyz_min[1], xyz_max[2] - xyz_min[2]);
+    a.verts = d_vertices; a.vcap = vertex_capacity;
+    a.quads = d_quads; a.qcap = quad_capacity;
+    a.tris = d_triangles;
+    a.n_vertices = n_vertices; a.n_quads = n_quads;
+    a.sizing_only = !d_vertices && !d_quads && !d_triangles;
+    int device = 0, num_sms = 0;
+    CUDA_TRY(cudaGetDevice(&device));
+    CUDA_TRY(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device));
+    uint8_t *base = nullptr;
+    dmc_status s = noalloc_setup(device, &base);
+    if (s != DMC_OK) return s;
+    if (a.n_cells == 0) return DMC_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (a.dtype == DMC_F32) return noalloc_run_t<float>(base, (const float *)a.vol, a, num_sms, st);
+    return noalloc_run_t<uint16_t>(base, (const uint16_t *)a.vol, a, num_sms, st);
+}
+

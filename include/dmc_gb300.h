@@ -41,7 +41,8 @@ typedef enum {
     DMC_ERR_TIMEOUT = 4,           /* a bounded device-side wait gave up */
     DMC_ERR_CUDA = 5,
     DMC_ERR_UNSUPPORTED = 6,
-    DMC_ERR_DEVICE_CHECK = 7       /* a device-side bounds check failed */
+    DMC_ERR_DEVICE_CHECK = 7,      /* a device-side bounds check failed */
+    DMC_ERR_TOO_LARGE = 8          /* volume exceeds the fixed scratch of dmc_extract_device_noalloc */
 } dmc_status;
 
 typedef enum { DMC_F32 = 0, DMC_U16 = 1 } dmc_dtype;
@@ -200,6 +201,33 @@ typedef enum {
 } dmc_option;
 
 dmc_status dmc_set_option(dmc_ctx *ctx, dmc_option opt, int64_t value);
+
+/* ---- no-allocation extraction (no reference counterpart) ----------------
+ *
+ * For callers that must not have the library allocate device memory: a
+ * process whose device memory is held by a pool allocator that has reserved
+ * what is free (a framework's caching allocator, an application heap), where
+ * a cudaMalloc from a library fails or fragments the pool; and latency-bound
+ * loops sharing the GPU with other streams, where cudaMalloc / cudaFree can
+ * synchronise the device.  This call allocates nothing: it runs the simple
+ * per-cell pipeline (10 bytes of scratch per cell) in one fixed array of the
+ * library's own device memory, ~10.1 MiB per device, so it takes volumes of
+ * at most DMC_NOALLOC_MAX_CELLS cells ((nx-1)(ny-1)(nz-1)); larger ones are
+ * rejected with DMC_ERR_TOO_LARGE before any GPU work.
+ *
+ * No context: it runs on the calling thread's current device, on `stream`
+ * (NULL: the legacy default stream), and returns when the mesh is complete.
+ * The first call on a device looks up the array's address and uploads the
+ * lookup tables; make it before any stream capture.  The array is one per
+ * device: calls on the same device must not overlap (concurrent calls from
+ * several host threads race on it).  Outputs and errors as in
+ * dmc_extract_device (all output pointers NULL: count only). */
+#define DMC_NOALLOC_MAX_CELLS 1048576u
+
+dmc_status dmc_extract_device_noalloc(const dmc_volume *vol, const float xyz_min[3], const float xyz_max[3],
+                                      float iso, float *d_vertices, uint64_t vertex_capacity,
+                                      uint32_t *d_quads, uint64_t quad_capacity, uint32_t *d_triangles,
+                                      uint64_t *n_vertices, uint64_t *n_quads, void *stream);
 
 #ifdef __cplusplus
 }
