@@ -19,7 +19,7 @@ import numpy as np
 
 from . import build as _build
 
-__all__ = ["DMCError", "Extractor", "Mesh", "setup_device_luts", "run_dmc", "cleanup_device_luts",
+__all__ = ["DMCError", "Extractor", "Server", "Mesh", "setup_device_luts", "run_dmc", "cleanup_device_luts",
            "load_library", "STATUS"]
 
 STATUS = {
@@ -36,6 +36,8 @@ ABI_SYMBOLS = [
     "dmc_version", "dmc_tables_sha256", "dmc_status_string", "dmc_create", "dmc_destroy",
     "dmc_set_algo", "dmc_run", "dmc_mesh_free", "dmc_extract_device", "dmc_get_stats",
     "dmc_extract_batch", "dmc_batch_wait", "dmc_set_option", "dmc_extract_device_noalloc",
+    "dmc_server_create", "dmc_server_destroy", "dmc_server_add_volume", "dmc_server_submit", "dmc_server_wait",
+    "dmc_server_release", "dmc_server_get_stats", "dmc_server_replay",
 ]
 BATCH_ASYNC, BATCH_GRAPH = 0x1, 0x2
 OPT_BRICK_PLANES = 1
@@ -60,6 +62,25 @@ class _BatchItem(ctypes.Structure):
 class _BatchResult(ctypes.Structure):
     _fields_ = [("vertex_offset", ctypes.c_uint64), ("n_vertices", ctypes.c_uint64),
                 ("quad_offset", ctypes.c_uint64), ("n_quads", ctypes.c_uint64)]
+
+
+class _ServerConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("lanes", ctypes.c_uint32), ("max_batch", ctypes.c_uint32),
+                ("vertex_arena", ctypes.c_uint64), ("quad_arena", ctypes.c_uint64),
+                ("want_triangles", ctypes.c_int), ("plain", ctypes.c_int)]
+
+
+class _ServerResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("n_vertices", ctypes.c_uint64), ("n_quads", ctypes.c_uint64),
+                ("vertices", ctypes.c_void_p), ("quads", ctypes.c_void_p), ("triangles", ctypes.c_void_p),
+                ("t_submit", ctypes.c_double), ("t_start", ctypes.c_double), ("t_done", ctypes.c_double),
+                ("batch_size", ctypes.c_uint32)]
+
+
+class _ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("batches", ctypes.c_uint64),
+                ("max_batch_seen", ctypes.c_uint64), ("arena_peak_vertices", ctypes.c_uint64),
+                ("arena_peak_quads", ctypes.c_uint64)]
 
 
 class _Mesh(ctypes.Structure):
@@ -119,6 +140,16 @@ def load_library(build_if_missing=True):
                                     ctypes.c_void_p]
     L.dmc_batch_wait.argtypes = [ctypes.c_void_p, P(_BatchResult), P(ctypes.c_uint64), P(ctypes.c_uint64)]
     L.dmc_set_option.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int64]
+    L.dmc_server_create.argtypes = [P(_ServerConfig), P(ctypes.c_void_p)]
+    L.dmc_server_destroy.argtypes = [ctypes.c_void_p]
+    L.dmc_server_add_volume.argtypes = [ctypes.c_void_p, P(_Volume), P(ctypes.c_float), P(ctypes.c_float),
+                                        P(ctypes.c_uint32)]
+    L.dmc_server_submit.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_float, P(ctypes.c_uint64)]
+    L.dmc_server_wait.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double, P(_ServerResult)]
+    L.dmc_server_release.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
+    L.dmc_server_get_stats.argtypes = [ctypes.c_void_p, P(_ServerStats)]
+    L.dmc_server_replay.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     L.dmc_extract_device_noalloc.argtypes = [P(_Volume), P(ctypes.c_float), P(ctypes.c_float), ctypes.c_float,
                                              ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
                                              ctypes.c_void_p, P(ctypes.c_uint64), P(ctypes.c_uint64),
@@ -374,6 +405,125 @@ def _stream_handle(stream):
 
 def _results_array(hres):
     return np.array([[r.vertex_offset, r.n_vertices, r.quad_offset, r.n_quads] for r in hres], dtype=np.uint64).reshape(-1, 4)
+
+
+class Server:
+    """Serving loop (``dmc_server_*``): a pool of device-resident volumes and
+    continuous batching of (volume, isovalue) requests.
+
+    ``vertex_arena`` / ``quad_arena`` size the output space shared by all
+    requests in flight or not yet released; a request is admitted when its
+    worst-case output (7 vertices, 3 quads per cell) fits.  ``plain=True``
+    serves each request alone with ``dmc_extract_device`` (the per-request
+    baseline)."""
+
+    def __init__(self, device=0, vertex_arena=1 << 28, quad_arena=1 << 27, lanes=2, max_batch=64,
+                 triangles=False, plain=False):
+        self._lib = load_library()
+        cfg = _ServerConfig(int(device), int(lanes), int(max_batch), int(vertex_arena), int(quad_arena),
+                            1 if triangles else 0, 1 if plain else 0)
+        h = ctypes.c_void_p()
+        _check(self._lib.dmc_server_create(ctypes.byref(cfg), ctypes.byref(h)), "dmc_server_create")
+        self._h = h
+        self._volumes = []          # keep the pool's tensors alive
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.dmc_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def add_volume(self, volume, xyz_min=None, xyz_max=None):
+        """Adds a CUDA tensor [z,y,x] (float32, or int16 holding uint16 bits) to the pool; returns its id."""
+        t = volume
+        if not t.is_cuda or not t.is_contiguous() or t.dim() != 3:
+            raise DMCError(1, "pool volume must be a contiguous 3-D CUDA tensor")
+        dt = {"float32": 0, "int16": 1, "uint16": 1}.get(str(t.dtype).replace("torch.", ""))
+        if dt is None:
+            raise DMCError(1, "pool volume dtype must be float32 or (u)int16")
+        dims = (t.shape[2], t.shape[1], t.shape[0])
+        mn, mx = _default_extent(dims, xyz_min, xyz_max)
+        vol = _volume_struct(t.data_ptr(), dt, dims)
+        vid = ctypes.c_uint32()
+        _check(self._lib.dmc_server_add_volume(self._h, ctypes.byref(vol), _f3(mn), _f3(mx), ctypes.byref(vid)),
+               "dmc_server_add_volume")
+        self._volumes.append(t)
+        return int(vid.value)
+
+    def submit(self, volume_id, iso):
+        rid = ctypes.c_uint64()
+        _check(self._lib.dmc_server_submit(self._h, int(volume_id), ctypes.c_float(iso), ctypes.byref(rid)),
+               "dmc_server_submit")
+        return int(rid.value)
+
+    def wait(self, request_id, timeout=60.0):
+        """Returns a dict with status, counts, device pointers and timestamps."""
+        r = _ServerResult()
+        _check(self._lib.dmc_server_wait(self._h, int(request_id), float(timeout), ctypes.byref(r)),
+               "dmc_server_wait")
+        return dict(status=int(r.status), n_vertices=int(r.n_vertices), n_quads=int(r.n_quads),
+                    vertices=r.vertices, quads=r.quads, triangles=r.triangles, t_submit=r.t_submit,
+                    t_start=r.t_start, t_done=r.t_done, batch_size=int(r.batch_size))
+
+    def tensors(self, result):
+        """Zero-copy CUDA tensors over a result's mesh (vertices [V,3] f32,
+        quads [Q,4] int32, triangles [2Q,3] int32 or None); valid until the
+        request is released."""
+        import torch
+        nv, nq = result["n_vertices"], result["n_quads"]
+
+        def view(ptr, shape, typestr):
+            if not shape[0]:
+                return torch.empty(shape, dtype=torch.float32 if typestr == "<f4" else torch.int32, device="cuda")
+            return torch.as_tensor(_DeviceArray(ptr, shape, typestr), device="cuda")
+        v = view(result["vertices"], (nv, 3), "<f4")
+        q = view(result["quads"], (nq, 4), "<i4")
+        t = view(result["triangles"], (2 * nq, 3), "<i4") if result["triangles"] else None
+        return v, q, t
+
+    def fetch(self, result):
+        """Host copies of a result's mesh: (vertices, quads, triangles or None) as numpy arrays."""
+        v, q, t = self.tensors(result)
+        return v.cpu().numpy(), q.cpu().numpy().view(np.uint32), (t.cpu().numpy().view(np.uint32) if t is not None else None)
+
+    def release(self, request_id):
+        _check(self._lib.dmc_server_release(self._h, int(request_id)), "dmc_server_release")
+
+    def stats(self):
+        s = _ServerStats()
+        _check(self._lib.dmc_server_get_stats(self._h, ctypes.byref(s)))
+        return {k: int(getattr(s, k)) for k, _ in _ServerStats._fields_}
+
+    def replay(self, volume_ids, isos, arrivals):
+        """Load generator (``dmc_server_replay``): returns (latency seconds, statuses) as numpy arrays."""
+        n = len(volume_ids)
+        vids = np.ascontiguousarray(volume_ids, np.uint32)
+        iso = np.ascontiguousarray(isos, np.float32)
+        arr = np.ascontiguousarray(arrivals, np.float64)
+        lat = np.zeros(n, np.float64)
+        st = np.zeros(n, np.int32)
+        _check(self._lib.dmc_server_replay(self._h, n, vids.ctypes.data, iso.ctypes.data, arr.ctypes.data,
+                                           lat.ctypes.data, st.ctypes.data), "dmc_server_replay")
+        return lat, st
+
+
+class _DeviceArray:
+    """__cuda_array_interface__ over library-owned device memory."""
+
+    def __init__(self, ptr, shape, typestr):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (int(ptr), False),
+                                         "version": 2, "strides": None}
 
 
 # ---------------------------------------------------------------------------

@@ -202,6 +202,64 @@ typedef enum {
 
 dmc_status dmc_set_option(dmc_ctx *ctx, dmc_option opt, int64_t value);
 
+/* ---- serving loop (no reference counterpart) -----------------------------
+ *
+ * A server keeps a pool of device-resident volumes and extracts (volume,
+ * isovalue) requests as they arrive.  Requests are admitted in FIFO order
+ * while their worst-case output (7 vertices and 3 quads per cell) fits the
+ * server's output arenas; admitted requests are batched onto `lanes`
+ * concurrent pipelines (each a context with its own stream, launched as a
+ * CUDA graph), so requests that arrive while others run join the next batch
+ * as soon as a lane and arena space are free.  A result's device pointers
+ * stay valid until dmc_server_release.  All calls are thread-safe. */
+typedef struct dmc_server dmc_server;
+
+typedef struct {
+    int device;
+    uint32_t lanes;            /* batches in flight at once (0: 2) */
+    uint32_t max_batch;        /* requests per batch (0: 64) */
+    uint64_t vertex_arena;     /* vertices the output arena holds, < 2^32 */
+    uint64_t quad_arena;       /* quads (and triangle pairs) the output arena holds, < 2^32 */
+    int want_triangles;
+    int plain;                 /* 1: one lane, each request extracted alone by dmc_extract_device */
+} dmc_server_config;
+
+typedef struct {
+    dmc_status status;
+    uint64_t n_vertices;
+    uint64_t n_quads;
+    const float *vertices;     /* device memory, 3 * n_vertices */
+    const uint32_t *quads;     /* device memory, 4 * n_quads; indices relative to vertices */
+    const uint32_t *triangles; /* device memory, 6 * n_quads, or NULL */
+    double t_submit, t_start, t_done;   /* seconds on the server's clock */
+    uint32_t batch_size;       /* requests in the batch that served this one */
+} dmc_server_result;
+
+typedef struct {
+    uint64_t submitted, completed, batches, max_batch_seen;
+    uint64_t arena_peak_vertices, arena_peak_quads;
+} dmc_server_stats;
+
+dmc_status dmc_server_create(const dmc_server_config *cfg, dmc_server **server);
+/* Fails requests never admitted, waits for batches in flight, frees everything. */
+dmc_status dmc_server_destroy(dmc_server *server);
+/* Adds a volume in DEVICE memory (owned by the caller, kept resident while the
+ * server lives).  DMC_ERR_OUTPUT_OVERFLOW if its bound exceeds the arenas. */
+dmc_status dmc_server_add_volume(dmc_server *server, const dmc_volume *vol, const float xyz_min[3],
+                                 const float xyz_max[3], uint32_t *volume_id);
+dmc_status dmc_server_submit(dmc_server *server, uint32_t volume_id, float iso, uint64_t *request_id);
+/* Waits up to timeout_s for the request; DMC_ERR_TIMEOUT if it is not done.
+ * The request's own status is in out->status. */
+dmc_status dmc_server_wait(dmc_server *server, uint64_t request_id, double timeout_s, dmc_server_result *out);
+/* Returns the request's output space to the arenas; the request id ends. */
+dmc_status dmc_server_release(dmc_server *server, uint64_t request_id);
+dmc_status dmc_server_get_stats(dmc_server *server, dmc_server_stats *stats);
+/* Load generator: submits request i at arrival_s[i] seconds after the call
+ * starts (a separate thread keeps the schedule), waits for and releases
+ * each, and reports latency_s[i] = done - submit and status[i]. */
+dmc_status dmc_server_replay(dmc_server *server, uint32_t n, const uint32_t *volume_ids, const float *isos,
+                             const double *arrival_s, double *latency_s, dmc_status *status);
+
 /* ---- no-allocation extraction (no reference counterpart) ----------------
  *
  * For callers that must not have the library allocate device memory: a
