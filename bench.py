@@ -352,13 +352,203 @@ def run_batch_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+SERVED_DESC = ("device-resident pool of 64 volumes, per-axis dims log-uniform 32-512, f32 blobs / u16 lattice "
+               "noise / f32 gyroid; requests (volume, iso uniform in that field's 5th-95th percentile) with "
+               "seeded Poisson arrivals; admission by worst-case output bound")
+
+
+def make_pool(device="cuda"):
+    """The serving pool and each volume's 5th/95th percentile (from a 1M-sample draw)."""
+    import torch
+    from framework_gb300 import fields
+    specs = fields.served_pool_specs()
+    vols = []
+    g = torch.Generator(device="cpu")
+    g.manual_seed(77)
+    for sp in specs:
+        t = fields.make_pool_volume(sp, device=device)
+        flat = t.reshape(-1)
+        idx = torch.randint(0, flat.numel(), (min(flat.numel(), 1 << 20),), generator=g).to(device)
+        smp = flat[idx].to(torch.int32) & 0xFFFF if t.dtype == torch.int16 else flat[idx]
+        lo, hi = torch.quantile(smp.to(torch.float32), torch.tensor([0.05, 0.95], device=device)).tolist()
+        vols.append(dict(volume=t, lo=lo, hi=hi, kind=sp["kind"], u16=t.dtype == torch.int16))
+    torch.cuda.synchronize()
+    return vols
+
+
+def request_trace(vols, n, rate, seed):
+    """n requests: uniform volume, iso uniform in [P5, P95]; Poisson arrivals at `rate`/s (0: all at once)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    vid = rng.integers(0, len(vols), n)
+    iso = np.array([rng.uniform(vols[v]["lo"], vols[v]["hi"]) for v in vid], np.float32)
+    arr = np.cumsum(rng.exponential(1.0 / rate, n)) if rate > 0 else np.zeros(n)
+    return vid.astype(np.uint32), iso, arr
+
+
+def _lat_summary(lat, arrivals, n):
+    import numpy as np
+    ok = lat[lat >= 0]
+    span = float(np.max(arrivals + lat)) if len(lat) else 0.0
+    return {"p50_ms": round(1e3 * float(np.percentile(ok, 50)), 3), "p99_ms": round(1e3 * float(np.percentile(ok, 99)), 3),
+            "throughput": round(n / span, 2) if span > 0 else None}
+
+
+def _warm(srv, idmap, vols):
+    """Every pool volume once, at its median-ish isovalue (graph capture, scratch growth)."""
+    import numpy as np
+    iso = np.array([0.5 * (d["lo"] + d["hi"]) for d in vols], np.float32)
+    srv.replay(idmap, iso, np.zeros(len(vols)))
+
+
+def served_measure(vols, n_req=600, quick=False):
+    """Saturation throughput and a Poisson load sweep for the batched server
+    and the plain per-request server on the same traces."""
+    import numpy as np
+    import framework_gb300 as fg
+    out = {}
+    servers = {"served": dict(lanes=2, max_batch=64), "plain": dict(plain=True)}
+    for name, kw in servers.items():
+        with fg.Server(0, vertex_arena=(1 << 31), quad_arena=(1 << 30), **kw) as srv:
+            ids = [srv.add_volume(d["volume"]) for d in vols]
+            idmap = np.array(ids, np.uint32)
+            _warm(srv, idmap, vols)
+            n_sat = n_req if name == "served" else max(64, n_req // 4)
+            vid, iso, arr = request_trace(vols, n_sat, 0, seed=2)
+            t0 = time.perf_counter()
+            lat, st = srv.replay(idmap[vid], iso, arr)
+            wall = time.perf_counter() - t0
+            if (st != 0).any():
+                print("%s saturation: failed requests by status %s" % (
+                    name, dict(zip(*[x.tolist() for x in np.unique(st[st != 0], return_counts=True)]))),
+                    file=sys.stderr, flush=True)
+            cap = n_sat / wall
+            out[name] = {"capacity_rps": round(cap, 2), "saturation": _lat_summary(lat, arr, n_sat),
+                         "stats": srv.stats()}
+    # offered loads: fractions of each server's own capacity, and the plain
+    # server's 80% load offered to both
+    loads = [("plain@0.8plain", "plain", 0.8 * out["plain"]["capacity_rps"]),
+             ("served@0.8plain", "served", 0.8 * out["plain"]["capacity_rps"]),
+             ("served@0.8served", "served", 0.8 * out["served"]["capacity_rps"])]
+    if not quick:
+        loads.insert(2, ("served@0.5served", "served", 0.5 * out["served"]["capacity_rps"]))
+    sweep = {}
+    for label, name, rate in loads:
+        kw = servers[name]
+        n = max(200, min(n_req, int(rate * (4.0 if not quick else 2.0))))
+        with fg.Server(0, vertex_arena=(1 << 31), quad_arena=(1 << 30), **kw) as srv:
+            idmap = np.array([srv.add_volume(d["volume"]) for d in vols], np.uint32)
+            _warm(srv, idmap, vols)
+            vid, iso, arr = request_trace(vols, n, rate, seed=3)
+            lat, st = srv.replay(idmap[vid], iso, arr)
+            bad = {int(k): int(c) for k, c in zip(*np.unique(st[st != 0], return_counts=True))}
+            if bad:
+                print("load %s: failed requests by status %s" % (label, bad), file=sys.stderr, flush=True)
+            sweep[label] = dict(offered_rps=round(rate, 2), requests=n, failed=bad, **_lat_summary(lat, arr, n))
+    out["sweep"] = sweep
+    return out
+
+
+def served_cpu_sample(vols, budget):
+    """The oracle, all host threads, on the first requests of the saturation trace for ~budget seconds."""
+    import oracle
+    from framework_gb300 import fields
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    vid, iso, _ = request_trace(vols, 256, 0, seed=2)
+    done, used = 0, 0.0
+    for v, x in zip(vid, iso):
+        t = vols[v]["volume"]
+        host = fields.as_u16_numpy(t) if vols[v]["u16"] else t.cpu().numpy()
+        t0 = time.perf_counter()
+        oracle.extract(host, iso=float(x))
+        used += time.perf_counter() - t0
+        done += 1
+        if used >= budget:
+            break
+    return done / used, cores, "first %d requests of the saturation trace (%.1f s)" % (done, used)
+
+
+def run_served_reference(args, rank):
+    """CPU restatement over a bounded prefix of the request trace (requests/s, all host threads)."""
+    if rank != 0:
+        return
+    import torch
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    vols = make_pool(dev)
+    v, cores, sample = served_cpu_sample(vols, min(20.0, 120.0 / max(1, args.steps + args.warmup)))
+    line = {
+        "impl": "reference", "metric": "requests/s", "value": round(v, 3), "unit": "requests/s",
+        "n_gpus": args.gpus, "steps": 1, "warmup": 0, "ms_per_step": round(1e3 / v, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+u16", "data": "synthetic",
+        "config": {"workload": "served64", "desc": SERVED_DESC},
+        "cpu_baseline": {"value": round(v, 3), "unit": "requests/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(v, 3), "unit": "requests/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_served(args, rank, world):
+    import numpy as np
+    import torch
+    import framework_gb300 as fg
+    vols = make_pool("cuda")
+    N = sum(d["volume"].numel() for d in vols)
+    nbytes = sum(d["volume"].numel() * d["volume"].element_size() for d in vols)
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    m = served_measure(vols, n_req=max(200, 60 * args.steps))
+    clk = clocks.stop()
+    # end to end: a burst of requests, each mesh copied to host memory and released
+    vid, iso, _ = request_trace(vols, 128, 0, seed=4)
+    d2h = 0
+    with fg.Server(0, vertex_arena=(1 << 31), quad_arena=(1 << 30)) as srv:
+        idmap = [srv.add_volume(d["volume"]) for d in vols]
+        for v in range(len(vols)):                     # warm up: each volume once
+            r = srv.submit(idmap[v], 0.5 * (vols[v]["lo"] + vols[v]["hi"]))
+            srv.wait(r, timeout=600.0)
+            srv.release(r)
+        t0 = time.perf_counter()
+        rids = [srv.submit(idmap[v], float(x)) for v, x in zip(vid, iso)]
+        for r in rids:
+            res = srv.wait(r, timeout=600.0)
+            vv, qq, _ = srv.fetch(res)
+            d2h += vv.nbytes + qq.nbytes
+            srv.release(r)
+        e2e_s = time.perf_counter() - t0
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        v, cores, sample = served_cpu_sample(vols, 10.0)
+        cpu = {"value": round(v, 3), "unit": "requests/s", "cores": cores, "kind": "port", "sample": sample}
+    line = {
+        "metric": "requests/s", "value": m["served"]["capacity_rps"], "unit": "requests/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 / m["served"]["capacity_rps"], 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+u16", "data": "synthetic",
+        "config": {"workload": "served64", "desc": SERVED_DESC, "volumes": len(vols), "points": N,
+                   "pool_bytes": nbytes, "mix": {k: sum(1 for d in vols if d["kind"] == k) for k in ("blobs", "noise", "gyroid")},
+                   "served": m["served"], "plain": m["plain"], "sweep": m["sweep"],
+                   "served_over_plain": round(m["served"]["capacity_rps"] / m["plain"]["capacity_rps"], 2),
+                   "p99_ms_at_0.8_served_capacity": m["sweep"]["served@0.8served"]["p99_ms"],
+                   "l2": "pool %.2f GB > L2" % (nbytes / 1e9)},
+        "cpu_baseline": cpu,
+        "e2e": {"value": round(len(rids) / e2e_s, 2), "unit": "requests/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(d2h / len(rids)), "note": "pool resident on the device; per request the mesh is copied to host"},
+        "gpu_launches": None,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="noise1024", choices=sorted(WORKLOADS) + ["batch256"])
+    ap.add_argument("--workload", default="noise1024", choices=sorted(WORKLOADS) + ["batch256", "served64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     args = ap.parse_args()
@@ -375,6 +565,8 @@ def main():
     if args.impl == "reference":
         if args.workload == "batch256":
             run_batch_reference(args, rank)
+        elif args.workload == "served64":
+            run_served_reference(args, rank)
         else:
             run_reference(args, rank)
         if dist:
@@ -383,6 +575,12 @@ def main():
         return
 
     torch.cuda.set_device(local)
+    if args.workload == "served64":
+        run_served(args, rank, world)
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
     if args.workload == "batch256":
         run_batch(args, rank, world)
         if dist:

@@ -848,6 +848,7 @@ struct BatchState {
     uint32_t cap_items = 0;
     uint64_t cap_seg = 0, cap_coord = 0;
     uint64_t layout_gen = 0;           // scratch_gen the layout was carved for (0: none)
+    uint64_t layout_id = 0;            // bumped on every re-carve: captured graphs hold the addresses
     // device layout (inside ctx->scratch)
     brick::BatchHead *d_plan = nullptr;
     uint2 *seg_cnt = nullptr, *seg_off = nullptr;
@@ -867,7 +868,7 @@ struct BatchState {
     // whose output arguments are rewritten when a batch targets other buffers
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
-    uint64_t g_scratch_gen = 0, g_stage_gen = 0;
+    uint64_t g_layout_id = 0, g_stage_gen = 0;
     cudaGraphNode_t emit_node[2] = {nullptr, nullptr};
     cudaKernelNodeParams emit_params[2]{};
     brick::EmitOut g_out{};
@@ -940,6 +941,7 @@ static dmc_status batch_layout(Ctx *ctx, BatchState &b, uint32_t items, uint64_t
     b.d_res = (dmc_batch_result *)(base + o_res);
     b.tickets = (uint32_t *)(base + o_tk);
     b.layout_gen = ctx->scratch_gen;
+    ++b.layout_id;
     const size_t stage = b.plan_bytes + sizeof(dmc_batch_result) * (size_t)b.cap_items;
     if (stage > b.h_stage_bytes) {
         if (b.h_stage) { CUDA_TRY(cudaDeviceSynchronize()); cudaFreeHost(b.h_stage); b.h_stage = nullptr; b.h_stage_bytes = 0; }
@@ -1070,7 +1072,7 @@ static dmc_status capture_graph(Ctx *ctx, BatchState &b, const brick::EmitOut &e
     ce = cudaGraphInstantiate(&b.gexec, graph, 0);
     if (ce != cudaSuccess) { cudaGraphDestroy(graph); CUDA_TRY(ce); }
     b.graph = graph;
-    b.g_scratch_gen = ctx->scratch_gen;
+    b.g_layout_id = b.layout_id;
     b.g_stage_gen = b.stage_gen;
     b.g_out = eo;
     return DMC_OK;
@@ -1179,7 +1181,7 @@ dmc_status brick_extract(Ctx *ctx, const BrickItem *items, uint32_t n, const Bri
     if (o.mode == BATCH_GRAPH) {
         // the graph's per-volume results always go to scratch; a caller's
         // device results are copied from there after the launch
-        if (!b.gexec || b.g_scratch_gen != ctx->scratch_gen || b.g_stage_gen != b.stage_gen) {
+        if (!b.gexec || b.g_layout_id != b.layout_id || b.g_stage_gen != b.stage_gen) {
             if ((s = capture_graph(ctx, b, eo, nb)) != DMC_OK) return s;
         }
         if ((s = retarget_graph(ctx, b, eo)) != DMC_OK) return s;

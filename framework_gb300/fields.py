@@ -164,3 +164,30 @@ def uneven_batch_specs(count=256, lo=16, hi=256, seed=5):
         iso = float(rng.uniform(-0.5, 0.5))
         specs.append(dict(dims=(int(d[0]), int(d[1]), int(d[2])), freq=f, iso=iso, seed=1000 + i))
     return specs
+
+
+def served_pool_specs(count=64, lo=32, hi=512, seed=9):
+    """Per-volume recipe of the serving pool: dims log-uniform in [lo, hi] per
+    axis; field kind uniform over blobs (float32), lattice noise (uint16) and
+    gyroid (float32).  Blobs keep 32 centres, sigma 8-32, amplitude 0.5-1.5;
+    noise keeps 4 octaves and persistence 0.5 with a base period of 32 voxels
+    (most pool volumes are far smaller than 1024); gyroid frequency uniform in
+    [0.05, 0.4] rad/voxel."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(count):
+        d = np.floor(np.exp(rng.uniform(math.log(lo), math.log(hi), 3))).astype(int)
+        d = np.clip(d, lo, hi)
+        kind = ("blobs", "noise", "gyroid")[int(rng.integers(0, 3))]
+        specs.append(dict(dims=(int(d[0]), int(d[1]), int(d[2])), kind=kind,
+                          freq=float(rng.uniform(0.05, 0.4)), seed=2000 + i))
+    return specs
+
+
+def make_pool_volume(spec, device="cuda"):
+    """One serving-pool volume from served_pool_specs (float32, or int16 holding uint16 bits)."""
+    if spec["kind"] == "blobs":
+        return gaussian_blobs(spec["dims"], seed=spec["seed"], device=device)
+    if spec["kind"] == "noise":
+        return value_noise_u16(spec["dims"], base_period=32, seed=spec["seed"], device=device)
+    return gyroid(spec["dims"], spec["freq"], seed=spec["seed"], device=device)

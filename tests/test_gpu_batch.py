@@ -214,6 +214,21 @@ def test_uneven_gyroid_batch(extractor):
     _check_slices(vols, res, v, q, t, alone)
 
 
+def test_graph_after_layout_growth():
+    """Growing batches in graph mode on a fresh context: each growth re-carves
+    the scratch layout (often inside the same allocation); the graph must be
+    captured again and every batch stay exact."""
+    import framework_gb300 as fg
+    vols = _mixed_batch(21, count=14)
+    with fg.Extractor(0) as ex:
+        alone = [_alone(ex, d) for d in vols]
+        v, q, t = _buffers(*_total(alone))
+        for k in (1, 2, 4, 7, 14, 3):
+            ex.extract_batch(vols[:k], v, q, t, mode="graph")
+            nv, nq, res = ex.batch_wait()
+            _check_slices(vols[:k], res, v, q, t, alone[:k])
+
+
 def test_default_stream_ordering(extractor, batch_case):
     """A volume written by torch on its current stream just before an
     asynchronous batch is seen complete by the batch."""
