@@ -37,6 +37,9 @@ WORKLOADS = {
                  "512^3 float32 sum of 32 Gaussian blobs (sigma 8-32, amplitude 0.5-1.5), iso 0.5"),
     "sphere64": ((64, 64, 64), "float32", 0.0,
                  "64^3 float32 sphere SDF radius 20 + uniform noise 0.01, iso 0"),
+    # the 1024^3 noise field's statistics on an eighth of the volume (profiling case)
+    "noise512": ((512, 512, 512), "uint16", 32768.0,
+                 "512^3 uint16 4-octave lattice value noise (period 128, persistence 0.5), iso 32768"),
 }
 
 
@@ -44,7 +47,7 @@ def make_volume(name, device, zrange=None):
     import torch
     from framework_gb300 import fields
     dims, dtype, iso, _ = WORKLOADS[name]
-    if name == "noise1024":
+    if name in ("noise1024", "noise512"):
         vol = fields.value_noise_u16(dims, device=device)
     elif name == "blobs512":
         vol = fields.gaussian_blobs(dims, device=device)
@@ -296,6 +299,7 @@ def run_batch(args, rank, world):
         hq.copy_(qbuf, non_blocking=True)
         torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
+    line = None
     if rank == 0:
         hbm, peak_kind = peaks()
         alg_bytes = 4 * N + 12 * V + 16 * Q
@@ -328,8 +332,8 @@ def run_batch(args, rank, world):
             "gpu_launches": 7 * args.steps,
             "clocks": clk,
         }
-        print(json.dumps(line), flush=True)
     ex.close()
+    return line if rank == 0 else None
 
 
 def run_batch_reference(args, rank):
@@ -518,7 +522,7 @@ def run_served(args, rank, world):
             srv.release(r)
         e2e_s = time.perf_counter() - t0
     if rank != 0:
-        return
+        return None
     cpu = None
     if not args.no_cpu_baseline:
         v, cores, sample = served_cpu_sample(vols, 10.0)
@@ -536,10 +540,10 @@ def run_served(args, rank, world):
         "cpu_baseline": cpu,
         "e2e": {"value": round(len(rids) / e2e_s, 2), "unit": "requests/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": int(d2h / len(rids)), "note": "pool resident on the device; per request the mesh is copied to host"},
-        "gpu_launches": None,
+        "gpu_launches": 7 * m["served"]["stats"]["batches"],
         "clocks": clk,
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def main():
@@ -551,6 +555,8 @@ def main():
     ap.add_argument("--workload", default="noise1024", choices=sorted(WORKLOADS) + ["batch256", "served64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default workload only: skip the batched and served summaries")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -576,13 +582,17 @@ def main():
 
     torch.cuda.set_device(local)
     if args.workload == "served64":
-        run_served(args, rank, world)
+        line = run_served(args, rank, world)
+        if line:
+            print(json.dumps(line), flush=True)
         if dist:
             dist.barrier()
             dist.destroy_process_group()
         return
     if args.workload == "batch256":
-        run_batch(args, rank, world)
+        line = run_batch(args, rank, world)
+        if line:
+            print(json.dumps(line), flush=True)
         if dist:
             dist.barrier()
             dist.destroy_process_group()
@@ -668,11 +678,31 @@ def main():
             "cpu_baseline": cpu,
             "e2e": {"value": round(N / e2e_s / 1e9, 3), "unit": "GVoxels/s", "h2d_bytes_per_step": elem * N,
                     "d2h_bytes_per_step": 12 * V + 16 * Q + 24 * Q, "steps": e2e_steps},
-            "gpu_launches": 4 * args.steps,
+            "gpu_launches": 5 * args.steps,
             "clocks": clk,
         }
-        print(json.dumps(line), flush=True)
     ex.close()
+    if not args.no_extras:
+        # the batched (256 uneven volumes) and served (64-volume pool) forms, summarised
+        del vol, vbuf, qbuf
+        torch.cuda.empty_cache()
+        sub = argparse.Namespace(**vars(args))
+        sub.no_cpu_baseline = True
+        sub.steps, sub.e2e_steps = min(args.steps, 10), 1
+        b = run_batch(sub, rank, world)
+        torch.cuda.empty_cache()
+        sv = run_served(sub, rank, world)
+        if line is not None:
+            line["batched"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "e2e", "roofline")}
+            line["batched"].update({k: b["config"][k] for k in ("volumes", "points", "plain_volumes_per_s",
+                                                               "batched_over_plain", "autotune", "kernel_ms")})
+            line["served"] = {"value": sv["value"], "unit": sv["unit"], "e2e": sv["e2e"]}
+            line["served"].update({k: sv["config"][k] for k in ("volumes", "pool_bytes", "served_over_plain",
+                                                                "p99_ms_at_0.8_served_capacity", "sweep")})
+            line["served"]["plain_capacity_rps"] = sv["config"]["plain"]["capacity_rps"]
+            line["gpu_launches"] += b["gpu_launches"] + sv["gpu_launches"]
+    if line is not None:
+        print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
         dist.destroy_process_group()

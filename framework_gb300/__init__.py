@@ -20,7 +20,7 @@ import numpy as np
 from . import build as _build
 
 __all__ = ["DMCError", "Extractor", "Server", "Mesh", "setup_device_luts", "run_dmc", "cleanup_device_luts",
-           "load_library", "STATUS"]
+           "write_obj", "load_library", "STATUS"]
 
 STATUS = {
     0: "DMC_OK", 1: "DMC_ERR_INVALID_ARG", 2: "DMC_ERR_OOM", 3: "DMC_ERR_OUTPUT_OVERFLOW",
@@ -37,7 +37,7 @@ ABI_SYMBOLS = [
     "dmc_set_algo", "dmc_run", "dmc_mesh_free", "dmc_extract_device", "dmc_get_stats",
     "dmc_extract_batch", "dmc_batch_wait", "dmc_set_option", "dmc_extract_device_noalloc",
     "dmc_server_create", "dmc_server_destroy", "dmc_server_add_volume", "dmc_server_submit", "dmc_server_wait",
-    "dmc_server_release", "dmc_server_get_stats", "dmc_server_replay",
+    "dmc_server_release", "dmc_server_get_stats", "dmc_server_replay", "dmc_write_obj",
 ]
 BATCH_ASYNC, BATCH_GRAPH = 0x1, 0x2
 OPT_BRICK_PLANES = 1
@@ -140,6 +140,8 @@ def load_library(build_if_missing=True):
                                     ctypes.c_void_p]
     L.dmc_batch_wait.argtypes = [ctypes.c_void_p, P(_BatchResult), P(ctypes.c_uint64), P(ctypes.c_uint64)]
     L.dmc_set_option.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int64]
+    L.dmc_write_obj.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
+                                ctypes.c_uint32]
     L.dmc_server_create.argtypes = [P(_ServerConfig), P(ctypes.c_void_p)]
     L.dmc_server_destroy.argtypes = [ctypes.c_void_p]
     L.dmc_server_add_volume.argtypes = [ctypes.c_void_p, P(_Volume), P(ctypes.c_float), P(ctypes.c_float),
@@ -524,6 +526,19 @@ class _DeviceArray:
     def __init__(self, ptr, shape, typestr):
         self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (int(ptr), False),
                                          "version": 2, "strides": None}
+
+
+def write_obj(path, vertices, faces):
+    """``dmc_write_obj``: vertices (V,3) float32 and triangles (T,3) or quads
+    (Q,4) uint32 in host memory to a Wavefront OBJ file, in the reference's
+    dump_obj format (dmc.cu:2238-2246)."""
+    L = load_library()
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+    f = np.ascontiguousarray(faces, np.uint32)
+    if f.ndim != 2 or f.shape[1] not in (3, 4):
+        raise DMCError(1, "faces must be (n, 3) or (n, 4)")
+    _check(L.dmc_write_obj(os.fsencode(path), v.ctypes.data, v.shape[0], f.ctypes.data, f.shape[0], f.shape[1]),
+           "dmc_write_obj")
 
 
 # ---------------------------------------------------------------------------

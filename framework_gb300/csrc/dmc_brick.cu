@@ -160,9 +160,12 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
     const uint64_t plane0 = (uint64_t)p * pts.y;
     const T *base = vol + (plane0 + y0) * sx + x0 + lane;
     if (p + 1 < pts.z && (uint32_t)lane < nrow) {
-        // next plane, this lane's row: every line of the brick's columns
+        // next plane, this lane's row: the lines of the brick's own columns.
+        // The two halo columns are left to demand loads: prefetching their
+        // line would pull in a whole line of the next brick's columns, which
+        // is usually evicted before that brick is swept.
         const char *nxt = reinterpret_cast<const char *>(vol + (plane0 + pts.y + y0 + lane) * sx + x0);
-        const uint32_t bytes = min((uint32_t)(W + 2), pts.x - x0) * (uint32_t)sizeof(T);
+        const uint32_t bytes = min((uint32_t)W, pts.x - x0) * (uint32_t)sizeof(T);
         for (uint32_t o = 0; o < bytes; o += 128) asm volatile("prefetch.global.L2 [%0];" ::"l"(nxt + o));
     }
     bool cok[GROUPS];

@@ -130,6 +130,14 @@ dmc_status dmc_extract_device(dmc_ctx *ctx, const dmc_volume *vol, const float x
                               uint32_t *d_triangles,
                               uint64_t *n_vertices, uint64_t *n_quads, void *stream);
 
+/* Writes a mesh in host memory as Wavefront OBJ, in the format of the
+ * reference's dump_obj (dmc.cu:2238-2246): "v x y z" lines (six significant
+ * digits), then "f ..." lines with 1-based indices; verts_per_face is 3
+ * (triangles) or 4 (quads).  Indices out of range give DMC_ERR_INVALID_ARG
+ * before anything is written. */
+dmc_status dmc_write_obj(const char *path, const float *vertices, uint64_t n_vertices,
+                         const uint32_t *faces, uint64_t n_faces, uint32_t verts_per_face);
+
 /* Counters of the last call on this context (for a batch: summed over its
  * volumes). */
 dmc_status dmc_get_stats(const dmc_ctx *ctx, dmc_stats *stats);
