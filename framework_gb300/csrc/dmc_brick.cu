@@ -676,25 +676,30 @@ __global__ void __launch_bounds__(32 * NWB, EMIT ? 2 : 4) brick_sweep(const Batc
                             if (q >= out.qcap) {
                                 atomicOr(err, DEV_ERR_OVERFLOW);
                             } else {
-                                const uint32_t e_up = s != 1 ? entry_of(S, prv, r + 1, c) : 0u;    // (c, r+1, k-1)
-                                const uint32_t e_z = s != 0 ? entry_of(S, cur, r, c) : 0u;         // (c, r, k)
-                                const uint32_t e_zup = s == 2 ? entry_of(S, cur, r + 1, c) : 0u;   // (c, r+1, k)
                                 const uint32_t ring = s == 0 ? kRing6 : (s == 1 ? kRing9 : kRing10);
                                 const bool ccw = (info >> (s + 3)) & 1u;
-                                uint32_t idx[4];
-#pragma unroll
+                                // one rolled lookup site for the four ring cells keeps the
+                                // sweep's code within the instruction cache
+                                uint32_t idx[4] = {0u, 0u, 0u, 0u};
+#pragma unroll 1
                                 for (int it = 0; it < 4; ++it) {
                                     const int kk = ccw ? it : (4 - it) & 3;    // ccw 0,1,2,3; cw 0,3,2,1 (dmc.cu:1636-1645)
                                     const uint32_t sl = (ring >> (8 * kk)) & 0xffu;
                                     const int pl = (sl & 1u) ? cur : prv;
-                                    const uint32_t bsel = (sl >> 1) & 3u;
                                     const uint32_t plus = (sl >> 3) & 1u, dr = (sl >> 4) & 1u;
-                                    const uint32_t li = (bsel == 0 ? oi : bsel == 1 ? e_up : bsel == 2 ? e_z : e_zup) + plus;
-                                    if (li >= S.rowstart[pl][HROWS]) { atomicOr(err, DEV_ERR_BOUNDS); idx[it] = 0; continue; }
-                                    const uint32_t rd = M.ent(pl, li);
-                                    uint32_t m = lut_m(tab, cell_cfg(rd), cell_l2(rd), (int)ring_edge(s, kk));
-                                    if (m == 0xffu) { atomicOr(err, DEV_ERR_BOUNDS); m = 0; }
-                                    idx[it] = S.segv[pl][r + dr][(c + (int)plus) == W ? 1 : 0] + cell_vrel(rd) + m - g.vbase;
+                                    // ring cell (c + plus, r + dr) of plane pl follows (c, r + dr) in its list
+                                    const uint32_t li = entry_of(S, pl, r + (int)dr, c) + plus;
+                                    uint32_t val = 0;
+                                    if (li >= S.rowstart[pl][HROWS]) {
+                                        atomicOr(err, DEV_ERR_BOUNDS);
+                                    } else {
+                                        const uint32_t rd = M.ent(pl, li);
+                                        uint32_t m = lut_m(tab, cell_cfg(rd), cell_l2(rd), (int)ring_edge(s, kk));
+                                        if (m == 0xffu) { atomicOr(err, DEV_ERR_BOUNDS); m = 0; }
+                                        val = S.segv[pl][r + dr][(c + (int)plus) == W ? 1 : 0] + cell_vrel(rd) + m - g.vbase;
+                                    }
+#pragma unroll
+                                    for (int j = 0; j < 4; ++j) idx[j] = it == j ? val : idx[j];
                                 }
                                 reinterpret_cast<uint4 *>(out.quads)[q] = make_uint4(idx[0], idx[1], idx[2], idx[3]);
                                 if (out.tris) {
