@@ -143,6 +143,16 @@ __device__ __forceinline__ uint32_t at_or_below(uint16_t v, float, uint32_t thr)
 template <class T>
 __device__ __forceinline__ T raw_load(const T *p) { return __ldg(p); }
 
+// Four consecutive samples in one load (8 bytes of uint16, 16 of float).
+__device__ __forceinline__ uint2 load4(const uint16_t *p) { return __ldg(reinterpret_cast<const uint2 *>(p)); }
+__device__ __forceinline__ float4 load4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
+__device__ __forceinline__ uint16_t elem4(uint2 v, int q)
+{
+    const uint32_t w = q < 2 ? v.x : v.y;
+    return (uint16_t)((q & 1) ? (w >> 16) : (w & 0xffffu));
+}
+__device__ __forceinline__ float elem4(float4 v, int q) { return q == 0 ? v.x : q == 1 ? v.y : q == 2 ? v.z : v.w; }
+
 // Column masks of point plane p for the lane's columns x0+lane+32j and the two
 // halo columns x0+W, x0+W+1: bit r = sample (x, y0+r, p) below the isovalue,
 // rows 0..33.  Samples outside the volume read as 0 (their cells are never
@@ -158,7 +168,6 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
     const uint32_t nrow = pz ? min(34u, pts.y - y0) : 0u;
     const uint64_t sx = pts.x;
     const uint64_t plane0 = (uint64_t)p * pts.y;
-    const T *base = vol + (plane0 + y0) * sx + x0 + lane;
     if (p + 1 < pts.z && (uint32_t)lane < nrow) {
         // next plane, this lane's row: the lines of the brick's own columns.
         // The two halo columns are left to demand loads: prefetching their
@@ -172,50 +181,91 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
 #pragma unroll
     for (int j = 0; j < GROUPS; ++j) cok[j] = x0 + lane + 32 * j < pts.x;
     const bool full = cok[GROUPS - 1] && nrow == 34;
-    if (full) {
+    // All 34 rows and 128 columns in range and rows aligned for 4-sample
+    // loads (warp-uniform): lane l takes the adjacent columns 4l..4l+3 of a
+    // row in one load.  Otherwise lane l takes columns l, l+32, l+64, l+96.
+    const bool vec = nrow == 34 && x0 + W <= pts.x && (pts.x & 3u) == 0 &&
+                     (reinterpret_cast<uintptr_t>(vol) & (4 * sizeof(T) - 1)) == 0;
+    if (vec) {
+        const T *vb = vol + (plane0 + y0) * sx + x0 + 4 * lane;
+        using V = decltype(load4(vb));
 #pragma unroll 1
         for (int r0 = 0; r0 < 32; r0 += 8) {
-            T v[8][GROUPS];
+            V v[8];
 #pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const T *row = base + (uint64_t)(r0 + i) * sx;
-#pragma unroll
-                for (int j = 0; j < GROUPS; ++j) v[i][j] = raw_load(row + 32 * j);
-            }
+            for (int i = 0; i < 8; ++i) v[i] = load4(vb + (uint64_t)(r0 + i) * sx);
 #pragma unroll
             for (int i = 0; i < 8; ++i)
 #pragma unroll
-                for (int j = 0; j < GROUPS; ++j) {
-                    lo[j] |= below(v[i][j], iso, thr) << (r0 + i);
-                    elo[j] |= at_or_below(v[i][j], iso, thr_le) << (r0 + i);
+                for (int q = 0; q < 4; ++q) {
+                    const T t = elem4(v[i], q);
+                    lo[q] |= below(t, iso, thr) << (r0 + i);
+                    elo[q] |= at_or_below(t, iso, thr_le) << (r0 + i);
                 }
         }
 #pragma unroll
         for (int i = 0; i < 2; ++i) {
-            const T *row = base + (uint64_t)(32 + i) * sx;
+            const V v = load4(vb + (uint64_t)(32 + i) * sx);
 #pragma unroll
-            for (int j = 0; j < GROUPS; ++j) {
-                const T v = raw_load(row + 32 * j);
-                hi[j] |= below(v, iso, thr) << i;
-                ehi[j] |= at_or_below(v, iso, thr_le) << i;
+            for (int q = 0; q < 4; ++q) {
+                const T t = elem4(v, q);
+                hi[q] |= below(t, iso, thr) << i;
+                ehi[q] |= at_or_below(t, iso, thr_le) << i;
             }
         }
+        // columns 4l..4l+3: two 16-byte stores per mask
+        uint4 *lt4 = reinterpret_cast<uint4 *>(&m.lt[4 * lane]), *le4 = reinterpret_cast<uint4 *>(&m.le[4 * lane]);
+        lt4[0] = make_uint4(lo[0], hi[0], lo[1], hi[1]);
+        lt4[1] = make_uint4(lo[2], hi[2], lo[3], hi[3]);
+        le4[0] = make_uint4(elo[0], ehi[0], elo[1], ehi[1]);
+        le4[1] = make_uint4(elo[2], ehi[2], elo[3], ehi[3]);
     } else {
-        for (uint32_t r = 0; r < nrow; ++r) {
-            const T *row = base + (uint64_t)r * sx;
-            for (int j = 0; j < GROUPS; ++j) {
-                if (!cok[j]) continue;
-                const T v = raw_load(row + 32 * j);
-                const uint32_t b = below(v, iso, thr), e = at_or_below(v, iso, thr_le);
-                if (r < 32) { lo[j] |= b << r; elo[j] |= e << r; }
-                else { hi[j] |= b << (r - 32); ehi[j] |= e << (r - 32); }
+        const T *base = vol + (plane0 + y0) * sx + x0 + lane;
+        if (full) {
+#pragma unroll 1
+            for (int r0 = 0; r0 < 32; r0 += 8) {
+                T v[8][GROUPS];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const T *row = base + (uint64_t)(r0 + i) * sx;
+#pragma unroll
+                    for (int j = 0; j < GROUPS; ++j) v[i][j] = raw_load(row + 32 * j);
+                }
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+#pragma unroll
+                    for (int j = 0; j < GROUPS; ++j) {
+                        lo[j] |= below(v[i][j], iso, thr) << (r0 + i);
+                        elo[j] |= at_or_below(v[i][j], iso, thr_le) << (r0 + i);
+                    }
+            }
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const T *row = base + (uint64_t)(32 + i) * sx;
+#pragma unroll
+                for (int j = 0; j < GROUPS; ++j) {
+                    const T v = raw_load(row + 32 * j);
+                    hi[j] |= below(v, iso, thr) << i;
+                    ehi[j] |= at_or_below(v, iso, thr_le) << i;
+                }
+            }
+        } else {
+            for (uint32_t r = 0; r < nrow; ++r) {
+                const T *row = base + (uint64_t)r * sx;
+                for (int j = 0; j < GROUPS; ++j) {
+                    if (!cok[j]) continue;
+                    const T v = raw_load(row + 32 * j);
+                    const uint32_t b = below(v, iso, thr), e = at_or_below(v, iso, thr_le);
+                    if (r < 32) { lo[j] |= b << r; elo[j] |= e << r; }
+                    else { hi[j] |= b << (r - 32); ehi[j] |= e << (r - 32); }
+                }
             }
         }
-    }
 #pragma unroll
-    for (int j = 0; j < GROUPS; ++j) {
-        m.lt[lane + 32 * j] = (uint64_t)lo[j] | ((uint64_t)hi[j] << 32);
-        m.le[lane + 32 * j] = (uint64_t)elo[j] | ((uint64_t)ehi[j] << 32);
+        for (int j = 0; j < GROUPS; ++j) {
+            m.lt[lane + 32 * j] = (uint64_t)lo[j] | ((uint64_t)hi[j] << 32);
+            m.le[lane + 32 * j] = (uint64_t)elo[j] | ((uint64_t)ehi[j] << 32);
+        }
     }
 #pragma unroll 1
     for (int hc = 0; hc < 2; ++hc) {
