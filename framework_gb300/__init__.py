@@ -276,7 +276,7 @@ class Extractor:
         return Mesh(verts, quads, tris, self.stats())
 
     def extract_device(self, volume, xyz_min=None, xyz_max=None, iso=0.0, vertices=None, quads=None,
-                       triangles=None, stream=None, dims=None, dtype=None):
+                       triangles=None, stream=None, dims=None, dtype=None, num_smooth=0):
         """Device-memory extraction (``dmc_extract_device``).
 
         ``volume`` is a CUDA tensor [z,y,x] (float32, or int16 holding uint16
@@ -308,7 +308,8 @@ class Extractor:
             qcap = min(qcap, triangles.numel() // 6)
         nv, nq = ctypes.c_uint64(), ctypes.c_uint64()
         st = _stream_handle(stream)
-        rc = self._lib.dmc_extract_device(self._h, ctypes.byref(vol), _f3(mn), _f3(mx), ctypes.c_float(iso), 0,
+        rc = self._lib.dmc_extract_device(self._h, ctypes.byref(vol), _f3(mn), _f3(mx), ctypes.c_float(iso),
+                                          int(num_smooth),
                                           vptr, vcap, qptr, qcap, tptr, ctypes.byref(nv), ctypes.byref(nq), st)
         if rc != 0:
             e = DMCError(rc, "dmc_extract_device")

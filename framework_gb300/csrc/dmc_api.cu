@@ -111,7 +111,9 @@ static dmc_status run_path(dmc_ctx *ctx, ExtractArgs &a, cudaStream_t st)
 {
     Ctx *c = &ctx->c;
     int algo = c->algo;
-    if (algo == DMC_ALGO_AUTO) algo = brick_supports(a) ? DMC_ALGO_BRICK : DMC_ALGO_SIMPLE;
+    // smoothing needs per-cell offsets, which only the simple path keeps
+    if (a.num_smooth && algo == DMC_ALGO_BRICK) return DMC_ERR_UNSUPPORTED;
+    if (algo == DMC_ALGO_AUTO) algo = (brick_supports(a) && !a.num_smooth) ? DMC_ALGO_BRICK : DMC_ALGO_SIMPLE;
     if (algo == DMC_ALGO_BRICK && !brick_supports(a)) return DMC_ERR_UNSUPPORTED;
     c->stats.algo = algo;
     return algo == DMC_ALGO_BRICK ? brick_run(c, a, st) : simple_run(c, a, st);
@@ -235,11 +237,13 @@ dmc_status dmc_extract_device(dmc_ctx *ctx, const dmc_volume *vol, const float x
                               uint64_t *n_vertices, uint64_t *n_quads, void *stream)
 {
     if (!ctx || !n_vertices || !n_quads) return DMC_ERR_INVALID_ARG;
-    if (num_smooth) return DMC_ERR_UNSUPPORTED;
     ExtractArgs a;
     dmc_status s = make_args(vol, xyz_min, xyz_max, iso, a);
     if (s != DMC_OK) return s;
     if ((vertex_capacity && !d_vertices) || (quad_capacity && !d_quads)) return DMC_ERR_INVALID_ARG;
+    // smoothing walks the quad rings, so it needs the quad buffer with the vertices
+    if (num_smooth && (!d_vertices) != (!d_quads)) return DMC_ERR_INVALID_ARG;
+    a.num_smooth = num_smooth;
     Ctx *c = &ctx->c;
     if (c->batch_pending) return DMC_ERR_INVALID_ARG;   // an asynchronous batch holds the scratch
     if (cudaSetDevice(c->device) != cudaSuccess) return DMC_ERR_CUDA;
@@ -346,10 +350,10 @@ dmc_status dmc_run(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min[3], 
 {
     if (!ctx || !out) return DMC_ERR_INVALID_ARG;
     memset(out, 0, sizeof(*out));
-    if (num_smooth) return DMC_ERR_UNSUPPORTED;
     ExtractArgs a;
     dmc_status s = make_args(vol, xyz_min, xyz_max, iso, a);
     if (s != DMC_OK) return s;
+    a.num_smooth = num_smooth;
     Ctx *c = &ctx->c;
     if (c->batch_pending) return DMC_ERR_INVALID_ARG;   // an asynchronous batch holds the scratch
     if (cudaSetDevice(c->device) != cudaSuccess) return DMC_ERR_CUDA;

@@ -64,6 +64,7 @@ struct ExtractArgs {
     uint32_t *tris;
     uint64_t *n_vertices, *n_quads;
     bool sizing_only;                  // count only: report totals, write no mesh
+    uint32_t num_smooth;               // smoothing iterations (simple path; needs the quad buffer)
 };
 
 dmc_status ctx_reserve_scratch(Ctx *ctx, size_t bytes);

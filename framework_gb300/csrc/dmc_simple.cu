@@ -201,6 +201,190 @@ __global__ void __launch_bounds__(kSimpleThreads) simple_emit(const T *vol, uint
 }
 
 // ---------------------------------------------------------------------------
+// Vertex smoothing (dmc.cu:1710-1981, driven at 2157-2169).  One iteration:
+// simple_smooth_edges moves the crossing of every owned edge that has a quad
+// onto the split triangle of its ring of four dual vertices, projected along
+// the edge's axis; simple_smooth_duals then recomputes every dual vertex as
+// the mean of its patch's crossings.  Single precision with explicit rounding
+// (no fused multiply-add), correctly rounded square root and division, in the
+// reference's operand order.  Two restatements of the reference's arithmetic:
+// lengths are normalised with 1/sqrt instead of the approximate rsqrtf, and a
+// convex quadrilateral is split at the corner with the smallest cosine
+// instead of the largest acosf angle (the same corner except where acosf
+// rounds two cosines to one angle).
+
+__device__ __forceinline__ bool cross_z_positive(float lx, float ly, float mx, float my, float rx, float ry)
+{
+    const float dx1 = __fsub_rn(rx, mx), dy1 = __fsub_rn(ry, my);
+    const float dx2 = __fsub_rn(lx, mx), dy2 = __fsub_rn(ly, my);
+    return __fsub_rn(__fmul_rn(dx1, dy2), __fmul_rn(dx2, dy1)) >= 0.f;
+}
+
+__device__ __forceinline__ float corner_cos(float lx, float ly, float mx, float my, float rx, float ry)
+{
+    float ux = __fsub_rn(lx, mx), uy = __fsub_rn(ly, my), vx = __fsub_rn(rx, mx), vy = __fsub_rn(ry, my);
+    const float iu = __fdiv_rn(1.f, __fsqrt_rn(__fadd_rn(__fmul_rn(ux, ux), __fmul_rn(uy, uy))));
+    const float iv = __fdiv_rn(1.f, __fsqrt_rn(__fadd_rn(__fmul_rn(vx, vx), __fmul_rn(vy, vy))));
+    ux = __fmul_rn(ux, iu); uy = __fmul_rn(uy, iu); vx = __fmul_rn(vx, iv); vy = __fmul_rn(vy, iv);
+    return __fadd_rn(__fmul_rn(ux, vx), __fmul_rn(uy, vy));
+}
+
+// is_inside_triangle (dmc.cu:1894-1912) in the projection plane
+__device__ __forceinline__ bool inside_triangle(const float p0[2], const float p1[2], const float p2[2], float ox,
+                                                float oy, float &alpha, float &beta, float &gamma)
+{
+    const float v0x = __fsub_rn(p1[0], p0[0]), v0y = __fsub_rn(p1[1], p0[1]);
+    const float v1x = __fsub_rn(p2[0], p0[0]), v1y = __fsub_rn(p2[1], p0[1]);
+    const float v2x = __fsub_rn(ox, p0[0]), v2y = __fsub_rn(oy, p0[1]);
+    const float d00 = __fadd_rn(__fmul_rn(v0x, v0x), __fmul_rn(v0y, v0y));
+    const float d10 = __fadd_rn(__fmul_rn(v1x, v0x), __fmul_rn(v1y, v0y));
+    const float d11 = __fadd_rn(__fmul_rn(v1x, v1x), __fmul_rn(v1y, v1y));
+    const float d20 = __fadd_rn(__fmul_rn(v2x, v0x), __fmul_rn(v2y, v0y));
+    const float d21 = __fadd_rn(__fmul_rn(v2x, v1x), __fmul_rn(v2y, v1y));
+    const float inv = __fdiv_rn(1.f, __fsub_rn(__fmul_rn(d00, d11), __fmul_rn(d10, d10)));
+    beta = __fmul_rn(__fsub_rn(__fmul_rn(d11, d20), __fmul_rn(d10, d21)), inv);
+    gamma = __fmul_rn(__fsub_rn(__fmul_rn(d00, d21), __fmul_rn(d10, d20)), inv);
+    alpha = __fsub_rn(__fsub_rn(1.f, beta), gamma);
+    return (-1e-4 < (double)beta) && (-1e-4 < (double)gamma) && ((double)__fadd_rn(beta, gamma) < 1.0 + 1e-4);
+}
+
+// New crossing of owned edge s (0: edge 6, 1: 9, 2: 10) from its quad ring;
+// false when it stays (complex quadrilateral, or the edge outside both halves).
+__device__ bool smooth_edge(const float *__restrict__ verts, const uint32_t ring[4], int s, float ox, float oy,
+                            float out[3])
+{
+    const int ax = s == 2 ? 1 : 0, ay = s == 0 ? 1 : 2;     // 6: xy, 9: xz, 10: yz
+    float P[4][2];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        P[i][0] = verts[3 * (uint64_t)ring[i] + ax];
+        P[i][1] = verts[3 * (uint64_t)ring[i] + ay];
+    }
+    int npos = 0, ipos = 0, ineg = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int l = (i + 3) & 3, r = (i + 1) & 3;
+        if (cross_z_positive(P[l][0], P[l][1], P[i][0], P[i][1], P[r][0], P[r][1])) { ++npos; ipos = i; }
+        else ineg = i;
+    }
+    if (npos == 2) return false;
+    int split0;
+    if (npos == 0 || npos == 4) {
+        float best = corner_cos(P[3][0], P[3][1], P[0][0], P[0][1], P[1][0], P[1][1]);
+        split0 = 0;
+#pragma unroll
+        for (int i = 1; i < 4; ++i) {
+            const int l = (i + 3) & 3, r = (i + 1) & 3;
+            const float c = corner_cos(P[l][0], P[l][1], P[i][0], P[i][1], P[r][0], P[r][1]);
+            if (c < best) { best = c; split0 = i; }
+        }
+    } else {
+        split0 = npos == 1 ? ipos : ineg;
+    }
+    const int split1 = (split0 + 2) & 3;
+    float al, be, ga;
+    int a, b, c;
+    if (inside_triangle(P[split0], P[(split0 + 1) & 3], P[split1], ox, oy, al, be, ga)) {
+        a = split0; b = (split0 + 1) & 3; c = split1;
+    } else if (inside_triangle(P[split1], P[(split1 + 1) & 3], P[split0], ox, oy, al, be, ga)) {
+        a = split1; b = (split1 + 1) & 3; c = split0;
+    } else {
+        return false;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float t = __fmul_rn(al, verts[3 * (uint64_t)ring[a] + k]);
+        t = __fadd_rn(t, __fmul_rn(be, verts[3 * (uint64_t)ring[b] + k]));
+        t = __fadd_rn(t, __fmul_rn(ga, verts[3 * (uint64_t)ring[c] + k]));
+        out[k] = t;
+    }
+    return true;
+}
+
+// bipolar/ccw bits of each active cell's own edges, for the smoothing passes
+template <class T>
+__global__ void __launch_bounds__(kSimpleThreads) simple_info(const T *vol, uint3 pts, uint3 cells, float iso,
+                                                              const uint8_t *cnt, uint8_t *inf, uint64_t n_cells)
+{
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n_cells; c += (uint64_t)gridDim.x * blockDim.x) {
+        if (!cnt[c]) continue;
+        uint32_t x, y, z;
+        cell_xyz(c, cells, x, y, z);
+        float v[8];
+        load_corners(vol, pts, x, y, z, v);
+        inf[c] = (uint8_t)owned_edge_info(v, iso);
+    }
+}
+
+__global__ void __launch_bounds__(kSimpleThreads) simple_smooth_edges(uint3 cells, float3 mn, float3 rng,
+        const uint8_t *cfg, const uint8_t *cnt, const uint8_t *inf, const uint32_t *vbase, const uint32_t *qbase,
+        uint64_t n_cells, float *verts, const uint32_t *quads, const DeviceTables *__restrict__ tabp)
+{
+    const DeviceTables &tab = *tabp;
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n_cells; c += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t b = cnt[c];
+        if (!((b >> 4) & 3u)) continue;
+        uint32_t x, y, z;
+        cell_xyz(c, cells, x, y, z);
+        const uint32_t cf = cfg[c], info = inf[c];
+        const uint32_t niso = nvert_of(tab, cf, (b & 0x80u) != 0);
+        const float x1 = ijk_to_xyz(x + 1, cells.x, rng.x, mn.x);
+        const float y1 = ijk_to_xyz(y + 1, cells.y, rng.y, mn.y);
+        const float z1 = ijk_to_xyz(z + 1, cells.z, rng.z, mn.z);
+        uint64_t q = qbase[c];
+        for (int s = 0; s < 3; ++s) {
+            if (!(info & (1u << s)) || !owned_quad_in_volume(s, x, y, z, cells) || !owned_sign_change(cf, s)) continue;
+            const uint4 r4 = reinterpret_cast<const uint4 *>(quads)[q++];
+            const uint32_t ring[4] = {r4.x, r4.y, r4.z, r4.w};
+            float nv[3];
+            if (smooth_edge(verts, ring, s, s == 2 ? y1 : x1, s == 0 ? y1 : z1, nv)) {
+                const uint64_t ev = (uint64_t)vbase[c] + niso + __popc(info & ((1u << s) - 1u));
+                verts[3 * ev + 0] = nv[0]; verts[3 * ev + 1] = nv[1]; verts[3 * ev + 2] = nv[2];
+            }
+        }
+    }
+}
+
+// owner-edge slot (0: edge 6, 1: 9, 2: 10) of each cell edge, 2 bits per edge
+constexpr uint32_t kOwnerSlot = 0x660066u;   // edges 0..11: 2,1,2,1,0,0,0,0,2,1,2,1
+
+__global__ void __launch_bounds__(kSimpleThreads) simple_smooth_duals(uint3 cells, const uint8_t *cfg,
+        const uint8_t *cnt, const uint8_t *inf, const uint32_t *vbase, uint64_t n_cells, float *verts,
+        const DeviceTables *__restrict__ tabp)
+{
+    const DeviceTables &tab = *tabp;
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n_cells; c += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t b = cnt[c];
+        if (!b) continue;
+        uint32_t x, y, z;
+        cell_xyz(c, cells, x, y, z);
+        const uint32_t cf = cfg[c];
+        const bool l2 = (b & 0x80u) != 0;
+        const uint32_t niso = nvert_of(tab, cf, l2);
+        float3 acc[4];
+        uint32_t n4[4] = {0, 0, 0, 0};
+        acc[0] = acc[1] = acc[2] = acc[3] = make_float3(0.f, 0.f, 0.f);
+#pragma unroll 1
+        for (int e = 0; e < 12; ++e) {
+            const uint32_t m = lut_m(tab, cf, l2, e);
+            if (m == 0xffu) continue;
+            if ((owner_dx(e) < 0 && x == 0) || (owner_dy(e) < 0 && y == 0) || (owner_dz(e) < 0 && z == 0)) continue;
+            const uint64_t o = ((uint64_t)(z + owner_dz(e)) * cells.y + (y + owner_dy(e))) * cells.x + (x + owner_dx(e));
+            const uint32_t slot = (kOwnerSlot >> (2 * e)) & 3u;
+            const uint64_t ev = (uint64_t)vbase[o] + nvert_of(tab, cfg[o], (cnt[o] & 0x80u) != 0) +
+                                __popc(inf[o] & ((1u << slot) - 1u));
+            const float3 src = make_float3(verts[3 * ev], verts[3 * ev + 1], verts[3 * ev + 2]);
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (m == (uint32_t)k) { acc[k] = n4[k] ? add3(acc[k], src) : src; n4[k]++; }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if ((uint32_t)k < niso && n4[k]) store3(verts + 3 * ((uint64_t)vbase[c] + k), div3(acc[k], n4[k]));
+    }
+}
+
+// ---------------------------------------------------------------------------
 // host side
 
 static int grid_for(uint64_t n, int threads, int num_sms)
@@ -224,6 +408,7 @@ static dmc_status simple_run_t(Ctx *ctx, const T *vol, const ExtractArgs &a, cud
     auto carve = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~(size_t)255; return o; };
     size_t o_cfg = carve(C), o_cnt = carve(C), o_vb = carve(4 * C), o_qb = carve(4 * C);
     size_t o_tiles = carve(sizeof(TileState) * n_tiles);
+    const size_t o_inf = a.num_smooth ? carve(C) : 0;
     dmc_status s = ctx_reserve_scratch(ctx, off);
     if (s != DMC_OK) return s;
     uint8_t *base = (uint8_t *)ctx->scratch;
@@ -256,6 +441,16 @@ static dmc_status simple_run_t(Ctx *ctx, const T *vol, const ExtractArgs &a, cud
     simple_emit<T><<<g, kSimpleThreads, 0, st>>>(vol, a.pts, a.cells, a.iso, a.mn, a.rng, cfg, cnt, vb, qb, C,
                                                   a.verts, a.vcap, a.quads, a.qcap, a.tris, &ctx->d_ctl->err, ctx->d_tab);
     CUDA_TRY(cudaGetLastError());
+    if (a.num_smooth) {
+        uint8_t *inf = base + o_inf;
+        simple_info<T><<<g, kSimpleThreads, 0, st>>>(vol, a.pts, a.cells, a.iso, cnt, inf, C);
+        for (uint32_t it = 0; it < a.num_smooth; ++it) {
+            simple_smooth_edges<<<g, kSimpleThreads, 0, st>>>(a.cells, a.mn, a.rng, cfg, cnt, inf, vb, qb, C, a.verts,
+                                                               a.quads, ctx->d_tab);
+            simple_smooth_duals<<<g, kSimpleThreads, 0, st>>>(a.cells, cfg, cnt, inf, vb, C, a.verts, ctx->d_tab);
+        }
+        CUDA_TRY(cudaGetLastError());
+    }
     return DMC_OK;
 }
 

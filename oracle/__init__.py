@@ -38,6 +38,10 @@ def lib():
         L.oracle_dmc.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_uint32),
                                  ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
                                  ctypes.c_float, ctypes.c_int, ctypes.POINTER(_Mesh)]
+        L.oracle_dmc_ex.restype = ctypes.c_int
+        L.oracle_dmc_ex.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_uint32),
+                                    ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                                    ctypes.c_float, ctypes.c_int, ctypes.c_uint32, ctypes.POINTER(_Mesh)]
         L.oracle_free.argtypes = [ctypes.POINTER(_Mesh)]
         L.oracle_free.restype = None
         L.oracle_tables_sha256.restype = ctypes.c_char_p
@@ -55,7 +59,7 @@ def set_threads(n):
     lib().oracle_set_threads(int(n))
 
 
-def extract(volume, xyz_min=None, xyz_max=None, iso=0.0, precision=0):
+def extract(volume, xyz_min=None, xyz_max=None, iso=0.0, precision=0, num_smooth=0):
     """Run the oracle on ``volume`` (numpy array indexed [z, y, x], float32 or uint16).
 
     ``xyz_min``/``xyz_max`` default to 0 and dims-1 (unit spacing).  Returns a dict
@@ -78,7 +82,8 @@ def extract(volume, xyz_min=None, xyz_max=None, iso=0.0, precision=0):
     mn = (ctypes.c_float * 3)(*[float(v) for v in xyz_min])
     mx = (ctypes.c_float * 3)(*[float(v) for v in xyz_max])
     m = _Mesh()
-    rc = lib().oracle_dmc(vol.ctypes.data, dtype, dims, mn, mx, ctypes.c_float(iso), int(precision), ctypes.byref(m))
+    rc = lib().oracle_dmc_ex(vol.ctypes.data, dtype, dims, mn, mx, ctypes.c_float(iso), int(precision),
+                             int(num_smooth), ctypes.byref(m))
     if rc != 0:
         raise RuntimeError("oracle_dmc failed with code %d" % rc)
     try:

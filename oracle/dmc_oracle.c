@@ -227,14 +227,123 @@ void oracle_set_threads(int n)
 #endif
 }
 
+/* ---- vertex smoothing (dmc.cu:1710-1981, driven at 2157-2169) ----------
+ *
+ * One iteration moves the crossing of every owned edge that has a quad onto
+ * the split triangle of its ring of four dual vertices, projected along the
+ * edge's axis, then recomputes every dual vertex as the mean of its patch's
+ * (moved) crossings.  Arithmetic, shared bit for bit with the CUDA kernels:
+ * single precision without fused multiply-add, correctly rounded square root
+ * and division, the reference's operand order.  Two restatements of the
+ * reference's arithmetic (documented divergences): vector lengths are
+ * normalised with 1/sqrt (the reference uses the approximate rsqrtf), and the
+ * diagonal of a convex quadrilateral is chosen at the corner with the
+ * smallest cosine instead of the largest acosf angle (the same corner except
+ * where acosf rounds two cosines to one angle). */
+
+/* sign of the z component of (right - mid) x (left - mid) (dmc.cu:1742-1748) */
+static inline int cross_z_positive(const float l[2], const float m[2], const float r[2])
+{
+    float dx1 = r[0] - m[0], dy1 = r[1] - m[1];
+    float dx2 = l[0] - m[0], dy2 = l[1] - m[1];
+    float a = dx1 * dy2, b = dx2 * dy1;
+    return (a - b) >= 0.0f;
+}
+
+/* cosine of the angle at m between m->l and m->r (calc_radian without acosf, dmc.cu:1833-1843) */
+static inline float corner_cos(const float l[2], const float m[2], const float r[2])
+{
+    float ux = l[0] - m[0], uy = l[1] - m[1], vx = r[0] - m[0], vy = r[1] - m[1];
+    float iu = 1.0f / sqrtf(ux * ux + uy * uy), iv = 1.0f / sqrtf(vx * vx + vy * vy);
+    ux = ux * iu; uy = uy * iu; vx = vx * iv; vy = vy * iv;
+    return ux * vx + uy * vy;
+}
+
+/* is_inside_triangle (dmc.cu:1894-1912): barycentric (alpha, beta, gamma) of pt */
+static inline int inside_triangle(const float p0[2], const float p1[2], const float p2[2], const float pt[2],
+                                  float *alpha, float *beta, float *gamma)
+{
+    float v0x = p1[0] - p0[0], v0y = p1[1] - p0[1];
+    float v1x = p2[0] - p0[0], v1y = p2[1] - p0[1];
+    float v2x = pt[0] - p0[0], v2y = pt[1] - p0[1];
+    float d00 = v0x * v0x + v0y * v0y;
+    float d10 = v1x * v0x + v1y * v0y;
+    float d11 = v1x * v1x + v1y * v1y;
+    float d20 = v2x * v0x + v2y * v0y;
+    float d21 = v2x * v1x + v2y * v1y;
+    float denom = d00 * d11 - d10 * d10;
+    float inv = 1.0f / denom;
+    *beta = (d11 * d20 - d10 * d21) * inv;
+    *gamma = (d00 * d21 - d10 * d20) * inv;
+    *alpha = 1.0f - *beta - *gamma;
+    float bg = *beta + *gamma;
+    return (-1e-4 < (double)*beta) && (-1e-4 < (double)*gamma) && ((double)bg < 1.0 + 1e-4);
+}
+
+/* smooth_edge_vertices for one owned edge (axis s: 0 = edge 6, 1 = 9, 2 = 10)
+ * whose quad ring holds dual vertices ring[0..3]; origin is the edge's
+ * position in the projection plane.  Returns 1 and the new crossing in out
+ * when it moves. */
+static int smooth_edge(const float *vt, const uint32_t ring[4], int s, const float origin[2], float out[3])
+{
+    const int ax = s == 2 ? 1 : 0, ay = s == 0 ? 1 : 2;     /* 6: xy, 9: xz, 10: yz */
+    float P[4][2];
+    for (int i = 0; i < 4; ++i) { P[i][0] = vt[3 * (uint64_t)ring[i] + ax]; P[i][1] = vt[3 * (uint64_t)ring[i] + ay]; }
+    int npos = 0, nneg = 0, ipos = 0, ineg = 0;
+    for (int i = 0; i < 4; ++i) {
+        if (cross_z_positive(P[(i + 3) & 3], P[i], P[(i + 1) & 3])) { npos++; ipos = i; }
+        else { nneg++; ineg = i; }
+    }
+    if (npos == nneg) return 0;                              /* complex quadrilateral */
+    int split0;
+    if (npos == 0 || nneg == 0) {                             /* convex: corner with the widest angle */
+        float best = corner_cos(P[3], P[0], P[1]);
+        split0 = 0;
+        for (int i = 1; i < 4; ++i) {
+            float c = corner_cos(P[(i + 3) & 3], P[i], P[(i + 1) & 3]);
+            if (c < best) { best = c; split0 = i; }
+        }
+    } else {
+        split0 = npos < nneg ? ipos : ineg;                  /* the concave corner */
+    }
+    int split1 = (split0 + 2) & 3;
+    float al, be, ga;
+    int a, b, c;
+    if (inside_triangle(P[split0], P[(split0 + 1) & 3], P[split1], origin, &al, &be, &ga)) {
+        a = split0; b = (split0 + 1) & 3; c = split1;
+    } else if (inside_triangle(P[split1], P[(split1 + 1) & 3], P[split0], origin, &al, &be, &ga)) {
+        a = split1; b = (split1 + 1) & 3; c = split0;
+    } else {
+        return 0;
+    }
+    for (int k = 0; k < 3; ++k) {
+        float t = al * vt[3 * (uint64_t)ring[a] + k];
+        t = t + be * vt[3 * (uint64_t)ring[b] + k];
+        t = t + ga * vt[3 * (uint64_t)ring[c] + k];
+        out[k] = t;
+    }
+    return 1;
+}
+
+int oracle_dmc_ex(const void *vol, int dtype, const uint32_t dims[3], const float xyz_min[3],
+                  const float xyz_max[3], float iso, int precision, uint32_t num_smooth, oracle_mesh *out);
+
 /* Returns 0 on success, 1 bad argument, 2 out of memory, 3 more than 2^32-1
  * vertices (the reference indexes vertices with 32-bit integers). */
 int oracle_dmc(const void *vol, int dtype, const uint32_t dims[3],
                const float xyz_min[3], const float xyz_max[3], float iso,
                int precision, oracle_mesh *out)
 {
+    return oracle_dmc_ex(vol, dtype, dims, xyz_min, xyz_max, iso, precision, 0, out);
+}
+
+/* oracle_dmc with num_smooth smoothing iterations (FP32 replica only). */
+int oracle_dmc_ex(const void *vol, int dtype, const uint32_t dims[3], const float xyz_min[3],
+                  const float xyz_max[3], float iso, int precision, uint32_t num_smooth, oracle_mesh *out)
+{
     memset(out, 0, sizeof(*out));
     if (!vol || (dtype != 0 && dtype != 1) || (precision != 0 && precision != 1)) return 1;
+    if (precision == 1 && num_smooth) return 1;
     grid g;
     g.vol = vol; g.dtype = dtype;
     g.nx = dims[0]; g.ny = dims[1];
@@ -521,6 +630,67 @@ int oracle_dmc(const void *vol, int dtype, const uint32_t dims[3],
                 qd[4 * q + it] = rr->vertex_begin + lut_m(rr, re);
             }
             ++q;
+        }
+    }
+
+    /* step 8: smoothing iterations (dmc.cu:2157-2169) */
+    float *vt = out->vertices;
+    for (uint32_t it = 0; it < num_smooth; ++it) {
+        /* smooth_edge_vertices: reads dual vertices, writes crossings */
+        #pragma omp parallel for schedule(static)
+        for (int64_t a = 0; a < (int64_t)A; ++a) {
+            const cell_rec *r = &rec[a];
+            uint64_t i1 = r->index1d;
+            uint64_t x = i1 % g.cx, y = (i1 / g.cx) % g.cy, z = i1 / (g.cx * g.cy);
+            uint64_t q = qoff[a];
+            static const int P0[3] = {2, 5, 7};
+            static const int EDGE[3] = {6, 9, 10};
+            for (int s = 0; s < 3; ++s) {
+                if (!((r->info >> s) & 1u)) continue;
+                int exceed = s == 0 ? (x + 1 >= g.cx || y + 1 >= g.cy)
+                           : s == 1 ? (x + 1 >= g.cx || z + 1 >= g.cz)
+                                    : (y + 1 >= g.cy || z + 1 >= g.cz);
+                if (exceed) continue;
+                if (((r->config >> P0[s]) & 1u) == ((r->config >> 6) & 1u)) continue;
+                const float x1 = ijk_to_xyz(x + 1, csz[0], rng[0], xyz_min[0]);
+                const float y1 = ijk_to_xyz(y + 1, csz[1], rng[1], xyz_min[1]);
+                const float z1 = ijk_to_xyz(z + 1, csz[2], rng[2], xyz_min[2]);
+                const float origin[2] = {s == 2 ? y1 : x1, s == 0 ? y1 : z1};
+                float nv3[3];
+                if (smooth_edge(vt, &qd[4 * q], s, origin, nv3)) {
+                    float *dst = &vt[3 * (uint64_t)edge_vertex_index(r, EDGE[s])];
+                    dst[0] = nv3[0]; dst[1] = nv3[1]; dst[2] = nv3[2];
+                }
+                ++q;
+            }
+        }
+        /* calc_iso_vertices_kern: dual vertices from the current crossings;
+         * a patch without an owner inside the volume keeps its position */
+        #pragma omp parallel for schedule(static)
+        for (int64_t a = 0; a < (int64_t)A; ++a) {
+            cell_rec *r = &rec[a];
+            uint64_t i1 = r->index1d;
+            int64_t x = (int64_t)(i1 % g.cx), y = (int64_t)((i1 / g.cx) % g.cy), z = (int64_t)(i1 / (g.cx * g.cy));
+            uint8_t cnt[4] = {0, 0, 0, 0};
+            float acc[4][3];
+            for (int e = 0; e < 12; ++e) {
+                uint8_t m = lut_m(r, e);
+                if (m == 0xff) continue;
+                int64_t ox = x + OWNER_OFF[e][0], oy = y + OWNER_OFF[e][1], oz = z + OWNER_OFF[e][2];
+                if (ox < 0 || oy < 0 || oz < 0) continue;
+                uint64_t oi = ((uint64_t)oz * g.cy + (uint64_t)oy) * g.cx + (uint64_t)ox;
+                const float *src = &vt[3 * (uint64_t)edge_vertex_index(&rec[map[oi]], OWNER_EDGE[e])];
+                if (cnt[m] == 0) { acc[m][0] = src[0]; acc[m][1] = src[1]; acc[m][2] = src[2]; }
+                else { acc[m][0] = acc[m][0] + src[0]; acc[m][1] = acc[m][1] + src[1]; acc[m][2] = acc[m][2] + src[2]; }
+                cnt[m]++;
+            }
+            uint8_t niso = (uint8_t)(r->nv - ((r->info & 1u) + ((r->info >> 1) & 1u) + ((r->info >> 2) & 1u)));
+            for (uint8_t m = 0; m < niso; ++m) {
+                if (!cnt[m]) continue;
+                float d = (float)cnt[m];
+                float *dst = &vt[3 * ((uint64_t)r->vertex_begin + m)];
+                dst[0] = acc[m][0] / d; dst[1] = acc[m][1] / d; dst[2] = acc[m][2] / d;
+            }
         }
     }
     free(qoff); free(map); free(cfg); free(rec);

@@ -21,7 +21,7 @@ RING = {6: [6, 7, 4, 5], 9: [9, 1, 3, 11], 10: [10, 8, 0, 2]}
 F = np.float32
 
 
-def extract(vol, iso, xyz_min=(0, 0, 0), xyz_max=None):
+def extract(vol, iso, xyz_min=(0, 0, 0), xyz_max=None, num_smooth=0):
     vol = np.asarray(vol)
     nz, ny, nx = vol.shape
     cx, cy, cz = nx - 1, ny - 1, nz - 1
@@ -133,6 +133,7 @@ def extract(vol, iso, xyz_min=(0, 0, 0), xyz_max=None):
                 s, n = acc[m]
                 verts[r["vb"] + m] = [F(s[c] / F(n)) for c in range(3)]
     quads = []
+    quad_edge = []                      # (owner key, axis slot) of each quad
     for key in order:
         x, y, z = key
         r = active[key]
@@ -155,5 +156,98 @@ def extract(vol, iso, xyz_min=(0, 0, 0), xyz_max=None):
                 rr = active[rc]
                 q.append(rr["vb"] + lut(rr, re))
             quads.append(q)
+            quad_edge.append((key, s))
+    for _ in range(num_smooth):
+        _smooth_iteration(verts, quads, quad_edge, active, order, lut, edge_vertex, coord)
     V = np.array([v if v is not None else [np.nan] * 3 for v in verts], dtype=np.float32).reshape(-1, 3)
     return V, np.array(quads, dtype=np.uint32).reshape(-1, 4)
+
+
+# ---- smoothing (dmc.cu:1710-1981): the arithmetic of oracle/dmc_oracle.c ----
+
+def _cross_pos(l, m, r):
+    dx1, dy1 = F(r[0] - m[0]), F(r[1] - m[1])
+    dx2, dy2 = F(l[0] - m[0]), F(l[1] - m[1])
+    return F(F(dx1 * dy2) - F(dx2 * dy1)) >= 0
+
+
+def _corner_cos(l, m, r):
+    ux, uy, vx, vy = F(l[0] - m[0]), F(l[1] - m[1]), F(r[0] - m[0]), F(r[1] - m[1])
+    iu = F(F(1) / np.sqrt(F(F(ux * ux) + F(uy * uy))))
+    iv = F(F(1) / np.sqrt(F(F(vx * vx) + F(vy * vy))))
+    ux, uy, vx, vy = F(ux * iu), F(uy * iu), F(vx * iv), F(vy * iv)
+    return F(F(ux * vx) + F(uy * vy))
+
+
+def _inside(p0, p1, p2, pt):
+    v0x, v0y = F(p1[0] - p0[0]), F(p1[1] - p0[1])
+    v1x, v1y = F(p2[0] - p0[0]), F(p2[1] - p0[1])
+    v2x, v2y = F(pt[0] - p0[0]), F(pt[1] - p0[1])
+    d00 = F(F(v0x * v0x) + F(v0y * v0y))
+    d10 = F(F(v1x * v0x) + F(v1y * v0y))
+    d11 = F(F(v1x * v1x) + F(v1y * v1y))
+    d20 = F(F(v2x * v0x) + F(v2y * v0y))
+    d21 = F(F(v2x * v1x) + F(v2y * v1y))
+    inv = F(F(1) / F(F(d00 * d11) - F(d10 * d10)))
+    beta = F(F(F(d11 * d20) - F(d10 * d21)) * inv)
+    gamma = F(F(F(d00 * d21) - F(d10 * d20)) * inv)
+    alpha = F(F(F(1) - beta) - gamma)
+    ok = float(beta) > -1e-4 and float(gamma) > -1e-4 and float(F(beta + gamma)) < 1.0 + 1e-4
+    return ok, (alpha, beta, gamma)
+
+
+def _smooth_iteration(verts, quads, quad_edge, active, order, lut, edge_vertex, coord):
+    with np.errstate(all="ignore"):
+        moved = []
+        for q, (key, s) in zip(quads, quad_edge):
+            ax, ay = (1 if s == 2 else 0), (1 if s == 0 else 2)
+            P = [(verts[i][ax], verts[i][ay]) for i in q]
+            pos = [_cross_pos(P[(i + 3) % 4], P[i], P[(i + 1) % 4]) for i in range(4)]
+            npos = sum(pos)
+            if npos == 2:
+                continue
+            if npos in (0, 4):
+                cs = [_corner_cos(P[(i + 3) % 4], P[i], P[(i + 1) % 4]) for i in range(4)]
+                split0 = 0
+                for i in range(1, 4):
+                    if cs[i] < cs[split0]:
+                        split0 = i
+            else:
+                split0 = [i for i in range(4) if pos[i] == (npos == 1)][-1]
+            split1 = (split0 + 2) % 4
+            x, y, z = key
+            x1, y1, z1 = coord(x + 1, 0), coord(y + 1, 1), coord(z + 1, 2)
+            origin = (y1 if s == 2 else x1, y1 if s == 0 else z1)
+            ok, w = _inside(P[split0], P[(split0 + 1) % 4], P[split1], origin)
+            abc = (split0, (split0 + 1) % 4, split1)
+            if not ok:
+                ok, w = _inside(P[split1], P[(split1 + 1) % 4], P[split0], origin)
+                abc = (split1, (split1 + 1) % 4, split0)
+            if not ok:
+                continue
+            va, vb, vc = verts[q[abc[0]]], verts[q[abc[1]]], verts[q[abc[2]]]
+            nv = [F(F(F(w[0] * va[k]) + F(w[1] * vb[k])) + F(w[2] * vc[k])) for k in range(3)]
+            moved.append((edge_vertex(active[key], (6, 9, 10)[s]), nv))
+        for i, nv in moved:
+            verts[i] = nv
+        for key in order:
+            x, y, z = key
+            r = active[key]
+            acc = {}
+            for e in range(12):
+                m = lut(r, e)
+                if m == 255:
+                    continue
+                off, oe = OWNER[e]
+                o = (x + off[0], y + off[1], z + off[2])
+                if min(o) < 0:
+                    continue
+                src = verts[edge_vertex(active[o], oe)]
+                if m not in acc:
+                    acc[m] = [list(src), 1]
+                else:
+                    acc[m][0] = [F(acc[m][0][c] + src[c]) for c in range(3)]
+                    acc[m][1] += 1
+            for m, (sm, n) in acc.items():
+                if m < r["niso"]:
+                    verts[r["vb"] + m] = [F(sm[c] / F(n)) for c in range(3)]

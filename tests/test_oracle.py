@@ -126,3 +126,50 @@ def test_empty_and_degenerate_volumes():
     assert len(oracle.extract(np.ones((4, 4, 4), np.float32), iso=0.5)["vertices"]) == 0
     r = oracle.extract(np.zeros((2, 2, 2), np.float32), iso=0.0)   # all samples == iso: config 0
     assert len(r["vertices"]) == 0 and r["n_iso_samples"] == 8
+
+
+# ---- smoothing (dmc.cu:1710-1981) ------------------------------------------
+
+def _reference_sphere(n=21):
+    """The reference's own usage example (dmc.cu:2248-2306): |p| on a 21^3 grid over [-5, 5]^3."""
+    x = np.array([np.float32(i) / np.float32(n - 1) * np.float32(10.0) + np.float32(-5.0) for i in range(n)], np.float32)
+    z, y, xx = np.meshgrid(x, x, x, indexing="ij")
+    return np.sqrt(xx * xx + y * y + z * z).astype(np.float32)
+
+
+@pytest.mark.parametrize("num_smooth", [1, 2, 15])
+def test_smoothing_oracle_matches_refpy_on_reference_example(num_smooth):
+    vol = _reference_sphere()
+    V, Q = refpy.extract(vol, 4.1, (-5, -5, -5), (5, 5, 5), num_smooth=num_smooth)
+    o = oracle.extract(vol, (-5, -5, -5), (5, 5, 5), 4.1, num_smooth=num_smooth)
+    assert np.array_equal(Q, o["quads"])
+    assert np.array_equal(np.nan_to_num(V).view(np.uint32), np.nan_to_num(o["vertices"]).view(np.uint32))
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_smoothing_oracle_matches_refpy_random(seed):
+    rng = np.random.default_rng(300 + seed)
+    shape = tuple(int(s) for s in rng.integers(4, 9, 3))
+    if seed == 2:
+        vol, iso = rng.integers(0, 4, shape).astype(np.uint16), 1.5
+    else:
+        vol, iso = rng.normal(size=shape).astype(np.float32), float(rng.normal() * 0.2)
+    V, Q = refpy.extract(vol, iso, (0, 0, 0), None, num_smooth=3)
+    o = oracle.extract(vol, iso=iso, num_smooth=3)
+    assert np.array_equal(Q, o["quads"])
+    ok = ~np.isnan(V).any(1)  # refpy leaves the reference-undefined vertices as NaN
+    assert V.shape == o["vertices"].shape and ok.mean() > 0.5
+    assert _bits_equal(V[ok], o["vertices"][ok])
+
+
+def test_smoothing_keeps_topology_and_moves_vertices():
+    vol = _reference_sphere()
+    a = oracle.extract(vol, (-5, -5, -5), (5, 5, 5), 4.1)
+    b = oracle.extract(vol, (-5, -5, -5), (5, 5, 5), 4.1, num_smooth=5)
+    assert np.array_equal(a["quads"], b["quads"])
+    assert a["vertices"].shape == b["vertices"].shape
+    moved = np.any(a["vertices"] != b["vertices"], axis=1)
+    assert moved.mean() > 0.5
+    # smoothed vertices stay near the surface (radius 4.1, cell size 0.5)
+    r = np.linalg.norm(b["vertices"], axis=1)
+    assert np.all(np.abs(r - 4.1) < 0.5)
