@@ -108,7 +108,11 @@ dmc_status dmc_set_algo(dmc_ctx *ctx, dmc_algo algo);
  * HOST memory.  Copies the volume to the device, extracts, and returns the
  * mesh in host memory allocated by the library (triangles only when
  * want_triangles != 0).  num_smooth > 0 runs the reference's vertex smoothing
- * (dmc.cu:1914-1981) that many times. */
+ * (dmc.cu:1914-1981, 2157-2169) that many times: each iteration moves the
+ * crossing of every owned edge with a quad onto the split triangle of its
+ * projected ring of dual vertices, then recomputes the dual vertices.  It
+ * runs on the simple kernel family (the only one that keeps per-cell
+ * offsets); with DMC_ALGO_BRICK selected it returns DMC_ERR_UNSUPPORTED. */
 dmc_status dmc_run(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min[3], const float xyz_max[3],
                    float iso, uint32_t num_smooth, int want_triangles, dmc_mesh *out);
 
@@ -121,8 +125,10 @@ void dmc_mesh_free(dmc_mesh *mesh);
  * vertices / quads).  d_triangles may be NULL.  On DMC_ERR_OUTPUT_OVERFLOW the
  * counts are still reported in *n_vertices / *n_quads so the caller can
  * retry.  With all three output pointers NULL the call only counts: it
- * returns DMC_OK with the totals and writes no mesh.  `stream` is a cudaStream_t (NULL: the context's stream).  The call
- * returns after the mesh is complete. */
+ * returns DMC_OK with the totals and writes no mesh.  num_smooth > 0 smooths
+ * as dmc_run does and needs d_quads along with d_vertices.  `stream` is a
+ * cudaStream_t (NULL: the context's stream).  The call returns after the mesh
+ * is complete. */
 dmc_status dmc_extract_device(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min[3], const float xyz_max[3],
                               float iso, uint32_t num_smooth,
                               float *d_vertices, uint64_t vertex_capacity,
