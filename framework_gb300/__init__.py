@@ -37,7 +37,7 @@ ABI_SYMBOLS = [
     "dmc_set_algo", "dmc_run", "dmc_mesh_free", "dmc_extract_device", "dmc_get_stats",
     "dmc_extract_batch", "dmc_batch_wait", "dmc_set_option", "dmc_extract_device_noalloc",
     "dmc_server_create", "dmc_server_destroy", "dmc_server_add_volume", "dmc_server_submit", "dmc_server_wait",
-    "dmc_server_release", "dmc_server_get_stats", "dmc_server_replay", "dmc_write_obj",
+    "dmc_server_release", "dmc_server_get_stats", "dmc_server_replay", "dmc_write_obj", "dmc_compact_mesh",
 ]
 BATCH_ASYNC, BATCH_GRAPH = 0x1, 0x2
 OPT_BRICK_PLANES = 1
@@ -140,6 +140,8 @@ def load_library(build_if_missing=True):
                                     ctypes.c_void_p]
     L.dmc_batch_wait.argtypes = [ctypes.c_void_p, P(_BatchResult), P(ctypes.c_uint64), P(ctypes.c_uint64)]
     L.dmc_set_option.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int64]
+    L.dmc_compact_mesh.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
+                                   ctypes.c_void_p, ctypes.c_void_p, P(ctypes.c_uint64), ctypes.c_void_p]
     L.dmc_write_obj.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
                                 ctypes.c_uint32]
     L.dmc_server_create.argtypes = [P(_ServerConfig), P(ctypes.c_void_p)]
@@ -316,6 +318,22 @@ class Extractor:
             e.counts = (int(nv.value), int(nq.value))
             raise e
         return int(nv.value), int(nq.value)
+
+    def compact_mesh(self, vertices, quads, triangles=None, out_vertices=None, stream=None):
+        """``dmc_compact_mesh``: keep only the vertices the quads reference.
+
+        ``vertices`` (CUDA float32 [V,3]) is read; ``quads`` (CUDA int32 [Q,4])
+        and ``triangles`` ([2Q,3]) are renumbered in place.  Returns the kept
+        vertices as a view of ``out_vertices`` (allocated when not given)."""
+        import torch
+        if out_vertices is None:
+            out_vertices = torch.empty_like(vertices)
+        n = ctypes.c_uint64()
+        _check(self._lib.dmc_compact_mesh(self._h, vertices.data_ptr(), vertices.shape[0], quads.data_ptr(),
+                                          quads.shape[0], triangles.data_ptr() if triangles is not None else None,
+                                          out_vertices.data_ptr(), ctypes.byref(n), _stream_handle(stream)),
+               "dmc_compact_mesh")
+        return out_vertices[:int(n.value)]
 
     def set_option(self, option, value):
         """``dmc_set_option``: e.g. ``set_option(OPT_BRICK_PLANES, 16)``; 0 restores the automatic choice."""

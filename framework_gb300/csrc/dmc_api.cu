@@ -72,6 +72,10 @@ struct dmc_ctx {
     OutBufs out;
 };
 
+namespace dmc {
+Ctx *ctx_of(dmc_ctx *ctx) { return &ctx->c; }
+}
+
 static bool valid_volume(const dmc_volume *vol)
 {
     if (!vol || !vol->data) return false;

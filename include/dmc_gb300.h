@@ -144,6 +144,18 @@ dmc_status dmc_extract_device(dmc_ctx *ctx, const dmc_volume *vol, const float x
 dmc_status dmc_write_obj(const char *path, const float *vertices, uint64_t n_vertices,
                          const uint32_t *faces, uint64_t n_faces, uint32_t verts_per_face);
 
+/* Opt-in post-processing (no reference counterpart; the result no longer
+ * has the reference's vertex numbering): drops every vertex no quad
+ * references -- all edge crossings, which only serve to place the dual
+ * vertices, and any unreferenced dual vertex -- keeping the others in order.
+ * Kept vertices go to d_out_vertices (device, room for n_vertices, must not
+ * overlap d_vertices); d_quads (4 per quad) and, if not NULL, d_triangles (6
+ * per quad) are renumbered in place.  *n_out_vertices receives the count.
+ * Out-of-range indices give DMC_ERR_DEVICE_CHECK. */
+dmc_status dmc_compact_mesh(dmc_ctx *ctx, const float *d_vertices, uint64_t n_vertices,
+                            uint32_t *d_quads, uint64_t n_quads, uint32_t *d_triangles,
+                            float *d_out_vertices, uint64_t *n_out_vertices, void *stream);
+
 /* Counters of the last call on this context (for a batch: summed over its
  * volumes). */
 dmc_status dmc_get_stats(const dmc_ctx *ctx, dmc_stats *stats);
