@@ -111,6 +111,20 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(rows)}
 
 
+def combine_ranks(ms, units, dist, device):
+    """Whole-job figures when every rank processed its own `units` in `ms`
+    (independent volumes, weak scaling): the slowest rank's time and the
+    units of all ranks.  Without a process group, the rank's own."""
+    if dist is None:
+        return ms, units
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(u.item())
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -238,7 +252,7 @@ def batch_cpu_sample(vols, target_s=10.0):
     return done / t_used, cores, "first %d of %d volumes (%.1f s)" % (done, len(vols), t_used)
 
 
-def run_batch(args, rank, world):
+def run_batch(args, rank, world, dist=None):
     """Batched extraction of the uneven gyroid mix: graph-launched pipeline
     (vol/s) against one plain extraction call per volume."""
     import torch
@@ -267,7 +281,7 @@ def run_batch(args, rank, world):
         nv, nq, _r = ex.batch_wait()
     ev1.record(stream)
     torch.cuda.synchronize()
-    ms = ev0.elapsed_time(ev1) / args.steps
+    ms, total_vols = combine_ranks(ev0.elapsed_time(ev1) / args.steps, n, dist, "cuda")
     clk = clocks.stop()
     assert (nv, nq) == (V, Q)
     # per-kernel split from one synchronous call
@@ -303,7 +317,7 @@ def run_batch(args, rank, world):
     if rank == 0:
         hbm, peak_kind = peaks()
         alg_bytes = 4 * N + 12 * V + 16 * Q
-        value = n * world / (ms * 1e-3)
+        value = total_vols / (ms * 1e-3)
         achieved = alg_bytes / (st["emit_ms"] * 1e-3) / 1e9 if st["emit_ms"] > 0 else None
         cpu = None
         if not args.no_cpu_baseline:
@@ -493,7 +507,7 @@ def run_served_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
-def run_served(args, rank, world):
+def run_served(args, rank, world, dist=None):
     import numpy as np
     import torch
     import framework_gb300 as fg
@@ -504,6 +518,8 @@ def run_served(args, rank, world):
     clocks.start()
     m = served_measure(vols, n_req=max(200, 60 * args.steps))
     clk = clocks.stop()
+    # every rank serves its own request stream: whole-job capacity is the sum
+    _, total_rps = combine_ranks(0.0, m["served"]["capacity_rps"], dist, "cuda")
     # end to end: a burst of requests, each mesh copied to host memory and released
     vid, iso, _ = request_trace(vols, 128, 0, seed=4)
     d2h = 0
@@ -528,7 +544,7 @@ def run_served(args, rank, world):
         v, cores, sample = served_cpu_sample(vols, 10.0)
         cpu = {"value": round(v, 3), "unit": "requests/s", "cores": cores, "kind": "port", "sample": sample}
     line = {
-        "metric": "requests/s", "value": m["served"]["capacity_rps"], "unit": "requests/s", "n_gpus": world,
+        "metric": "requests/s", "value": round(total_rps, 2), "unit": "requests/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 / m["served"]["capacity_rps"], 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+u16", "data": "synthetic",
         "config": {"workload": "served64", "desc": SERVED_DESC, "volumes": len(vols), "points": N,
@@ -582,7 +598,7 @@ def main():
 
     torch.cuda.set_device(local)
     if args.workload == "served64":
-        line = run_served(args, rank, world)
+        line = run_served(args, rank, world, dist)
         if line:
             print(json.dumps(line), flush=True)
         if dist:
@@ -590,7 +606,7 @@ def main():
             dist.destroy_process_group()
         return
     if args.workload == "batch256":
-        line = run_batch(args, rank, world)
+        line = run_batch(args, rank, world, dist)
         if line:
             print(json.dumps(line), flush=True)
         if dist:
@@ -627,11 +643,7 @@ def main():
     if dist:
         dist.barrier()
     clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms, total_points = combine_ranks(ev0.elapsed_time(ev1) / args.steps, N, dist, "cuda")
     st = ex.stats()
 
     # end to end through the host API: pinned host volume in, host mesh out
@@ -653,7 +665,7 @@ def main():
         alg_bytes = elem * N + 12 * V + 16 * Q
         emit_avg = sum(emit_ms) / len(emit_ms)
         achieved = alg_bytes / (emit_avg * 1e-3) / 1e9
-        value = N * world / (ms * 1e-3) / 1e9
+        value = total_points / (ms * 1e-3) / 1e9
         cpu = None
         if not args.no_cpu_baseline:
             v, cores, sample = cpu_oracle_sample(host, iso)
@@ -689,9 +701,9 @@ def main():
         sub = argparse.Namespace(**vars(args))
         sub.no_cpu_baseline = True
         sub.steps, sub.e2e_steps = min(args.steps, 10), 1
-        b = run_batch(sub, rank, world)
+        b = run_batch(sub, rank, world, dist)
         torch.cuda.empty_cache()
-        sv = run_served(sub, rank, world)
+        sv = run_served(sub, rank, world, dist)
         if line is not None:
             line["batched"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "e2e", "roofline")}
             line["batched"].update({k: b["config"][k] for k in ("volumes", "points", "plain_volumes_per_s",
