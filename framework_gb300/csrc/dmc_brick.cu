@@ -177,23 +177,24 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
         const uint32_t bytes = min((uint32_t)W, pts.x - x0) * (uint32_t)sizeof(T);
         for (uint32_t o = 0; o < bytes; o += 128) asm volatile("prefetch.global.L2 [%0];" ::"l"(nxt + o));
     }
-    bool cok[GROUPS];
-#pragma unroll
-    for (int j = 0; j < GROUPS; ++j) cok[j] = x0 + lane + 32 * j < pts.x;
-    const bool full = cok[GROUPS - 1] && nrow == 34;
-    // All 34 rows and 128 columns in range and rows aligned for 4-sample
-    // loads (warp-uniform): lane l takes the adjacent columns 4l..4l+3 of a
-    // row in one load.  Otherwise lane l takes columns l, l+32, l+64, l+96.
-    const bool vec = nrow == 34 && x0 + W <= pts.x && (pts.x & 3u) == 0 &&
+    // Rows past the volume (or past 34) and columns past it give 0 bits: the
+    // loads are predicated and the bits masked, so every brick takes the same
+    // batched path (8 rows of loads in flight) whatever its position.
+    const uint32_t rmask = nrow >= 32 ? 0xffffffffu : ((1u << nrow) - 1u);
+    const uint32_t hmask = nrow > 32 ? ((1u << (nrow - 32)) - 1u) : 0u;
+    // All 128 columns in range and rows aligned for 4-sample loads
+    // (warp-uniform): lane l takes the adjacent columns 4l..4l+3 of a row in
+    // one load.  Otherwise lane l takes columns l, l+32, l+64, l+96.
+    const bool vec = x0 + W <= pts.x && (pts.x & 3u) == 0 &&
                      (reinterpret_cast<uintptr_t>(vol) & (4 * sizeof(T) - 1)) == 0;
     if (vec) {
         const T *vb = vol + (plane0 + y0) * sx + x0 + 4 * lane;
         using V = decltype(load4(vb));
 #pragma unroll 1
-        for (int r0 = 0; r0 < 32; r0 += 8) {
+        for (uint32_t r0 = 0; r0 < 32; r0 += 8) {
             V v[8];
 #pragma unroll
-            for (int i = 0; i < 8; ++i) v[i] = load4(vb + (uint64_t)(r0 + i) * sx);
+            for (int i = 0; i < 8; ++i) v[i] = r0 + i < nrow ? load4(vb + (uint64_t)(r0 + i) * sx) : V{};
 #pragma unroll
             for (int i = 0; i < 8; ++i)
 #pragma unroll
@@ -205,7 +206,7 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
         }
 #pragma unroll
         for (int i = 0; i < 2; ++i) {
-            const V v = load4(vb + (uint64_t)(32 + i) * sx);
+            const V v = 32u + i < nrow ? load4(vb + (uint64_t)(32 + i) * sx) : V{};
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const T t = elem4(v, q);
@@ -215,56 +216,47 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
         }
         // columns 4l..4l+3: two 16-byte stores per mask
         uint4 *lt4 = reinterpret_cast<uint4 *>(&m.lt[4 * lane]), *le4 = reinterpret_cast<uint4 *>(&m.le[4 * lane]);
-        lt4[0] = make_uint4(lo[0], hi[0], lo[1], hi[1]);
-        lt4[1] = make_uint4(lo[2], hi[2], lo[3], hi[3]);
-        le4[0] = make_uint4(elo[0], ehi[0], elo[1], ehi[1]);
-        le4[1] = make_uint4(elo[2], ehi[2], elo[3], ehi[3]);
+        lt4[0] = make_uint4(lo[0] & rmask, hi[0] & hmask, lo[1] & rmask, hi[1] & hmask);
+        lt4[1] = make_uint4(lo[2] & rmask, hi[2] & hmask, lo[3] & rmask, hi[3] & hmask);
+        le4[0] = make_uint4(elo[0] & rmask, ehi[0] & hmask, elo[1] & rmask, ehi[1] & hmask);
+        le4[1] = make_uint4(elo[2] & rmask, ehi[2] & hmask, elo[3] & rmask, ehi[3] & hmask);
     } else {
         const T *base = vol + (plane0 + y0) * sx + x0 + lane;
-        if (full) {
+        bool cok[GROUPS];
+#pragma unroll
+        for (int j = 0; j < GROUPS; ++j) cok[j] = x0 + lane + 32 * j < pts.x;
 #pragma unroll 1
-            for (int r0 = 0; r0 < 32; r0 += 8) {
-                T v[8][GROUPS];
+        for (uint32_t r0 = 0; r0 < 32; r0 += 8) {
+            T v[8][GROUPS];
 #pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    const T *row = base + (uint64_t)(r0 + i) * sx;
+            for (int i = 0; i < 8; ++i) {
+                const T *row = base + (uint64_t)(r0 + i) * sx;
 #pragma unroll
-                    for (int j = 0; j < GROUPS; ++j) v[i][j] = raw_load(row + 32 * j);
-                }
-#pragma unroll
-                for (int i = 0; i < 8; ++i)
-#pragma unroll
-                    for (int j = 0; j < GROUPS; ++j) {
-                        lo[j] |= below(v[i][j], iso, thr) << (r0 + i);
-                        elo[j] |= at_or_below(v[i][j], iso, thr_le) << (r0 + i);
-                    }
+                for (int j = 0; j < GROUPS; ++j) v[i][j] = (r0 + i < nrow && cok[j]) ? raw_load(row + 32 * j) : T(0);
             }
 #pragma unroll
-            for (int i = 0; i < 2; ++i) {
-                const T *row = base + (uint64_t)(32 + i) * sx;
+            for (int i = 0; i < 8; ++i)
 #pragma unroll
                 for (int j = 0; j < GROUPS; ++j) {
-                    const T v = raw_load(row + 32 * j);
-                    hi[j] |= below(v, iso, thr) << i;
-                    ehi[j] |= at_or_below(v, iso, thr_le) << i;
+                    lo[j] |= below(v[i][j], iso, thr) << (r0 + i);
+                    elo[j] |= at_or_below(v[i][j], iso, thr_le) << (r0 + i);
                 }
-            }
-        } else {
-            for (uint32_t r = 0; r < nrow; ++r) {
-                const T *row = base + (uint64_t)r * sx;
-                for (int j = 0; j < GROUPS; ++j) {
-                    if (!cok[j]) continue;
-                    const T v = raw_load(row + 32 * j);
-                    const uint32_t b = below(v, iso, thr), e = at_or_below(v, iso, thr_le);
-                    if (r < 32) { lo[j] |= b << r; elo[j] |= e << r; }
-                    else { hi[j] |= b << (r - 32); ehi[j] |= e << (r - 32); }
-                }
+        }
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            const T *row = base + (uint64_t)(32 + i) * sx;
+#pragma unroll
+            for (int j = 0; j < GROUPS; ++j) {
+                const T v = (32u + i < nrow && cok[j]) ? raw_load(row + 32 * j) : T(0);
+                hi[j] |= below(v, iso, thr) << i;
+                ehi[j] |= at_or_below(v, iso, thr_le) << i;
             }
         }
 #pragma unroll
         for (int j = 0; j < GROUPS; ++j) {
-            m.lt[lane + 32 * j] = (uint64_t)lo[j] | ((uint64_t)hi[j] << 32);
-            m.le[lane + 32 * j] = (uint64_t)elo[j] | ((uint64_t)ehi[j] << 32);
+            const uint32_t cm = cok[j] ? 0xffffffffu : 0u;
+            m.lt[lane + 32 * j] = (uint64_t)(lo[j] & rmask & cm) | ((uint64_t)(hi[j] & hmask & cm) << 32);
+            m.le[lane + 32 * j] = (uint64_t)(elo[j] & rmask & cm) | ((uint64_t)(ehi[j] & hmask & cm) << 32);
         }
     }
 #pragma unroll 1
