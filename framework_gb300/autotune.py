@@ -14,7 +14,7 @@ import json
 import math
 import os
 
-CANDIDATES = (0, 4, 8, 16, 32, 64)   # 0: the library's own choice from the batch size
+CANDIDATES = (0, 2, 4, 8, 16, 32)   # 0: the library's own choice from the batch size
 DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")
 
 

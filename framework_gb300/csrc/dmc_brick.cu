@@ -1168,8 +1168,9 @@ dmc_status brick_extract(Ctx *ctx, const BrickItem *items, uint32_t n, const Bri
     BatchState &b = *bp;
     if (b.in_flight) return DMC_ERR_INVALID_ARG;
     const int gmax = std::max(std::max(b.grid[0][0], b.grid[0][1]), std::max(b.grid[1][0], b.grid[1][1]));
-    // planes per brick: long sweeps amortise the z halo, but keep at least
-    // three bricks per warp so that the persistent warps stay busy
+    // planes per brick: long sweeps amortise the z halo, but the last wave of
+    // bricks leaves warps idle, so keep at least six bricks per warp (down
+    // to two planes per brick)
     uint32_t zc = ctx->brick_zc ? ctx->brick_zc : 32;
     if (!ctx->brick_zc) {
         for (;;) {
@@ -1178,7 +1179,7 @@ dmc_status brick_extract(Ctx *ctx, const BrickItem *items, uint32_t n, const Bri
                 const uint3 c = items[i].cells;
                 nb += (uint64_t)((c.x + W - 1) / W) * ((c.y + ROWS - 1) / ROWS) * ((c.z + zc - 1) / zc);
             }
-            if (zc <= 4 || nb >= 3ull * (uint64_t)gmax * NWB) break;
+            if (zc <= 2 || nb >= 6ull * (uint64_t)gmax * NWB) break;
             zc >>= 1;
         }
     }
