@@ -720,29 +720,31 @@ __global__ void __launch_bounds__(32 * NWB, EMIT ? 2 : 4) brick_sweep(const Batc
                             } else {
                                 const uint32_t ring = s == 0 ? kRing6 : (s == 1 ? kRing9 : kRing10);
                                 const bool ccw = (info >> (s + 3)) & 1u;
-                                // one rolled lookup site for the four ring cells keeps the
-                                // sweep's code within the instruction cache
-                                uint32_t idx[4] = {0u, 0u, 0u, 0u};
-#pragma unroll 1
+                                // The four ring cells are ranked independently (their
+                                // lookups overlap); each rank is branch-free: the list
+                                // start of its row plus the active cells left of column c.
+                                const uint32_t qc = (uint32_t)c >> 5, bm = (1u << (c & 31)) - 1u;
+                                const uint32_t m0 = qc > 0 ? ~0u : bm, m1 = qc > 1 ? ~0u : (qc == 1 ? bm : 0u);
+                                const uint32_t m2 = qc > 2 ? ~0u : (qc == 2 ? bm : 0u), m3 = qc == 3 ? bm : 0u;
+                                uint32_t idx[4];
+                                bool bad = false;
+#pragma unroll
                                 for (int it = 0; it < 4; ++it) {
                                     const int kk = ccw ? it : (4 - it) & 3;    // ccw 0,1,2,3; cw 0,3,2,1 (dmc.cu:1636-1645)
                                     const uint32_t sl = (ring >> (8 * kk)) & 0xffu;
                                     const int pl = (sl & 1u) ? cur : prv;
-                                    const uint32_t plus = (sl >> 3) & 1u, dr = (sl >> 4) & 1u;
-                                    // ring cell (c + plus, r + dr) of plane pl follows (c, r + dr) in its list
-                                    const uint32_t li = entry_of(S, pl, r + (int)dr, c) + plus;
-                                    uint32_t val = 0;
-                                    if (li >= S.rowstart[pl][HROWS]) {
-                                        atomicOr(err, DEV_ERR_BOUNDS);
-                                    } else {
-                                        const uint32_t rd = M.ent(pl, li);
-                                        uint32_t m = lut_m(tab, cell_cfg(rd), cell_l2(rd), (int)ring_edge(s, kk));
-                                        if (m == 0xffu) { atomicOr(err, DEV_ERR_BOUNDS); m = 0; }
-                                        val = S.segv[pl][r + dr][(c + (int)plus) == W ? 1 : 0] + cell_vrel(rd) + m - g.vbase;
-                                    }
-#pragma unroll
-                                    for (int j = 0; j < 4; ++j) idx[j] = it == j ? val : idx[j];
+                                    const uint32_t plus = (sl >> 3) & 1u, rr = (uint32_t)r + ((sl >> 4) & 1u);
+                                    // ring cell (c + plus, rr) of plane pl follows (c, rr) in its list
+                                    const uint4 w = *reinterpret_cast<const uint4 *>(S.xrow[pl][rr]);
+                                    const uint32_t li = S.rowstart[pl][rr] + __popc(w.x & m0) + __popc(w.y & m1) +
+                                                        __popc(w.z & m2) + __popc(w.w & m3) + plus;
+                                    const bool ok = li < S.rowstart[pl][HROWS];
+                                    const uint32_t rd = ok ? M.ent(pl, li) : 0u;
+                                    const uint32_t m = lut_m(tab, cell_cfg(rd), cell_l2(rd), (int)ring_edge(s, kk));
+                                    bad |= !ok || m == 0xffu;
+                                    idx[it] = S.segv[pl][rr][(c + (int)plus) == W ? 1 : 0] + cell_vrel(rd) + (m == 0xffu ? 0u : m) - g.vbase;
                                 }
+                                if (bad) atomicOr(err, DEV_ERR_BOUNDS);
                                 reinterpret_cast<uint4 *>(out.quads)[q] = make_uint4(idx[0], idx[1], idx[2], idx[3]);
                                 if (out.tris) {
                                     uint32_t *tp = out.tris + 6 * q;
