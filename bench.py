@@ -646,17 +646,27 @@ def main():
     ms, total_points = combine_ranks(ev0.elapsed_time(ev1) / args.steps, N, dist, "cuda")
     st = ex.stats()
 
-    # end to end through the host API: pinned host volume in, host mesh out
+    # end to end through the host C-ABI call (dmc_run_into): pinned host
+    # volume in, mesh (vertices, quads, triangles) out into pinned host buffers
     host_t = torch.empty(vol.shape, dtype=vol.dtype, pin_memory=True)
     host_t.copy_(vol)
     host = fields.as_u16_numpy(host_t) if dtype == "uint16" else host_t.numpy()
+    hv = torch.empty((V, 3), dtype=torch.float32, pin_memory=True).numpy()
+    hq = torch.empty((Q, 4), dtype=torch.int32, pin_memory=True).numpy()
+    ht = torch.empty((2 * Q, 3), dtype=torch.int32, pin_memory=True).numpy()
     e2e_steps = max(1, min(args.e2e_steps, args.steps))
-    ex.run(host, iso=iso, triangles=True)
+    ex.run_into(host, hv, hq, ht, iso=iso)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        m = ex.run(host, iso=iso, triangles=True)
+        nv_e, nq_e = ex.run_into(host, hv, hq, ht, iso=iso)
     e2e_s = (time.perf_counter() - t0) / e2e_steps
+    assert (nv_e, nq_e) == (V, Q)
+    # the same through dmc_run, whose mesh the library allocates per call
+    t0 = time.perf_counter()
+    m = ex.run(host, iso=iso, triangles=True)
+    run_s = time.perf_counter() - t0
     assert len(m.vertices) == V and len(m.quads) == Q
+    del m
 
     line = None
     if rank == 0:
@@ -689,7 +699,9 @@ def main():
                          "pipeline_frac": round(alg_bytes / (ms * 1e-3) / 1e9 / hbm, 4)},
             "cpu_baseline": cpu,
             "e2e": {"value": round(N / e2e_s / 1e9, 3), "unit": "GVoxels/s", "h2d_bytes_per_step": elem * N,
-                    "d2h_bytes_per_step": 12 * V + 16 * Q + 24 * Q, "steps": e2e_steps},
+                    "d2h_bytes_per_step": 12 * V + 16 * Q + 24 * Q, "steps": e2e_steps,
+                    "call": "dmc_run_into, page-locked host buffers",
+                    "dmc_run_gvox_per_s": round(N / run_s / 1e9, 3)},
             "gpu_launches": 5 * args.steps,
             "clocks": clk,
         }

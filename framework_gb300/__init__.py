@@ -34,7 +34,7 @@ ALGO = {"auto": 0, "simple": 1, "brick": 2}
 # exported symbols of the C ABI (include/dmc_gb300.h)
 ABI_SYMBOLS = [
     "dmc_version", "dmc_tables_sha256", "dmc_status_string", "dmc_create", "dmc_destroy",
-    "dmc_set_algo", "dmc_run", "dmc_mesh_free", "dmc_extract_device", "dmc_get_stats",
+    "dmc_set_algo", "dmc_run", "dmc_run_into", "dmc_mesh_free", "dmc_extract_device", "dmc_get_stats",
     "dmc_extract_batch", "dmc_batch_wait", "dmc_set_option", "dmc_extract_device_noalloc",
     "dmc_server_create", "dmc_server_destroy", "dmc_server_add_volume", "dmc_server_submit", "dmc_server_wait",
     "dmc_server_release", "dmc_server_get_stats", "dmc_server_replay", "dmc_write_obj", "dmc_compact_mesh",
@@ -127,6 +127,9 @@ def load_library(build_if_missing=True):
     L.dmc_set_algo.argtypes = [ctypes.c_void_p, ctypes.c_int]
     L.dmc_run.argtypes = [ctypes.c_void_p, P(_Volume), P(ctypes.c_float), P(ctypes.c_float), ctypes.c_float,
                           ctypes.c_uint32, ctypes.c_int, P(_Mesh)]
+    L.dmc_run_into.argtypes = [ctypes.c_void_p, P(_Volume), P(ctypes.c_float), P(ctypes.c_float), ctypes.c_float,
+                               ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
+                               ctypes.c_void_p, P(ctypes.c_uint64), P(ctypes.c_uint64)]
     L.dmc_mesh_free.argtypes = [P(_Mesh)]
     L.dmc_mesh_free.restype = None
     L.dmc_extract_device.argtypes = [ctypes.c_void_p, P(_Volume), P(ctypes.c_float), P(ctypes.c_float), ctypes.c_float,
@@ -276,6 +279,33 @@ class Extractor:
         finally:
             self._lib.dmc_mesh_free(ctypes.byref(m))
         return Mesh(verts, quads, tris, self.stats())
+
+    def run_into(self, volume, vertices, quads, triangles=None, xyz_min=None, xyz_max=None, iso=0.0, num_smooth=0):
+        """Host-memory extraction into caller buffers (``dmc_run_into``).
+
+        ``volume`` is a numpy [z,y,x] float32/uint16 array; ``vertices``
+        (float32 [V,3]), ``quads`` (uint32/int32 [Q,4]) and ``triangles``
+        ([2Q,3] or None) are host arrays, e.g. numpy views of pinned torch
+        tensors.  Returns (n_vertices, n_quads); raises DMCError carrying the
+        needed counts in ``.counts`` when the buffers are too small."""
+        arr, vol = _host_volume(volume)
+        mn, mx = _default_extent(vol.dims, xyz_min, xyz_max)
+        for name, b in (("vertices", vertices), ("quads", quads), ("triangles", triangles)):
+            if b is not None and not b.flags["C_CONTIGUOUS"]:
+                raise DMCError(1, "%s must be C-contiguous" % name)
+        qcap = quads.size // 4
+        if triangles is not None:
+            qcap = min(qcap, triangles.size // 6)
+        nv, nq = ctypes.c_uint64(), ctypes.c_uint64()
+        rc = self._lib.dmc_run_into(self._h, ctypes.byref(vol), _f3(mn), _f3(mx), ctypes.c_float(iso), int(num_smooth),
+                                    vertices.ctypes.data, vertices.size // 3, quads.ctypes.data, qcap,
+                                    triangles.ctypes.data if triangles is not None else None,
+                                    ctypes.byref(nv), ctypes.byref(nq))
+        if rc != 0:
+            e = DMCError(rc, "dmc_run_into")
+            e.counts = (int(nv.value), int(nq.value))
+            raise e
+        return int(nv.value), int(nq.value)
 
     def extract_device(self, volume, xyz_min=None, xyz_max=None, iso=0.0, vertices=None, quads=None,
                        triangles=None, stream=None, dims=None, dtype=None, num_smooth=0):

@@ -349,11 +349,11 @@ dmc_status dmc_set_option(dmc_ctx *ctx, dmc_option opt, int64_t value)
     return DMC_ERR_INVALID_ARG;
 }
 
-dmc_status dmc_run(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min[3], const float xyz_max[3],
-                   float iso, uint32_t num_smooth, int want_triangles, dmc_mesh *out)
+// Host-volume extraction into the context's device output buffers (grown
+// as needed); the totals come back in *V, *Q.
+static dmc_status run_host(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min[3], const float xyz_max[3],
+                           float iso, uint32_t num_smooth, int want_triangles, uint64_t *V, uint64_t *Q)
 {
-    if (!ctx || !out) return DMC_ERR_INVALID_ARG;
-    memset(out, 0, sizeof(*out));
     ExtractArgs a;
     dmc_status s = make_args(vol, xyz_min, xyz_max, iso, a);
     if (s != DMC_OK) return s;
@@ -363,8 +363,8 @@ dmc_status dmc_run(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min[3], 
     if (cudaSetDevice(c->device) != cudaSuccess) return DMC_ERR_CUDA;
     cudaStream_t st = c->stream;
     c->stats = dmc_stats{};
-    uint64_t V = 0, Q = 0;
-    a.n_vertices = &V; a.n_quads = &Q;
+    *V = 0; *Q = 0;
+    a.n_vertices = V; a.n_quads = Q;
     CUDA_TRY(cudaEventRecord(c->ev0, st));
     if (a.n_cells > 0) {
         // upload the host volume (dmc.cu:2077-2079)
@@ -382,28 +382,60 @@ dmc_status dmc_run(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min[3], 
             if (want_triangles && ctx->out.tb / 24 < a.qcap) a.qcap = ctx->out.tb / 24;
             s = run_path(ctx, a, st);
             if (s != DMC_ERR_OUTPUT_OVERFLOW || attempt == 1) break;
-            if (V >= 0xFFFFFFFFull || Q >= 0xFFFFFFFFull) break;
-            if ((s = reserve(&ctx->out.v, &ctx->out.vb, 12 * (V ? V : 1))) != DMC_OK) return s;
-            if ((s = reserve(&ctx->out.q, &ctx->out.qb, 16 * (Q ? Q : 1))) != DMC_OK) return s;
-            if (want_triangles && (s = reserve(&ctx->out.t, &ctx->out.tb, 24 * (Q ? Q : 1))) != DMC_OK) return s;
+            if (*V >= 0xFFFFFFFFull || *Q >= 0xFFFFFFFFull) break;
+            if ((s = reserve(&ctx->out.v, &ctx->out.vb, 12 * (*V ? *V : 1))) != DMC_OK) return s;
+            if ((s = reserve(&ctx->out.q, &ctx->out.qb, 16 * (*Q ? *Q : 1))) != DMC_OK) return s;
+            if (want_triangles && (s = reserve(&ctx->out.t, &ctx->out.tb, 24 * (*Q ? *Q : 1))) != DMC_OK) return s;
             CUDA_TRY(cudaMemsetAsync(c->d_ctl, 0, sizeof(DevCtl), st));
         }
         if (s != DMC_OK) { finish(ctx, st); return s; }
     }
     s = finish(ctx, st);
-    c->stats.n_vertices = V; c->stats.n_quads = Q;
+    c->stats.n_vertices = *V; c->stats.n_quads = *Q;
+    return s;
+}
+
+// download the mesh (dmc.cu:2197-2205) from the context's device buffers
+static dmc_status download(dmc_ctx *ctx, uint64_t V, uint64_t Q, float *hv, uint32_t *hq, uint32_t *ht)
+{
+    cudaStream_t st = ctx->c.stream;
+    if (V) CUDA_TRY(cudaMemcpyAsync(hv, ctx->out.v, 12 * V, cudaMemcpyDeviceToHost, st));
+    if (Q && hq) CUDA_TRY(cudaMemcpyAsync(hq, ctx->out.q, 16 * Q, cudaMemcpyDeviceToHost, st));
+    if (Q && ht) CUDA_TRY(cudaMemcpyAsync(ht, ctx->out.t, 24 * Q, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return DMC_OK;
+}
+
+dmc_status dmc_run(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min[3], const float xyz_max[3],
+                   float iso, uint32_t num_smooth, int want_triangles, dmc_mesh *out)
+{
+    if (!ctx || !out) return DMC_ERR_INVALID_ARG;
+    memset(out, 0, sizeof(*out));
+    uint64_t V = 0, Q = 0;
+    dmc_status s = run_host(ctx, vol, xyz_min, xyz_max, iso, num_smooth, want_triangles, &V, &Q);
     if (s != DMC_OK) return s;
-    // download the mesh (dmc.cu:2197-2205)
     out->n_vertices = V; out->n_quads = Q; out->n_triangles = want_triangles ? 2 * Q : 0;
     out->vertices = (float *)malloc(V ? 12 * V : 1);
     out->quads = (uint32_t *)malloc(Q ? 16 * Q : 1);
     if (want_triangles) out->triangles = (uint32_t *)malloc(Q ? 24 * Q : 1);
     if (!out->vertices || !out->quads || (want_triangles && !out->triangles)) { dmc_mesh_free(out); return DMC_ERR_OOM; }
-    if (V) CUDA_TRY(cudaMemcpyAsync(out->vertices, ctx->out.v, 12 * V, cudaMemcpyDeviceToHost, st));
-    if (Q) CUDA_TRY(cudaMemcpyAsync(out->quads, ctx->out.q, 16 * Q, cudaMemcpyDeviceToHost, st));
-    if (Q && want_triangles) CUDA_TRY(cudaMemcpyAsync(out->triangles, ctx->out.t, 24 * Q, cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaStreamSynchronize(st));
-    return DMC_OK;
+    return download(ctx, V, Q, out->vertices, out->quads, want_triangles ? out->triangles : nullptr);
+}
+
+dmc_status dmc_run_into(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min[3], const float xyz_max[3],
+                        float iso, uint32_t num_smooth, float *h_vertices, uint64_t vertex_capacity,
+                        uint32_t *h_quads, uint64_t quad_capacity, uint32_t *h_triangles,
+                        uint64_t *n_vertices, uint64_t *n_quads)
+{
+    if (!ctx || !n_vertices || !n_quads) return DMC_ERR_INVALID_ARG;
+    if ((vertex_capacity && !h_vertices) || (quad_capacity && !h_quads)) return DMC_ERR_INVALID_ARG;
+    *n_vertices = 0; *n_quads = 0;
+    uint64_t V = 0, Q = 0;
+    dmc_status s = run_host(ctx, vol, xyz_min, xyz_max, iso, num_smooth, h_triangles != nullptr, &V, &Q);
+    *n_vertices = V; *n_quads = Q;
+    if (s != DMC_OK) return s;
+    if (V > vertex_capacity || Q > quad_capacity) return DMC_ERR_OUTPUT_OVERFLOW;
+    return download(ctx, V, Q, h_vertices, h_quads, h_triangles);
 }
 
 }  // extern "C"

@@ -116,6 +116,19 @@ dmc_status dmc_set_algo(dmc_ctx *ctx, dmc_algo algo);
 dmc_status dmc_run(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min[3], const float xyz_max[3],
                    float iso, uint32_t num_smooth, int want_triangles, dmc_mesh *out);
 
+/* dmc_run into caller-owned HOST buffers (no reference counterpart; same
+ * extraction): vertices (3 floats each), quads (4 indices) and, when
+ * h_triangles is not NULL, triangles (6 indices per quad) with the given
+ * capacities in vertices / quads.  Nothing is allocated per call, and with
+ * page-locked (pinned) buffers both copies run at the full host-link rate:
+ * the form to use when meshes are large or calls frequent.  When the mesh is
+ * larger than the capacities the call returns DMC_ERR_OUTPUT_OVERFLOW with
+ * the needed counts in *n_vertices / *n_quads and copies nothing. */
+dmc_status dmc_run_into(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min[3], const float xyz_max[3],
+                        float iso, uint32_t num_smooth, float *h_vertices, uint64_t vertex_capacity,
+                        uint32_t *h_quads, uint64_t quad_capacity, uint32_t *h_triangles,
+                        uint64_t *n_vertices, uint64_t *n_quads);
+
 /* Releases the buffers of a mesh returned by dmc_run. */
 void dmc_mesh_free(dmc_mesh *mesh);
 

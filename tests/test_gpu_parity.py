@@ -134,3 +134,30 @@ def test_reference_shaped_module_api():
     fg.cleanup_device_luts()
     r = oracle.extract(vol, (-5, -5, -5), (5, 5, 5), 0.0)
     assert _bits_equal(v, r["vertices"]) and np.array_equal(t, r["triangles"])
+
+
+def test_run_into_matches_run(extractor):
+    """dmc_run_into (caller host buffers, here page-locked) gives dmc_run's mesh."""
+    import torch
+    import framework_gb300 as fg
+    from framework_gb300 import fields
+    vol = fields.value_noise_u16((120, 90, 70), base_period=16, seed=9)
+    host = fields.as_u16_numpy(vol)
+    m = extractor.run(host, (-1, 0, 2), (5, 4, 9), 32768.0, triangles=True)
+    V, Q = len(m.vertices), len(m.quads)
+    hv = torch.empty((V, 3), dtype=torch.float32, pin_memory=True).numpy()
+    hq = torch.empty((Q, 4), dtype=torch.int32, pin_memory=True).numpy()
+    ht = torch.empty((2 * Q, 3), dtype=torch.int32, pin_memory=True).numpy()
+    for rep in range(2):
+        hv.fill(-1), hq.fill(-1), ht.fill(-1)
+        nv, nq = extractor.run_into(host, hv, hq, ht, (-1, 0, 2), (5, 4, 9), 32768.0)
+        assert (nv, nq) == (V, Q)
+        assert np.array_equal(hv.view(np.uint32), m.vertices.view(np.uint32))
+        assert np.array_equal(hq.view(np.uint32), m.quads) and np.array_equal(ht.view(np.uint32), m.triangles)
+    # pageable numpy buffers and no triangles work the same
+    pv, pq = np.empty((V, 3), np.float32), np.empty((Q, 4), np.uint32)
+    assert extractor.run_into(host, pv, pq, None, (-1, 0, 2), (5, 4, 9), 32768.0) == (V, Q)
+    assert np.array_equal(pv.view(np.uint32), m.vertices.view(np.uint32)) and np.array_equal(pq, m.quads)
+    with pytest.raises(fg.DMCError) as e:
+        extractor.run_into(host, pv[:V - 1], pq, None, (-1, 0, 2), (5, 4, 9), 32768.0)
+    assert e.value.status == 3 and e.value.counts == (V, Q)
