@@ -375,6 +375,10 @@ SERVED_DESC = ("device-resident pool of 64 volumes, per-axis dims log-uniform 32
                "seeded Poisson arrivals; admission by worst-case output bound")
 
 
+# output arenas of the served bench: 4.0 G vertices (48 GB) and 2.1 G quads (34 GB)
+SERVED_VERTEX_ARENA, SERVED_QUAD_ARENA = 0xF0000000, 0x80000000
+
+
 def make_pool(device="cuda"):
     """The serving pool and each volume's 5th/95th percentile (from a 1M-sample draw)."""
     import torch
@@ -427,7 +431,7 @@ def served_measure(vols, n_req=600, quick=False):
     out = {}
     servers = {"served": dict(lanes=2, max_batch=64), "plain": dict(plain=True)}
     for name, kw in servers.items():
-        with fg.Server(0, vertex_arena=(1 << 31), quad_arena=(1 << 30), **kw) as srv:
+        with fg.Server(0, vertex_arena=SERVED_VERTEX_ARENA, quad_arena=SERVED_QUAD_ARENA, **kw) as srv:
             ids = [srv.add_volume(d["volume"]) for d in vols]
             idmap = np.array(ids, np.uint32)
             _warm(srv, idmap, vols)
@@ -454,7 +458,7 @@ def served_measure(vols, n_req=600, quick=False):
     for label, name, rate in loads:
         kw = servers[name]
         n = max(200, min(n_req, int(rate * (4.0 if not quick else 2.0))))
-        with fg.Server(0, vertex_arena=(1 << 31), quad_arena=(1 << 30), **kw) as srv:
+        with fg.Server(0, vertex_arena=SERVED_VERTEX_ARENA, quad_arena=SERVED_QUAD_ARENA, **kw) as srv:
             idmap = np.array([srv.add_volume(d["volume"]) for d in vols], np.uint32)
             _warm(srv, idmap, vols)
             vid, iso, arr = request_trace(vols, n, rate, seed=3)
@@ -523,7 +527,7 @@ def run_served(args, rank, world, dist=None):
     # end to end: a burst of requests, each mesh copied to host memory and released
     vid, iso, _ = request_trace(vols, 128, 0, seed=4)
     d2h = 0
-    with fg.Server(0, vertex_arena=(1 << 31), quad_arena=(1 << 30)) as srv:
+    with fg.Server(0, vertex_arena=SERVED_VERTEX_ARENA, quad_arena=SERVED_QUAD_ARENA) as srv:
         idmap = [srv.add_volume(d["volume"]) for d in vols]
         for v in range(len(vols)):                     # warm up: each volume once
             r = srv.submit(idmap[v], 0.5 * (vols[v]["lo"] + vols[v]["hi"]))
