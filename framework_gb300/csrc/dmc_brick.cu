@@ -53,6 +53,8 @@ struct Geom {
     uint64_t brick_base;   // first brick of this volume in the launch's brick numbering
     uint64_t seg_base;     // first segment of this volume in the shared segment arrays
     uint64_t nseg;
+    uint64_t mask_base;    // first word of this volume's plane masks in the mask store
+    uint32_t mask_tw;      // words of one mask over a row of tiles: 130 per tile, the last one rounded to even
     float iso;
     uint32_t iso_u16;      // uint16 samples: v < iso  <=>  v < iso_u16 (65536: always)
     uint32_t isole_u16;    // uint16 samples: v <= iso <=>  v < isole_u16
@@ -66,6 +68,20 @@ struct alignas(16) PlaneMasks {
     uint64_t lt[W + 2];                // bit r: sample (x0+c, y0+r) < iso
     uint64_t le[W + 2];                // bit r: sample <= iso
 };
+
+// Mask store (global scratch): the count sweep keeps the masks of every
+// point plane of every tile (128 + 2 columns x 34 rows) and the emit sweep
+// copies them back instead of reading and comparing the samples again.
+// Chunk of tile (xs, yb), plane p: lt of its columns, then le of them, each
+// mask_cols() words; tiles of one row lie side by side.
+__device__ __forceinline__ uint32_t mask_cols(const Geom &g, uint32_t x0)
+{
+    return min((uint32_t)W + 2u, (g.pts.x - x0 + 1u) & ~1u);   // columns in the volume, rounded to even
+}
+__device__ __forceinline__ uint64_t *mask_chunk(uint64_t *masks, const Geom &g, uint32_t xs, uint32_t yb, uint32_t p)
+{
+    return masks + g.mask_base + ((uint64_t)p * g.nyb + yb) * 2ull * g.mask_tw + 2ull * (W + 2) * xs;
+}
 
 // Per-warp state used by both sweeps (the count sweep allocates only this).
 struct alignas(16) SweepSmem {
@@ -86,6 +102,7 @@ struct alignas(16) WarpSmem : SweepSmem {
     uint32_t qwork[QBUF];              // quads of one round: entry | edge << 16 | wanted edges << 18
     uint32_t ent[2][CAP];              // packed cell: vrel 11 | qrel 10 | cfg 8 | lut2 1
     uint8_t info[2][CAP];              // own-edge bipolar/ccw bits
+    uint64_t mbar[2];                  // completion of the bulk copies into mask[0] / mask[1]
 };
 
 static_assert(sizeof(WarpSmem) % 16 == 0 && sizeof(SweepSmem) % 16 == 0, "per-warp shared memory must keep 16-byte alignment");
@@ -157,10 +174,11 @@ __device__ __forceinline__ float elem4(float4 v, int q) { return q == 0 ? v.x : 
 // halo columns x0+W, x0+W+1: bit r = sample (x, y0+r, p) below the isovalue,
 // rows 0..33.  Samples outside the volume read as 0 (their cells are never
 // active).  Loads go out 32 per lane before their results are used, and the
-// next plane's rows are prefetched into L2.
+// next plane's rows are prefetched into L2.  With gm set, the masks also go
+// to the mask store chunk gm (ncolr columns per mask).
 template <class T>
 __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint32_t thr, uint32_t thr_le, uint32_t x0,
-                                        uint32_t y0, uint32_t p, PlaneMasks &m, int lane)
+                                        uint32_t y0, uint32_t p, PlaneMasks &m, int lane, uint64_t *gm, uint32_t ncolr)
 {
     uint32_t lo[GROUPS] = {0, 0, 0, 0}, hi[GROUPS] = {0, 0, 0, 0};
     uint32_t elo[GROUPS] = {0, 0, 0, 0}, ehi[GROUPS] = {0, 0, 0, 0};
@@ -215,11 +233,16 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
             }
         }
         // columns 4l..4l+3: two 16-byte stores per mask
+        const uint4 t0 = make_uint4(lo[0] & rmask, hi[0] & hmask, lo[1] & rmask, hi[1] & hmask);
+        const uint4 t1 = make_uint4(lo[2] & rmask, hi[2] & hmask, lo[3] & rmask, hi[3] & hmask);
+        const uint4 e0 = make_uint4(elo[0] & rmask, ehi[0] & hmask, elo[1] & rmask, ehi[1] & hmask);
+        const uint4 e1 = make_uint4(elo[2] & rmask, ehi[2] & hmask, elo[3] & rmask, ehi[3] & hmask);
         uint4 *lt4 = reinterpret_cast<uint4 *>(&m.lt[4 * lane]), *le4 = reinterpret_cast<uint4 *>(&m.le[4 * lane]);
-        lt4[0] = make_uint4(lo[0] & rmask, hi[0] & hmask, lo[1] & rmask, hi[1] & hmask);
-        lt4[1] = make_uint4(lo[2] & rmask, hi[2] & hmask, lo[3] & rmask, hi[3] & hmask);
-        le4[0] = make_uint4(elo[0] & rmask, ehi[0] & hmask, elo[1] & rmask, ehi[1] & hmask);
-        le4[1] = make_uint4(elo[2] & rmask, ehi[2] & hmask, elo[3] & rmask, ehi[3] & hmask);
+        lt4[0] = t0; lt4[1] = t1; le4[0] = e0; le4[1] = e1;
+        if (gm) {   // all 128 columns are in the volume here, so ncolr >= 128
+            uint4 *g4 = reinterpret_cast<uint4 *>(gm + 4 * lane), *ge4 = reinterpret_cast<uint4 *>(gm + ncolr + 4 * lane);
+            g4[0] = t0; g4[1] = t1; ge4[0] = e0; ge4[1] = e1;
+        }
     } else {
         const T *base = vol + (plane0 + y0) * sx + x0 + lane;
         bool cok[GROUPS];
@@ -255,8 +278,12 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
 #pragma unroll
         for (int j = 0; j < GROUPS; ++j) {
             const uint32_t cm = cok[j] ? 0xffffffffu : 0u;
-            m.lt[lane + 32 * j] = (uint64_t)(lo[j] & rmask & cm) | ((uint64_t)(hi[j] & hmask & cm) << 32);
-            m.le[lane + 32 * j] = (uint64_t)(elo[j] & rmask & cm) | ((uint64_t)(ehi[j] & hmask & cm) << 32);
+            const uint32_t c = lane + 32 * j;
+            const uint64_t t = (uint64_t)(lo[j] & rmask & cm) | ((uint64_t)(hi[j] & hmask & cm) << 32);
+            const uint64_t e = (uint64_t)(elo[j] & rmask & cm) | ((uint64_t)(ehi[j] & hmask & cm) << 32);
+            m.lt[c] = t;
+            m.le[c] = e;
+            if (gm && c < ncolr) { gm[c] = t; gm[ncolr + c] = e; }
         }
     }
 #pragma unroll 1
@@ -272,9 +299,75 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
         const uint32_t e32 = __ballot_sync(0xffffffffu, in1 && v <= iso);
         const uint32_t eh2 = __ballot_sync(0xffffffffu, in2 && v2 <= iso) & 3u;
         if (lane == 0) {
-            m.lt[W + hc] = (uint64_t)l32 | ((uint64_t)h2 << 32);
-            m.le[W + hc] = (uint64_t)e32 | ((uint64_t)eh2 << 32);
+            const uint64_t t = (uint64_t)l32 | ((uint64_t)h2 << 32), e = (uint64_t)e32 | ((uint64_t)eh2 << 32);
+            m.lt[W + hc] = t;
+            m.le[W + hc] = e;
+            if (gm && W + hc < ncolr) { gm[W + hc] = t; gm[ncolr + W + hc] = e; }
         }
+    }
+}
+
+// L2 prefetch of the brick's 33 sample rows (own columns) of point plane p,
+// which the corner gathers of the emit sweep read.  Every address lies in
+// the row: its first byte, then the starts of the following 128-byte lines.
+template <class T>
+__device__ __forceinline__ void prefetch_rows(const T *vol, uint3 pts, uint32_t x0, uint32_t y0, uint32_t p, int lane)
+{
+    const uint32_t nrow = min((uint32_t)HROWS, pts.y - y0);
+    const uint32_t bytes = min((uint32_t)W, pts.x - x0) * (uint32_t)sizeof(T);
+    for (uint32_t r = lane; r < nrow; r += 32) {
+        const char *row = reinterpret_cast<const char *>(vol + ((uint64_t)p * pts.y + y0 + r) * pts.x + x0);
+        const uintptr_t a = reinterpret_cast<uintptr_t>(row), end = a + bytes;
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(row));
+        for (uintptr_t l = (a & ~(uintptr_t)127) + 128; l < end; l += 128)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(l));
+    }
+}
+
+// mbarrier and bulk-copy (TMA) primitives for the mask fetches.  Waits are
+// bounded: a wait that gives up returns false and the caller reports
+// DEV_ERR_TIMEOUT.
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t *bar)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+{
+    const uint32_t a = smem_addr(bar);
+    for (uint32_t it = 0; it < (1u << 20); ++it) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}"
+                     : "=r"(done) : "r"(a), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// Bulk copy of plane p's masks from the mask store into slot m (lane 0
+// issues; the slot's mbarrier counts the bytes).  The warp must be done
+// reading the slot's previous plane.
+__device__ __forceinline__ void fetch_masks(uint64_t *masks, const Geom &g, uint32_t xs, uint32_t yb, uint32_t x0,
+                                            uint32_t p, PlaneMasks &m, uint64_t *bar, int lane)
+{
+    __syncwarp();
+    if (lane == 0) {
+        const uint32_t n = mask_cols(g, x0);
+        const uint64_t *src = mask_chunk(masks, g, xs, yb, p);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect(bar, 16u * n);
+        bulk_g2s(m.lt, src, 8u * n, bar);
+        bulk_g2s(m.le, src + n, 8u * n, bar);
     }
 }
 
@@ -491,7 +584,7 @@ template <class T, bool EMIT>
 __global__ void __launch_bounds__(32 * NWB, EMIT ? 2 : 4) brick_sweep(const BatchHead *__restrict__ head, uint32_t group,
                                                         const DeviceTables *__restrict__ tabp,
                                                         uint2 *__restrict__ seg_cnt, EmitOut out,
-                                                        Spill *__restrict__ spill, uint32_t *ticket,
+                                                        Spill *__restrict__ spill, uint64_t *masks, uint32_t *ticket,
                                                         unsigned long long *counters, uint32_t *err)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -501,6 +594,31 @@ __global__ void __launch_bounds__(32 * NWB, EMIT ? 2 : 4) brick_sweep(const Batc
     // the count sweep gives each warp only the SweepSmem part
     WarpSmem &S = *reinterpret_cast<WarpSmem *>(smem_raw + kTablesBytes + (size_t)warp * (EMIT ? sizeof(WarpSmem) : sizeof(SweepSmem)));
     WarpMem M{&S, spill + (uint64_t)blockIdx.x * NWB + warp};
+    // emit: parity of the next completion of each mask slot's mbarrier, and
+    // the slots with a copy in flight
+    uint32_t phase = 0, pend = 0;
+    if (EMIT) {
+        if (lane == 0) {
+            mbar_init(&S.mbar[0]);
+            mbar_init(&S.mbar[1]);
+            asm volatile("fence.mbarrier_init.release.cluster;\n\tfence.proxy.async.shared::cta;" ::: "memory");
+        }
+        __syncwarp();
+    }
+    // emit: waits for the masks of slot s.  If the copy never completes the
+    // error is reported, the copies in flight get another bounded wait (so
+    // none lands after the warp has left) and the warp stops.
+    auto wait_slot = [&](int s) -> bool {
+        if (__all_sync(0xffffffffu, mbar_wait(&S.mbar[s], (phase >> s) & 1u))) {
+            phase ^= 1u << s;
+            pend &= ~(1u << s);
+            return true;
+        }
+        if (lane == 0) atomicOr(err, DEV_ERR_TIMEOUT);
+        for (int q = 0; q < 2; ++q)
+            if ((pend >> q) & 1u) mbar_wait(&S.mbar[q], (phase >> q) & 1u);
+        return false;
+    };
     constexpr uint32_t NR = EMIT ? HROWS : ROWS;   // ranked rows
     uint32_t n_act = 0, n_l2 = 0, n_drop = 0;
     const uint32_t nvols = head->nvol[group];
@@ -526,14 +644,29 @@ __global__ void __launch_bounds__(32 * NWB, EMIT ? 2 : 4) brick_sweep(const Batc
         // the emit sweep also visits plane z1: quads of plane z1-1 reference it
         const uint32_t kend = EMIT ? z1 : z1 - 1;
 
-        load_plane<T>(vol, g.pts, g.iso, g.iso_u16, g.isole_u16, x0, y0, z0, S.mask[z0 & 1], lane);
+        // Point planes z0..z1 of the brick.  The count sweep computes their
+        // masks from the samples and keeps them in the mask store (each
+        // plane once: a brick's last plane only when it is the volume's
+        // last).  The emit sweep copies them back, one plane ahead, and reads
+        // samples only for the corner gathers, prefetched into L2.
+        const uint32_t ncolr = mask_cols(g, x0);
+        if (EMIT) {
+            fetch_masks(masks, g, xs, yb, x0, z0, S.mask[z0 & 1], &S.mbar[z0 & 1], lane);
+            fetch_masks(masks, g, xs, yb, x0, z0 + 1, S.mask[(z0 + 1) & 1], &S.mbar[(z0 + 1) & 1], lane);
+            pend = 3u;
+            prefetch_rows(vol, g.pts, x0, y0, z0, lane);
+            prefetch_rows(vol, g.pts, x0, y0, z0 + 1, lane);
+            if (!wait_slot(z0 & 1)) return;
+        } else {
+            load_plane<T>(vol, g.pts, g.iso, g.iso_u16, g.isole_u16, x0, y0, z0, S.mask[z0 & 1], lane,
+                          mask_chunk(masks, g, xs, yb, z0), ncolr);
+        }
         for (uint32_t k = z0; k <= kend; ++k) {
             const int cur = k & 1, prv = cur ^ 1;
             const int lp = EMIT ? cur : 0;                 // list slot of this plane
             const bool have_plane = k < g.cells.z;
             uint32_t L = 0;
             if (have_plane) {
-                load_plane<T>(vol, g.pts, g.iso, g.iso_u16, g.isole_u16, x0, y0, k + 1, S.mask[(k + 1) & 1], lane);
                 if (EMIT) {
                     for (uint32_t r = lane; r < HROWS; r += 32) {
                         const uint32_t yy = y0 + r;
@@ -544,6 +677,12 @@ __global__ void __launch_bounds__(32 * NWB, EMIT ? 2 : 4) brick_sweep(const Batc
                         }
                         S.segv[cur][r][0] = own.x; S.segv[cur][r][1] = nxt.x; S.segq[cur][r] = own.y;
                     }
+                    if (!wait_slot((k + 1) & 1)) return;
+                    if (k + 2 <= z1) prefetch_rows(vol, g.pts, x0, y0, k + 2, lane);
+                } else {
+                    const bool keep = k + 1 < z1 || z1 == g.cells.z;
+                    load_plane<T>(vol, g.pts, g.iso, g.iso_u16, g.isole_u16, x0, y0, k + 1, S.mask[(k + 1) & 1], lane,
+                                  keep ? mask_chunk(masks, g, xs, yb, k + 1) : nullptr, ncolr);
                 }
                 __syncwarp();
                 const uint64_t *mk = S.mask[cur].lt, *mk1 = S.mask[(k + 1) & 1].lt;
@@ -662,6 +801,11 @@ __global__ void __launch_bounds__(32 * NWB, EMIT ? 2 : 4) brick_sweep(const Batc
                     }
                 }
                 __syncwarp();
+            }
+            // plane k's masks are done with: its slot takes plane k+2
+            if (EMIT && k + 1 < g.cells.z && k + 1 <= kend) {
+                fetch_masks(masks, g, xs, yb, x0, k + 2, S.mask[cur], &S.mbar[cur], lane);
+                pend |= 1u << cur;
             }
             if (!EMIT) {
                 if (y0 + lane < g.cells.y) {
@@ -891,6 +1035,26 @@ static void iso_thresholds(float f, uint32_t &lt, uint32_t &le)
     else le = (uint32_t)f + 1;
 }
 
+// Mask store of one volume: for every point plane and row of tiles, the lt
+// and le words of each tile's columns (130 per tile; the last tile holds the
+// columns left in the volume, rounded up to even so that every chunk starts
+// and ends on a 16-byte boundary).
+static uint32_t mask_row_words(const BrickItem &it)
+{
+    using namespace brick;
+    const uint32_t nxs = (it.cells.x + W - 1) / W;
+    if (nxs == 0) return 0;
+    const uint32_t last = std::min<uint32_t>(W + 2, (it.pts.x - (nxs - 1) * W + 1) & ~1u);
+    return (W + 2) * (nxs - 1) + last;
+}
+static uint64_t mask_words(const BrickItem &it)
+{
+    using namespace brick;
+    if (it.cells.x == 0 || it.cells.y == 0 || it.cells.z == 0) return 0;
+    const uint64_t nyb = (it.cells.y + ROWS - 1) / ROWS;
+    return (uint64_t)it.pts.z * nyb * 2ull * mask_row_words(it);
+}
+
 // Per-context pipeline state.  Scratch (device) and staging (pinned host) are
 // laid out for capacities that only grow; a captured graph holds the
 // addresses of both, plus the output buffers, and is re-captured when any of
@@ -898,7 +1062,7 @@ static void iso_thresholds(float f, uint32_t &lt, uint32_t &le)
 struct BatchState {
     // capacities of the layout
     uint32_t cap_items = 0;
-    uint64_t cap_seg = 0, cap_coord = 0;
+    uint64_t cap_seg = 0, cap_coord = 0, cap_mask = 0;
     uint64_t layout_gen = 0;           // scratch_gen the layout was carved for (0: none)
     uint64_t layout_id = 0;            // bumped on every re-carve: captured graphs hold the addresses
     // device layout (inside ctx->scratch)
@@ -906,6 +1070,7 @@ struct BatchState {
     uint2 *seg_cnt = nullptr, *seg_off = nullptr;
     TileState *tiles = nullptr;
     brick::Spill *spill = nullptr;
+    uint64_t *masks = nullptr;          // mask store, cap_mask words
     float *coord = nullptr;
     dmc_batch_result *d_res = nullptr;
     uint32_t *tickets = nullptr;
@@ -959,15 +1124,17 @@ static dmc_status batch_state(Ctx *ctx, BatchState **out)
 }
 
 // Carves the scratch and staging for at least the given capacities.
-static dmc_status batch_layout(Ctx *ctx, BatchState &b, uint32_t items, uint64_t seg, uint64_t ncoord)
+static dmc_status batch_layout(Ctx *ctx, BatchState &b, uint32_t items, uint64_t seg, uint64_t ncoord, uint64_t nmask)
 {
     using namespace brick;
-    const bool fits = b.layout_gen == ctx->scratch_gen && items <= b.cap_items && seg <= b.cap_seg && ncoord <= b.cap_coord;
+    const bool fits = b.layout_gen == ctx->scratch_gen && items <= b.cap_items && seg <= b.cap_seg &&
+                      ncoord <= b.cap_coord && nmask <= b.cap_mask;
     if (fits) return DMC_OK;
     // grow with headroom so that a stream of similar batches settles on one layout
     b.cap_items = std::max<uint32_t>(b.cap_items, items + items / 4 + 1);
     b.cap_seg = std::max<uint64_t>(b.cap_seg, seg + seg / 4 + SCAN_TILE);
     b.cap_coord = std::max<uint64_t>(b.cap_coord, ncoord + ncoord / 4 + 64);
+    b.cap_mask = std::max<uint64_t>(b.cap_mask, nmask + nmask / 4 + 64);
     const uint64_t cap_tiles = (b.cap_seg + SCAN_TILE - 1) / SCAN_TILE;
     const int gmax = std::max(std::max(b.grid[0][0], b.grid[0][1]), std::max(b.grid[1][0], b.grid[1][1]));
     b.plan_bytes = sizeof(BatchHead) + sizeof(Geom) * (size_t)b.cap_items;
@@ -977,6 +1144,7 @@ static dmc_status batch_layout(Ctx *ctx, BatchState &b, uint32_t items, uint64_t
     const size_t o_cnt = carve(8 * b.cap_seg), o_off = carve(8 * b.cap_seg);
     const size_t o_tiles = carve(sizeof(TileState) * cap_tiles);
     const size_t o_spill = carve(sizeof(Spill) * (size_t)gmax * NWB);
+    const size_t o_mask = carve(8 * b.cap_mask);
     const size_t o_coord = carve(4 * b.cap_coord);
     const size_t o_res = carve(sizeof(dmc_batch_result) * (size_t)b.cap_items);
     const size_t o_tk = carve(256);
@@ -989,6 +1157,7 @@ static dmc_status batch_layout(Ctx *ctx, BatchState &b, uint32_t items, uint64_t
     b.seg_off = (uint2 *)(base + o_off);
     b.tiles = (TileState *)(base + o_tiles);
     b.spill = (Spill *)(base + o_spill);
+    b.masks = (uint64_t *)(base + o_mask);
     b.coord = (float *)(base + o_coord);
     b.d_res = (dmc_batch_result *)(base + o_res);
     b.tickets = (uint32_t *)(base + o_tk);
@@ -1022,12 +1191,12 @@ static dmc_status enqueue_front(Ctx *ctx, BatchState &b, dmc_batch_result *d_res
     if (timed) CUDA_TRY(cudaEventRecord(ctx->evk[0], st));
     if (all || nb[0]) {
         brick_sweep<float, false><<<b.grid[0][0], 32 * NWB, kCountSmem, st>>>(
-            b.d_plan, 0, ctx->d_tab, b.seg_cnt, EmitOut{}, b.spill, &b.tickets[0], ctx->d_ctl->counters, &ctx->d_ctl->err);
+            b.d_plan, 0, ctx->d_tab, b.seg_cnt, EmitOut{}, b.spill, b.masks, &b.tickets[0], ctx->d_ctl->counters, &ctx->d_ctl->err);
         CUDA_TRY(cudaGetLastError());
     }
     if (all || nb[1]) {
         brick_sweep<uint16_t, false><<<b.grid[1][0], 32 * NWB, kCountSmem, st>>>(
-            b.d_plan, 1, ctx->d_tab, b.seg_cnt, EmitOut{}, b.spill, &b.tickets[1], ctx->d_ctl->counters, &ctx->d_ctl->err);
+            b.d_plan, 1, ctx->d_tab, b.seg_cnt, EmitOut{}, b.spill, b.masks, &b.tickets[1], ctx->d_ctl->counters, &ctx->d_ctl->err);
         CUDA_TRY(cudaGetLastError());
     }
     if (timed) CUDA_TRY(cudaEventRecord(ctx->evk[1], st));
@@ -1050,12 +1219,12 @@ static dmc_status enqueue_back(Ctx *ctx, BatchState &b, const brick::EmitOut &eo
     if (timed) CUDA_TRY(cudaEventRecord(ctx->evk[3], st));
     if (all || nb[0]) {
         brick_sweep<float, true><<<b.grid[0][1], 32 * NWB, kEmitSmem, st>>>(
-            b.d_plan, 0, ctx->d_tab, nullptr, eo, b.spill, &b.tickets[2], ctx->d_ctl->counters, &ctx->d_ctl->err);
+            b.d_plan, 0, ctx->d_tab, nullptr, eo, b.spill, b.masks, &b.tickets[2], ctx->d_ctl->counters, &ctx->d_ctl->err);
         CUDA_TRY(cudaGetLastError());
     }
     if (all || nb[1]) {
         brick_sweep<uint16_t, true><<<b.grid[1][1], 32 * NWB, kEmitSmem, st>>>(
-            b.d_plan, 1, ctx->d_tab, nullptr, eo, b.spill, &b.tickets[3], ctx->d_ctl->counters, &ctx->d_ctl->err);
+            b.d_plan, 1, ctx->d_tab, nullptr, eo, b.spill, b.masks, &b.tickets[3], ctx->d_ctl->counters, &ctx->d_ctl->err);
         CUDA_TRY(cudaGetLastError());
     }
     if (timed) CUDA_TRY(cudaEventRecord(ctx->evk[4], st));
@@ -1143,10 +1312,11 @@ static dmc_status retarget_graph(Ctx *ctx, BatchState &b, const brick::EmitOut &
         uint2 *a_cnt = nullptr;
         EmitOut a_out = eo;
         Spill *a_spill = b.spill;
+        uint64_t *a_masks = b.masks;
         uint32_t *a_ticket = &b.tickets[2 + g];
         unsigned long long *a_counters = ctx->d_ctl->counters;
         uint32_t *a_err = &ctx->d_ctl->err;
-        void *args[] = {&a_head, &a_group, &a_tab, &a_cnt, &a_out, &a_spill, &a_ticket, &a_counters, &a_err};
+        void *args[] = {&a_head, &a_group, &a_tab, &a_cnt, &a_out, &a_spill, &a_masks, &a_ticket, &a_counters, &a_err};
         cudaKernelNodeParams kp = b.emit_params[g];
         kp.kernelParams = args;
         kp.extra = nullptr;
@@ -1186,21 +1356,22 @@ dmc_status brick_extract(Ctx *ctx, const BrickItem *items, uint32_t n, const Bri
         }
     }
     // descriptors: the f32 volumes, then the u16 ones (one launch per type)
-    uint64_t nseg = 0, ncoord = 0, nb[2] = {0, 0};
+    uint64_t nseg = 0, ncoord = 0, nmask = 0, nb[2] = {0, 0};
     uint32_t nvol[2] = {0, 0};
     for (uint32_t i = 0; i < n; ++i) {
         const BrickItem &it = items[i];
         nseg += (uint64_t)it.cells.z * it.cells.y * ((it.cells.x + W - 1) / W);
         ncoord += (uint64_t)it.pts.x + it.pts.y + it.pts.z;
+        nmask += mask_words(it);
         nvol[it.dtype == DMC_F32 ? 0 : 1]++;
     }
     const uint64_t n_tiles = (nseg + SCAN_TILE - 1) / SCAN_TILE;
     if (n_tiles >= (1ull << 31)) return DMC_ERR_UNSUPPORTED;
-    if ((s = batch_layout(ctx, b, n, nseg, ncoord)) != DMC_OK) return s;
+    if ((s = batch_layout(ctx, b, n, nseg, ncoord, nmask)) != DMC_OK) return s;
     BatchHead *head = (BatchHead *)b.h_stage;
     Geom *geoms = (Geom *)(head + 1);
     uint32_t pos[2] = {0, nvol[0]};
-    uint64_t seg_base = 0, coord_base = 0;
+    uint64_t seg_base = 0, coord_base = 0, mask_base = 0;
     for (uint32_t i = 0; i < n; ++i) {
         const BrickItem &it = items[i];
         const int grp = it.dtype == DMC_F32 ? 0 : 1;
@@ -1218,6 +1389,9 @@ dmc_status brick_extract(Ctx *ctx, const BrickItem *items, uint32_t n, const Bri
         g.nseg = (uint64_t)it.cells.z * it.cells.y * g.nxs;
         seg_base += g.nseg;
         g.coord = b.coord + coord_base;
+        g.mask_tw = mask_row_words(it);
+        g.mask_base = mask_base;
+        mask_base += mask_words(it);
         coord_base += (uint64_t)it.pts.x + it.pts.y + it.pts.z;
         g.item = i;
     }
