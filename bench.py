@@ -659,7 +659,8 @@ def main():
     hq = torch.empty((Q, 4), dtype=torch.int32, pin_memory=True).numpy()
     ht = torch.empty((2 * Q, 3), dtype=torch.int32, pin_memory=True).numpy()
     e2e_steps = max(1, min(args.e2e_steps, args.steps))
-    ex.run_into(host, hv, hq, ht, iso=iso)
+    for _ in range(2):   # the first call grows the context's device buffers, the second sets up the slab streams
+        ex.run_into(host, hv, hq, ht, iso=iso)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         nv_e, nq_e = ex.run_into(host, hv, hq, ht, iso=iso)
@@ -704,7 +705,8 @@ def main():
             "cpu_baseline": cpu,
             "e2e": {"value": round(N / e2e_s / 1e9, 3), "unit": "GVoxels/s", "h2d_bytes_per_step": elem * N,
                     "d2h_bytes_per_step": 12 * V + 16 * Q + 24 * Q, "steps": e2e_steps,
-                    "call": "dmc_run_into, page-locked host buffers",
+                    "call": "dmc_run_into, page-locked host buffers (upload, extraction and download overlapped "
+                            "in z slabs)",
                     "dmc_run_gvox_per_s": round(N / run_s / 1e9, 3)},
             "gpu_launches": 5 * args.steps,
             "clocks": clk,

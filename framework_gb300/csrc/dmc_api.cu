@@ -345,6 +345,10 @@ dmc_status dmc_set_option(dmc_ctx *ctx, dmc_option opt, int64_t value)
         if (value < 0 || value > 256) return DMC_ERR_INVALID_ARG;
         ctx->c.brick_zc = (uint32_t)value;
         return DMC_OK;
+    case DMC_OPT_STREAM_SLABS:
+        if (value < 0 || value > 16) return DMC_ERR_INVALID_ARG;
+        ctx->c.stream_slabs = (uint32_t)value;
+        return DMC_OK;
     }
     return DMC_ERR_INVALID_ARG;
 }
@@ -395,6 +399,47 @@ static dmc_status run_host(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_
     return s;
 }
 
+// internal status of run_streamed: the streamed path does not apply
+constexpr dmc_status kNotStreamed = (dmc_status)-1;
+
+// Streamed dmc_run_into (brick path, no smoothing): the volume goes up in z
+// slabs while earlier slabs are extracted and their meshes come down.  Taken
+// for volumes of 64 MiB and more unless the option says otherwise; returns
+// kNotStreamed when it does not apply.
+static dmc_status run_streamed(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min[3], const float xyz_max[3],
+                               float iso, uint32_t num_smooth, float *hv, uint64_t vcap, uint32_t *hq, uint64_t qcap,
+                               uint32_t *ht, uint64_t *V, uint64_t *Q, bool *dev_short)
+{
+    Ctx *c = &ctx->c;
+    *dev_short = false;
+    if (c->stream_slabs == 1 || num_smooth || c->algo == DMC_ALGO_SIMPLE || c->batch_pending) return kNotStreamed;
+    ExtractArgs a;
+    dmc_status s = make_args(vol, xyz_min, xyz_max, iso, a);
+    if (s != DMC_OK || a.n_cells == 0 || !brick_supports(a)) return kNotStreamed;
+    const uint64_t bytes = volume_bytes(vol);
+    uint32_t slabs = c->stream_slabs;
+    if (slabs == 0) {
+        if (bytes < (64ull << 20)) return kNotStreamed;
+        slabs = (uint32_t)std::min<uint64_t>(16, std::max<uint64_t>(2, bytes / (160ull << 20)));   // 12 at 2 GiB
+    }
+    // the context's device output buffers as they are: too small ones make
+    // the caller take the plain path, which grows them
+    if (!ctx->out.v || !ctx->out.q || (ht && !ctx->out.t)) { *dev_short = true; return DMC_ERR_OUTPUT_OVERFLOW; }
+    if (cudaSetDevice(c->device) != cudaSuccess) return DMC_ERR_CUDA;
+    if ((s = reserve(&c->d_vol, &c->d_vol_bytes, bytes)) != DMC_OK) return s;
+    c->stats = dmc_stats{};
+    c->stats.algo = DMC_ALGO_BRICK;
+    a.vol = c->d_vol;
+    a.verts = (float *)ctx->out.v; a.vcap = ctx->out.vb / 12;
+    a.quads = (uint32_t *)ctx->out.q; a.qcap = ctx->out.qb / 16;
+    a.tris = ht ? (uint32_t *)ctx->out.t : nullptr;
+    if (ht && ctx->out.tb / 24 < a.qcap) a.qcap = ctx->out.tb / 24;
+    StreamIO io{vol->data, hv, vcap, hq, qcap, ht};
+    s = brick_run_streamed(c, a, io, slabs, dev_short, c->stream);
+    *V = c->stats.n_vertices; *Q = c->stats.n_quads;
+    return s;
+}
+
 // download the mesh (dmc.cu:2197-2205) from the context's device buffers
 static dmc_status download(dmc_ctx *ctx, uint64_t V, uint64_t Q, float *hv, uint32_t *hq, uint32_t *ht)
 {
@@ -431,7 +476,16 @@ dmc_status dmc_run_into(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min
     if ((vertex_capacity && !h_vertices) || (quad_capacity && !h_quads)) return DMC_ERR_INVALID_ARG;
     *n_vertices = 0; *n_quads = 0;
     uint64_t V = 0, Q = 0;
-    dmc_status s = run_host(ctx, vol, xyz_min, xyz_max, iso, num_smooth, h_triangles != nullptr, &V, &Q);
+    bool dev_short = false;
+    dmc_status s = run_streamed(ctx, vol, xyz_min, xyz_max, iso, num_smooth, h_vertices, vertex_capacity, h_quads,
+                                quad_capacity, h_triangles, &V, &Q, &dev_short);
+    if (s != kNotStreamed && !(s == DMC_ERR_OUTPUT_OVERFLOW && dev_short)) {
+        *n_vertices = V; *n_quads = Q;
+        return s;
+    }
+    // not streamed, or the context's device buffers were too small: the
+    // plain path grows them (and they stay for the next call)
+    s = run_host(ctx, vol, xyz_min, xyz_max, iso, num_smooth, h_triangles != nullptr, &V, &Q);
     *n_vertices = V; *n_quads = Q;
     if (s != DMC_OK) return s;
     if (V > vertex_capacity || Q > quad_capacity) return DMC_ERR_OUTPUT_OVERFLOW;

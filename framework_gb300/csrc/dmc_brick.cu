@@ -29,6 +29,7 @@
 #include <algorithm>
 #include <new>
 #include <vector>
+#include <type_traits>
 
 namespace dmc {
 
@@ -41,7 +42,10 @@ constexpr int HROWS = ROWS + 1;           // with the halo row
 constexpr int MAXL = HROWS * (W + 1);     // most active cells one plane of a brick can hold
 constexpr int CAP = 256;                  // entries kept in shared memory per plane
 constexpr int OVF = MAXL - CAP;           // entries per plane that spill to global scratch
-constexpr int NWB = 8;                    // warps per block (independent)
+constexpr int NWB_COUNT = 8;              // warps per block of the count sweep (independent): 4 blocks per SM
+constexpr int NWB_EMIT = 8;               // of the emit sweep: 2 blocks per SM
+constexpr int nwb(bool emit) { return emit ? NWB_EMIT : NWB_COUNT; }
+constexpr int kMaxSlabs = 16;             // z slabs of a streamed host extraction
 constexpr int QBUF = 96;                  // quads of one round of owner cells (3 per cell)
 constexpr int SCAN_NT = 256, SCAN_ITEMS = 8, SCAN_TILE = SCAN_NT * SCAN_ITEMS;
 
@@ -517,6 +521,12 @@ struct EmitOut {
 // one).  The host writes it to pinned memory and one copy moves it to the
 // device, so the kernels take every batch-dependent size from here and a
 // captured graph replays any batch that fits the scratch layout.
+// Bricks [lo, lo + cnt) of a launch's numbering (cnt = kAllBricks: all of them).
+struct BrickRange {
+    uint32_t lo, cnt;
+};
+constexpr uint32_t kAllBricks = 0xffffffffu;
+
 struct alignas(64) BatchHead {
     unsigned long long nbricks[2];   // bricks of the f32 / u16 volumes
     unsigned long long nseg;         // segments of all volumes
@@ -581,8 +591,8 @@ __device__ __forceinline__ uint32_t ring_edge(int s, int kk)
 // Active cells are compacted per plane in output order and processed 32 at a
 // time, one per lane; quads are compacted the same way.
 template <class T, bool EMIT>
-__global__ void __launch_bounds__(32 * NWB, EMIT ? 2 : 4) brick_sweep(const BatchHead *__restrict__ head, uint32_t group,
-                                                        const DeviceTables *__restrict__ tabp,
+__global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 4) brick_sweep(const BatchHead *__restrict__ head, uint32_t group,
+                                                        BrickRange range, const DeviceTables *__restrict__ tabp,
                                                         uint2 *__restrict__ seg_cnt, EmitOut out,
                                                         Spill *__restrict__ spill, uint64_t *masks, uint32_t *ticket,
                                                         unsigned long long *counters, uint32_t *err)
@@ -593,7 +603,7 @@ __global__ void __launch_bounds__(32 * NWB, EMIT ? 2 : 4) brick_sweep(const Batc
     const DeviceTables &tab = stage_tables(tabp, reinterpret_cast<DeviceTables *>(smem_raw));
     // the count sweep gives each warp only the SweepSmem part
     WarpSmem &S = *reinterpret_cast<WarpSmem *>(smem_raw + kTablesBytes + (size_t)warp * (EMIT ? sizeof(WarpSmem) : sizeof(SweepSmem)));
-    WarpMem M{&S, spill + (uint64_t)blockIdx.x * NWB + warp};
+    WarpMem M{&S, spill + (uint64_t)blockIdx.x * nwb(EMIT) + warp};
     // emit: parity of the next completion of each mask slot's mbarrier, and
     // the slots with a copy in flight
     uint32_t phase = 0, pend = 0;
@@ -626,7 +636,9 @@ __global__ void __launch_bounds__(32 * NWB, EMIT ? 2 : 4) brick_sweep(const Batc
     const Geom *__restrict__ vols = batch_geoms(head) + (group ? head->nvol[0] : 0u);
 
     for (;;) {
-        const uint32_t bg = claim_brick(ticket, lane);
+        const uint32_t t = claim_brick(ticket, lane);
+        if (t >= range.cnt) break;
+        const uint64_t bg = (uint64_t)range.lo + t;
         if (bg >= nbricks) break;
         // volume of this brick: last one whose first brick is <= bg
         uint32_t lo = 0, hi = nvols - 1;
@@ -964,17 +976,33 @@ __global__ void volume_results(BatchHead *head, const uint2 *seg_cnt, const uint
     }
 }
 
+// Running totals and error word after a slab's scan, written to mapped host
+// memory so that the host learns each slab's output range while later slabs
+// are still uploading.
+__global__ void snap_totals(const DevCtl *ctl, unsigned long long *dst)
+{
+    if (threadIdx.x == 0) {
+        dst[0] = ctl->totals[0];
+        dst[1] = ctl->totals[1];
+        dst[2] = ctl->err;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // segment scan (decoupled look-back)
 
+// Scans segments [seg_lo, seg_lo + seg_cnt) (clipped to the plan's segments).
 __global__ void __launch_bounds__(SCAN_NT) seg_scan(const BatchHead *__restrict__ head, const uint2 *__restrict__ cnt,
-                                                    ScanCtl ctl, uint2 *__restrict__ off)
+                                                    ScanCtl ctl, uint2 *__restrict__ off, uint64_t seg_lo, uint64_t seg_cnt)
 {
     __shared__ uint32_t s_slot;
     __shared__ unsigned long long s_warp[SCAN_NT / 32 + 1];
     __shared__ unsigned long long s_ex[2];
-    const uint64_t n = head->nseg;
-    ctl.n_tiles = head->n_tiles;
+    const uint64_t rest = seg_lo >= head->nseg ? 0ull : (uint64_t)head->nseg - seg_lo;
+    const uint64_t n = rest < seg_cnt ? rest : seg_cnt;
+    cnt += seg_lo;
+    off += seg_lo;
+    ctl.n_tiles = (uint32_t)((n + SCAN_TILE - 1) / SCAN_TILE);
     // tiles are claimed in order, so a tile only waits on tiles whose blocks already run
     for (;;) {
         const uint32_t tile = claim_tile(ctl.ticket, &s_slot);
@@ -1009,8 +1037,8 @@ bool brick_supports(const ExtractArgs &a)
     return a.cells.x >= 1 && a.cells.y >= 1 && a.cells.z >= 1;
 }
 
-constexpr size_t kEmitSmem = brick::kTablesBytes + sizeof(brick::WarpSmem) * brick::NWB;
-constexpr size_t kCountSmem = brick::kTablesBytes + sizeof(brick::SweepSmem) * brick::NWB;
+constexpr size_t kEmitSmem = brick::kTablesBytes + sizeof(brick::WarpSmem) * brick::NWB_EMIT;
+constexpr size_t kCountSmem = brick::kTablesBytes + sizeof(brick::SweepSmem) * brick::NWB_COUNT;
 
 template <class T, bool EMIT>
 static int sweep_grid(Ctx *ctx)
@@ -1019,7 +1047,7 @@ static int sweep_grid(Ctx *ctx)
     const size_t smem = EMIT ? kEmitSmem : kCountSmem;
     cudaFuncSetAttribute(brick_sweep<T, EMIT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, brick_sweep<T, EMIT>, 32 * NWB, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, brick_sweep<T, EMIT>, 32 * nwb(EMIT), smem);
     if (b < 1) b = 1;
     return b * ctx->num_sms;
 }
@@ -1089,11 +1117,28 @@ struct BatchState {
     cudaGraphNode_t emit_node[2] = {nullptr, nullptr};
     cudaKernelNodeParams emit_params[2]{};
     brick::EmitOut g_out{};
+    // streamed host extraction: copy streams, per-slab events and mapped
+    // snapshots of the running totals (vertices, quads, error word per slab)
+    cudaStream_t s_in = nullptr, s_out = nullptr;
+    cudaEvent_t ev_start = nullptr;
+    cudaEvent_t ev_in[brick::kMaxSlabs]{}, ev_tot[brick::kMaxSlabs]{}, ev_emit[brick::kMaxSlabs]{};
+    unsigned long long *h_snap = nullptr, *d_snap = nullptr;
     // batch in flight
     bool in_flight = false;
     uint32_t n_inflight = 0;
     cudaEvent_t done = nullptr;
 };
+
+// Resident warps of the largest sweep launch: one spill slot each, and the
+// unit of the planes-per-brick rule.
+static uint64_t sweep_warps(const BatchState &b)
+{
+    using namespace brick;
+    uint64_t w = 0;
+    for (int t = 0; t < 2; ++t)
+        w = std::max<uint64_t>(w, std::max<uint64_t>((uint64_t)b.grid[t][0] * NWB_COUNT, (uint64_t)b.grid[t][1] * NWB_EMIT));
+    return w;
+}
 
 void batch_state_free(Ctx *ctx)
 {
@@ -1103,6 +1148,15 @@ void batch_state_free(Ctx *ctx)
     if (b->graph) cudaGraphDestroy(b->graph);
     if (b->done) cudaEventDestroy(b->done);
     if (b->h_stage) cudaFreeHost(b->h_stage);
+    if (b->s_in) cudaStreamDestroy(b->s_in);
+    if (b->s_out) cudaStreamDestroy(b->s_out);
+    if (b->ev_start) cudaEventDestroy(b->ev_start);
+    for (int i = 0; i < brick::kMaxSlabs; ++i) {
+        if (b->ev_in[i]) cudaEventDestroy(b->ev_in[i]);
+        if (b->ev_tot[i]) cudaEventDestroy(b->ev_tot[i]);
+        if (b->ev_emit[i]) cudaEventDestroy(b->ev_emit[i]);
+    }
+    if (b->h_snap) cudaFreeHost(b->h_snap);
     delete b;
     ctx->batch = nullptr;
 }
@@ -1136,14 +1190,13 @@ static dmc_status batch_layout(Ctx *ctx, BatchState &b, uint32_t items, uint64_t
     b.cap_coord = std::max<uint64_t>(b.cap_coord, ncoord + ncoord / 4 + 64);
     b.cap_mask = std::max<uint64_t>(b.cap_mask, nmask + nmask / 4 + 64);
     const uint64_t cap_tiles = (b.cap_seg + SCAN_TILE - 1) / SCAN_TILE;
-    const int gmax = std::max(std::max(b.grid[0][0], b.grid[0][1]), std::max(b.grid[1][0], b.grid[1][1]));
     b.plan_bytes = sizeof(BatchHead) + sizeof(Geom) * (size_t)b.cap_items;
     size_t off = 0;
     auto carve = [&](size_t bytes) { size_t r = off; off += (bytes + 255) & ~(size_t)255; return r; };
     const size_t o_plan = carve(b.plan_bytes);
     const size_t o_cnt = carve(8 * b.cap_seg), o_off = carve(8 * b.cap_seg);
-    const size_t o_tiles = carve(sizeof(TileState) * cap_tiles);
-    const size_t o_spill = carve(sizeof(Spill) * (size_t)gmax * NWB);
+    const size_t o_tiles = carve(sizeof(TileState) * (cap_tiles + kMaxSlabs));   // slabs: one partial tile each
+    const size_t o_spill = carve(sizeof(Spill) * (size_t)sweep_warps(b));
     const size_t o_mask = carve(8 * b.cap_mask);
     const size_t o_coord = carve(4 * b.cap_coord);
     const size_t o_res = carve(sizeof(dmc_batch_result) * (size_t)b.cap_items);
@@ -1190,20 +1243,20 @@ static dmc_status enqueue_front(Ctx *ctx, BatchState &b, dmc_batch_result *d_res
     CUDA_TRY(cudaGetLastError());
     if (timed) CUDA_TRY(cudaEventRecord(ctx->evk[0], st));
     if (all || nb[0]) {
-        brick_sweep<float, false><<<b.grid[0][0], 32 * NWB, kCountSmem, st>>>(
-            b.d_plan, 0, ctx->d_tab, b.seg_cnt, EmitOut{}, b.spill, b.masks, &b.tickets[0], ctx->d_ctl->counters, &ctx->d_ctl->err);
+        brick_sweep<float, false><<<b.grid[0][0], 32 * NWB_COUNT, kCountSmem, st>>>(
+            b.d_plan, 0, BrickRange{0, kAllBricks}, ctx->d_tab, b.seg_cnt, EmitOut{}, b.spill, b.masks, &b.tickets[0], ctx->d_ctl->counters, &ctx->d_ctl->err);
         CUDA_TRY(cudaGetLastError());
     }
     if (all || nb[1]) {
-        brick_sweep<uint16_t, false><<<b.grid[1][0], 32 * NWB, kCountSmem, st>>>(
-            b.d_plan, 1, ctx->d_tab, b.seg_cnt, EmitOut{}, b.spill, b.masks, &b.tickets[1], ctx->d_ctl->counters, &ctx->d_ctl->err);
+        brick_sweep<uint16_t, false><<<b.grid[1][0], 32 * NWB_COUNT, kCountSmem, st>>>(
+            b.d_plan, 1, BrickRange{0, kAllBricks}, ctx->d_tab, b.seg_cnt, EmitOut{}, b.spill, b.masks, &b.tickets[1], ctx->d_ctl->counters, &ctx->d_ctl->err);
         CUDA_TRY(cudaGetLastError());
     }
     if (timed) CUDA_TRY(cudaEventRecord(ctx->evk[1], st));
     ScanCtl ctl;
     ctl.tiles = b.tiles; ctl.ticket = &ctx->d_ctl->ticket; ctl.err = &ctx->d_ctl->err;
     ctl.totals = ctx->d_ctl->totals; ctl.n_tiles = 0;
-    seg_scan<<<2 * ctx->num_sms, SCAN_NT, 0, st>>>(b.d_plan, b.seg_cnt, ctl, b.seg_off);
+    seg_scan<<<2 * ctx->num_sms, SCAN_NT, 0, st>>>(b.d_plan, b.seg_cnt, ctl, b.seg_off, 0ull, ~0ull);
     CUDA_TRY(cudaGetLastError());
     volume_results<<<4, 128, 0, st>>>(b.d_plan, b.seg_cnt, b.seg_off, ctx->d_ctl->totals, d_res);
     CUDA_TRY(cudaGetLastError());
@@ -1218,13 +1271,13 @@ static dmc_status enqueue_back(Ctx *ctx, BatchState &b, const brick::EmitOut &eo
     using namespace brick;
     if (timed) CUDA_TRY(cudaEventRecord(ctx->evk[3], st));
     if (all || nb[0]) {
-        brick_sweep<float, true><<<b.grid[0][1], 32 * NWB, kEmitSmem, st>>>(
-            b.d_plan, 0, ctx->d_tab, nullptr, eo, b.spill, b.masks, &b.tickets[2], ctx->d_ctl->counters, &ctx->d_ctl->err);
+        brick_sweep<float, true><<<b.grid[0][1], 32 * NWB_EMIT, kEmitSmem, st>>>(
+            b.d_plan, 0, BrickRange{0, kAllBricks}, ctx->d_tab, nullptr, eo, b.spill, b.masks, &b.tickets[2], ctx->d_ctl->counters, &ctx->d_ctl->err);
         CUDA_TRY(cudaGetLastError());
     }
     if (all || nb[1]) {
-        brick_sweep<uint16_t, true><<<b.grid[1][1], 32 * NWB, kEmitSmem, st>>>(
-            b.d_plan, 1, ctx->d_tab, nullptr, eo, b.spill, b.masks, &b.tickets[3], ctx->d_ctl->counters, &ctx->d_ctl->err);
+        brick_sweep<uint16_t, true><<<b.grid[1][1], 32 * NWB_EMIT, kEmitSmem, st>>>(
+            b.d_plan, 1, BrickRange{0, kAllBricks}, ctx->d_tab, nullptr, eo, b.spill, b.masks, &b.tickets[3], ctx->d_ctl->counters, &ctx->d_ctl->err);
         CUDA_TRY(cudaGetLastError());
     }
     if (timed) CUDA_TRY(cudaEventRecord(ctx->evk[4], st));
@@ -1308,6 +1361,7 @@ static dmc_status retarget_graph(Ctx *ctx, BatchState &b, const brick::EmitOut &
     for (uint32_t g = 0; g < 2; ++g) {
         const BatchHead *a_head = b.d_plan;
         uint32_t a_group = g;
+        BrickRange a_range{0, kAllBricks};
         const DeviceTables *a_tab = ctx->d_tab;
         uint2 *a_cnt = nullptr;
         EmitOut a_out = eo;
@@ -1316,7 +1370,7 @@ static dmc_status retarget_graph(Ctx *ctx, BatchState &b, const brick::EmitOut &
         uint32_t *a_ticket = &b.tickets[2 + g];
         unsigned long long *a_counters = ctx->d_ctl->counters;
         uint32_t *a_err = &ctx->d_ctl->err;
-        void *args[] = {&a_head, &a_group, &a_tab, &a_cnt, &a_out, &a_spill, &a_masks, &a_ticket, &a_counters, &a_err};
+        void *args[] = {&a_head, &a_group, &a_range, &a_tab, &a_cnt, &a_out, &a_spill, &a_masks, &a_ticket, &a_counters, &a_err};
         cudaKernelNodeParams kp = b.emit_params[g];
         kp.kernelParams = args;
         kp.extra = nullptr;
@@ -1326,20 +1380,12 @@ static dmc_status retarget_graph(Ctx *ctx, BatchState &b, const brick::EmitOut &
     return DMC_OK;
 }
 
-// Extraction of one or many volumes: count sweep, one segment scan over all
-// volumes, per-volume offsets, emit sweep.  Vertices and quads of volume v
-// land at its offsets in the shared output buffers; quad indices are relative
-// to the volume's first vertex.
-dmc_status brick_extract(Ctx *ctx, const BrickItem *items, uint32_t n, const BrickOut &o, cudaStream_t st)
+// Chooses the planes per brick and writes the plan (head and one Geom per
+// volume: the f32 volumes, then the u16 ones) to the pinned staging, after
+// carving the scratch for it.  nb: bricks of each sample type.
+static dmc_status stage_plan(Ctx *ctx, BatchState &b, const BrickItem *items, uint32_t n, uint64_t nb[2])
 {
     using namespace brick;
-    if (n == 0) return DMC_ERR_INVALID_ARG;
-    BatchState *bp = nullptr;
-    dmc_status s = batch_state(ctx, &bp);
-    if (s != DMC_OK) return s;
-    BatchState &b = *bp;
-    if (b.in_flight) return DMC_ERR_INVALID_ARG;
-    const int gmax = std::max(std::max(b.grid[0][0], b.grid[0][1]), std::max(b.grid[1][0], b.grid[1][1]));
     // planes per brick: long sweeps amortise the z halo, but the last wave of
     // bricks leaves warps idle, so keep at least six bricks per warp (down
     // to two planes per brick)
@@ -1351,12 +1397,13 @@ dmc_status brick_extract(Ctx *ctx, const BrickItem *items, uint32_t n, const Bri
                 const uint3 c = items[i].cells;
                 nb += (uint64_t)((c.x + W - 1) / W) * ((c.y + ROWS - 1) / ROWS) * ((c.z + zc - 1) / zc);
             }
-            if (zc <= 2 || nb >= 6ull * (uint64_t)gmax * NWB) break;
+            if (zc <= 2 || nb >= 6ull * (uint64_t)sweep_warps(b)) break;
             zc >>= 1;
         }
     }
     // descriptors: the f32 volumes, then the u16 ones (one launch per type)
-    uint64_t nseg = 0, ncoord = 0, nmask = 0, nb[2] = {0, 0};
+    uint64_t nseg = 0, ncoord = 0, nmask = 0;
+    nb[0] = nb[1] = 0;
     uint32_t nvol[2] = {0, 0};
     for (uint32_t i = 0; i < n; ++i) {
         const BrickItem &it = items[i];
@@ -1367,7 +1414,8 @@ dmc_status brick_extract(Ctx *ctx, const BrickItem *items, uint32_t n, const Bri
     }
     const uint64_t n_tiles = (nseg + SCAN_TILE - 1) / SCAN_TILE;
     if (n_tiles >= (1ull << 31)) return DMC_ERR_UNSUPPORTED;
-    if ((s = batch_layout(ctx, b, n, nseg, ncoord, nmask)) != DMC_OK) return s;
+    dmc_status s = batch_layout(ctx, b, n, nseg, ncoord, nmask);
+    if (s != DMC_OK) return s;
     BatchHead *head = (BatchHead *)b.h_stage;
     Geom *geoms = (Geom *)(head + 1);
     uint32_t pos[2] = {0, nvol[0]};
@@ -1401,6 +1449,24 @@ dmc_status brick_extract(Ctx *ctx, const BrickItem *items, uint32_t n, const Bri
     head->nvol[0] = nvol[0]; head->nvol[1] = nvol[1];
     head->n = n;
     head->n_tiles = (uint32_t)n_tiles;
+    return DMC_OK;
+}
+
+// Extraction of one or many volumes: count sweep, one segment scan over all
+// volumes, per-volume offsets, emit sweep.  Vertices and quads of volume v
+// land at its offsets in the shared output buffers; quad indices are relative
+// to the volume's first vertex.
+dmc_status brick_extract(Ctx *ctx, const BrickItem *items, uint32_t n, const BrickOut &o, cudaStream_t st)
+{
+    using namespace brick;
+    if (n == 0) return DMC_ERR_INVALID_ARG;
+    BatchState *bp = nullptr;
+    dmc_status s = batch_state(ctx, &bp);
+    if (s != DMC_OK) return s;
+    BatchState &b = *bp;
+    if (b.in_flight) return DMC_ERR_INVALID_ARG;
+    uint64_t nb[2] = {0, 0};
+    if ((s = stage_plan(ctx, b, items, n, nb)) != DMC_OK) return s;
 
     EmitOut eo;
     eo.seg_off = b.seg_off; eo.verts = o.verts; eo.vcap = o.vcap; eo.quads = o.quads; eo.qcap = o.qcap; eo.tris = o.tris;
@@ -1445,6 +1511,174 @@ dmc_status brick_extract(Ctx *ctx, const BrickItem *items, uint32_t n, const Bri
     b.in_flight = true;
     b.n_inflight = n;
     return DMC_OK;
+}
+
+static dmc_status stream_state(BatchState &b)
+{
+    using namespace brick;
+    if (b.h_snap) return DMC_OK;
+    CUDA_TRY(cudaStreamCreateWithFlags(&b.s_in, cudaStreamNonBlocking));
+    CUDA_TRY(cudaStreamCreateWithFlags(&b.s_out, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreateWithFlags(&b.ev_start, cudaEventDisableTiming));
+    for (int i = 0; i < kMaxSlabs; ++i) {
+        CUDA_TRY(cudaEventCreateWithFlags(&b.ev_in[i], cudaEventDisableTiming));
+        CUDA_TRY(cudaEventCreateWithFlags(&b.ev_tot[i], cudaEventDisableTiming));
+        CUDA_TRY(cudaEventCreateWithFlags(&b.ev_emit[i], cudaEventDisableTiming));
+    }
+    unsigned long long *h = nullptr;
+    CUDA_TRY(cudaHostAlloc((void **)&h, 4 * sizeof(unsigned long long) * kMaxSlabs, cudaHostAllocMapped));
+    b.h_snap = h;
+    CUDA_TRY(cudaHostGetDevicePointer((void **)&b.d_snap, h, 0));
+    return DMC_OK;
+}
+
+template <class T>
+static void launch_sweep(Ctx *ctx, BatchState &b, bool emit, brick::BrickRange r, const brick::EmitOut &eo,
+                         uint32_t *ticket, cudaStream_t st)
+{
+    using namespace brick;
+    const uint32_t grp = std::is_same<T, float>::value ? 0 : 1;
+    if (emit)
+        brick_sweep<T, true><<<b.grid[grp][1], 32 * NWB_EMIT, kEmitSmem, st>>>(
+            b.d_plan, grp, r, ctx->d_tab, nullptr, eo, b.spill, b.masks, ticket, ctx->d_ctl->counters, &ctx->d_ctl->err);
+    else
+        brick_sweep<T, false><<<b.grid[grp][0], 32 * NWB_COUNT, kCountSmem, st>>>(
+            b.d_plan, grp, r, ctx->d_tab, b.seg_cnt, EmitOut{}, b.spill, b.masks, ticket, ctx->d_ctl->counters, &ctx->d_ctl->err);
+}
+
+// Host volume to host mesh in z slabs, so that the upload of later slabs,
+// the sweeps of the current ones and the download of finished ones overlap
+// (one copy stream each way; the sweeps on st).  Slab i is a run of whole
+// z bricks, cell planes [z_i, z_i+1).  Its count sweep runs once the point
+// planes up to z_i+1 + 1 are on the device (the 2B/3B test of its last plane
+// reads one plane further), its scan continues the running totals, and its
+// emit sweep follows the next slab's count and scan (the quads of its last
+// plane reference cells of the next plane).  The host reads the totals after
+// each slab's scan and downloads that slab's vertex and quad ranges once its
+// emit sweep is done.  The mesh equals the unstreamed one bit for bit: same
+// bricks, same segment order, the same scan in pieces.
+dmc_status brick_run_streamed(Ctx *ctx, const ExtractArgs &a, const StreamIO &io, uint32_t slabs, bool *dev_short,
+                              cudaStream_t st)
+{
+    using namespace brick;
+    *dev_short = false;
+    BatchState *bp = nullptr;
+    dmc_status s = batch_state(ctx, &bp);
+    if (s != DMC_OK) return s;
+    BatchState &b = *bp;
+    if (b.in_flight) return DMC_ERR_INVALID_ARG;
+    if ((s = stream_state(b)) != DMC_OK) return s;
+    BrickItem it;
+    it.data = a.vol; it.dtype = a.dtype; it.pts = a.pts; it.cells = a.cells; it.iso = a.iso; it.mn = a.mn; it.rng = a.rng;
+    uint64_t nb[2] = {0, 0};
+    if ((s = stage_plan(ctx, b, &it, 1, nb)) != DMC_OK) return s;
+    BatchHead *head = (BatchHead *)b.h_stage;
+    const Geom g = *(const Geom *)(head + 1);
+    const bool f32 = a.dtype == DMC_F32;
+    // Every slab but the last spans at least two cell planes: the emit sweep
+    // of slab i reads the masks of plane z_i+1 + 1, which the count sweep of
+    // slab i+1 stores only if that plane lies in slab i+1.
+    const uint32_t max_slabs = g.zc >= 2 ? g.nzb : g.nzb / 2;
+    const uint32_t S = std::max<uint32_t>(1u, std::min<uint32_t>(std::min<uint32_t>(slabs, max_slabs), (uint32_t)kMaxSlabs));
+    const uint64_t bricks_xy = (uint64_t)g.nxs * g.nyb, segs_z = (uint64_t)a.cells.y * g.nxs;
+    uint32_t zb[kMaxSlabs + 1], z[kMaxSlabs + 1];
+    uint64_t toff[kMaxSlabs + 1];
+    // Slab sizes ramp up and down (weights 1, 2, 3, 4, ..., 4, 3, 2, 1): the
+    // first slabs are uploaded and the last ones downloaded while the link
+    // carries nothing the other way, so they are kept short.
+    const uint32_t minb = g.zc >= 2 ? 1u : 2u;
+    uint64_t wsum = 0, wc[kMaxSlabs + 1];
+    wc[0] = 0;
+    for (uint32_t i = 0; i < S; ++i) wc[i + 1] = (wsum += std::min<uint32_t>(std::min(i + 1, S - i), 4u));
+    zb[0] = 0;
+    zb[S] = g.nzb;
+    for (uint32_t i = 1; i < S; ++i)
+        zb[i] = (uint32_t)std::min<uint64_t>(std::max<uint64_t>((uint64_t)g.nzb * wc[i] / wsum, zb[i - 1] + minb),
+                                             (uint64_t)g.nzb - (uint64_t)(S - i) * minb);
+    for (uint32_t i = 0; i <= S; ++i) z[i] = std::min<uint32_t>(zb[i] * g.zc, a.cells.z);
+    toff[0] = 0;
+    for (uint32_t i = 0; i < S; ++i) toff[i + 1] = toff[i] + ((uint64_t)(z[i + 1] - z[i]) * segs_z + SCAN_TILE - 1) / SCAN_TILE;
+    head->n_tiles = (uint32_t)toff[S];   // the prep kernel clears every slab's tiles
+
+    // uploads: slab i brings the point planes up to z_i+1 + 1 not brought before
+    const uint64_t plane = (uint64_t)a.pts.x * a.pts.y * (f32 ? 4u : 2u);
+    uint8_t *dvol = (uint8_t *)const_cast<void *>(a.vol);
+    const uint8_t *hvol = (const uint8_t *)io.h_vol;
+    CUDA_TRY(cudaEventRecord(ctx->ev0, st));
+    CUDA_TRY(cudaEventRecord(b.ev_start, st));
+    CUDA_TRY(cudaStreamWaitEvent(b.s_in, b.ev_start, 0));   // earlier work on st may still read the device volume
+    CUDA_TRY(cudaStreamWaitEvent(b.s_out, b.ev_start, 0));
+    uint64_t p0 = 0;
+    for (uint32_t i = 0; i < S; ++i) {
+        const uint64_t p1 = i + 1 == S ? a.pts.z - 1ull : std::min<uint64_t>((uint64_t)z[i + 1] + 1, a.pts.z - 1ull);
+        if (p0 <= p1)
+            CUDA_TRY(cudaMemcpyAsync(dvol + p0 * plane, hvol + p0 * plane, (p1 - p0 + 1) * plane, cudaMemcpyHostToDevice, b.s_in));
+        CUDA_TRY(cudaEventRecord(b.ev_in[i], b.s_in));
+        p0 = std::max(p0, p1 + 1);
+    }
+
+    CUDA_TRY(cudaMemcpyAsync(b.d_plan, b.h_stage, b.plan_bytes, cudaMemcpyHostToDevice, st));
+    batch_prep<<<2 * ctx->num_sms, 256, 0, st>>>(b.d_plan, b.tiles, b.tickets, ctx->d_ctl);
+    CUDA_TRY(cudaGetLastError());
+    EmitOut eo;
+    eo.seg_off = b.seg_off; eo.verts = a.verts; eo.vcap = a.vcap; eo.quads = a.quads; eo.qcap = a.qcap; eo.tris = a.tris;
+    auto range = [&](uint32_t i) { return BrickRange{(uint32_t)(zb[i] * bricks_xy), (uint32_t)((zb[i + 1] - zb[i]) * bricks_xy)}; };
+    for (uint32_t i = 0; i <= S; ++i) {
+        if (i < S) {
+            CUDA_TRY(cudaStreamWaitEvent(st, b.ev_in[i], 0));
+            if (f32) launch_sweep<float>(ctx, b, false, range(i), eo, &b.tickets[4 + 3 * i], st);
+            else launch_sweep<uint16_t>(ctx, b, false, range(i), eo, &b.tickets[4 + 3 * i], st);
+            CUDA_TRY(cudaGetLastError());
+            ScanCtl ctl;
+            ctl.tiles = b.tiles + toff[i]; ctl.ticket = &b.tickets[4 + 3 * i + 2]; ctl.err = &ctx->d_ctl->err;
+            ctl.totals = ctx->d_ctl->totals; ctl.n_tiles = 0; ctl.carry = ctx->d_ctl->totals;
+            seg_scan<<<2 * ctx->num_sms, SCAN_NT, 0, st>>>(b.d_plan, b.seg_cnt, ctl, b.seg_off, (uint64_t)z[i] * segs_z,
+                                                           (uint64_t)(z[i + 1] - z[i]) * segs_z);
+            snap_totals<<<1, 32, 0, st>>>(ctx->d_ctl, b.d_snap + 4 * i);
+            CUDA_TRY(cudaGetLastError());
+            CUDA_TRY(cudaEventRecord(b.ev_tot[i], st));
+        }
+        if (i >= 1) {
+            if (f32) launch_sweep<float>(ctx, b, true, range(i - 1), eo, &b.tickets[4 + 3 * (i - 1) + 1], st);
+            else launch_sweep<uint16_t>(ctx, b, true, range(i - 1), eo, &b.tickets[4 + 3 * (i - 1) + 1], st);
+            CUDA_TRY(cudaGetLastError());
+            CUDA_TRY(cudaEventRecord(b.ev_emit[i - 1], st));
+        }
+    }
+    CUDA_TRY(cudaEventRecord(ctx->ev1, st));
+    CUDA_TRY(cudaMemcpyAsync(ctx->h_ctl, ctx->d_ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, st));
+
+    // downloads, slab by slab, as the totals come in
+    uint64_t pv = 0, pq = 0;
+    bool host_short = false, stop = false;
+    for (uint32_t i = 0; i < S; ++i) {
+        CUDA_TRY(cudaEventSynchronize(b.ev_tot[i]));
+        const volatile unsigned long long *sn = b.h_snap + 4 * i;
+        const uint64_t tv = sn[0], tq = sn[1];
+        if (sn[2]) stop = true;
+        if (tv > a.vcap || tq > a.qcap) { *dev_short = true; stop = true; }
+        if (tv > io.vcap || tq > io.qcap) { host_short = true; stop = true; }
+        if (!stop && (tv > pv || tq > pq)) {
+            CUDA_TRY(cudaStreamWaitEvent(b.s_out, b.ev_emit[i], 0));
+            if (tv > pv)
+                CUDA_TRY(cudaMemcpyAsync(io.hv + 3 * pv, a.verts + 3 * pv, 12 * (tv - pv), cudaMemcpyDeviceToHost, b.s_out));
+            if (tq > pq) {
+                CUDA_TRY(cudaMemcpyAsync(io.hq + 4 * pq, a.quads + 4 * pq, 16 * (tq - pq), cudaMemcpyDeviceToHost, b.s_out));
+                if (io.ht)
+                    CUDA_TRY(cudaMemcpyAsync(io.ht + 6 * pq, a.tris + 6 * pq, 24 * (tq - pq), cudaMemcpyDeviceToHost, b.s_out));
+            }
+        }
+        pv = tv; pq = tq;
+    }
+    CUDA_TRY(cudaStreamSynchronize(st));
+    CUDA_TRY(cudaStreamSynchronize(b.s_out));
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) == cudaSuccess) ctx->stats.device_ms = ms;
+    stats_from_ctl(ctx);
+    if (ctx->h_ctl->err & DEV_ERR_OVERFLOW) *dev_short = true;
+    if (*dev_short) return DMC_ERR_OUTPUT_OVERFLOW;
+    if ((s = ctl_status(ctx->h_ctl)) != DMC_OK) return s;
+    return host_short ? DMC_ERR_OUTPUT_OVERFLOW : DMC_OK;
 }
 
 dmc_status brick_wait(Ctx *ctx, dmc_batch_result *h_results, uint64_t *n_vertices, uint64_t *n_quads)

@@ -44,6 +44,7 @@ struct Ctx {
     void *d_vol = nullptr;             // staging for host volumes (grow-only)
     uint64_t scratch_gen = 0;          // bumped whenever scratch moves (captured graphs hold its addresses)
     uint32_t brick_zc = 0;             // planes per brick (0: automatic)
+    uint32_t stream_slabs = 0;         // host extraction in z slabs: 0 automatic, 1 never, n >= 2 n slabs
     BatchState *batch = nullptr;
     bool batch_pending = false;        // an asynchronous batch awaits dmc_batch_wait
     size_t d_vol_bytes = 0;
@@ -96,6 +97,21 @@ struct BrickOut {
 void batch_state_free(Ctx *ctx);
 
 dmc_status brick_extract(Ctx *ctx, const BrickItem *items, uint32_t n, const BrickOut &o, cudaStream_t st);
+
+// Host side of a streamed extraction: the host volume, and the caller's host
+// output buffers with their capacities (vertices, quads; triangles may be null).
+struct StreamIO {
+    const void *h_vol;
+    float *hv; uint64_t vcap;
+    uint32_t *hq; uint64_t qcap;
+    uint32_t *ht;
+};
+// Streamed host extraction in z slabs (a.vol: the device copy of the volume,
+// a.verts/quads/tris: device output buffers).  DMC_ERR_OUTPUT_OVERFLOW with
+// *dev_short set means the device buffers were too small (nothing complete was
+// downloaded; the totals are in the context's stats).
+dmc_status brick_run_streamed(Ctx *ctx, const ExtractArgs &a, const StreamIO &io, uint32_t slabs, bool *dev_short,
+                              cudaStream_t st);
 // Completes an asynchronous batch: waits for it and checks its status.
 dmc_status brick_wait(Ctx *ctx, dmc_batch_result *h_results, uint64_t *n_vertices, uint64_t *n_quads);
 dmc_status upload_tables(Ctx *ctx);

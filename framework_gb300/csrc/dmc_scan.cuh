@@ -29,6 +29,10 @@ struct ScanCtl {
     uint32_t *err;
     unsigned long long *totals;   // [0] vertices, [1] quads (written by the last tile)
     uint32_t n_tiles;
+    // optional carry-in: the scan continues from these totals (read by tile 0
+    // only, before the last tile overwrites them), so that consecutive
+    // launches over consecutive ranges form one scan
+    const unsigned long long *carry = nullptr;
 };
 
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p)
@@ -64,8 +68,8 @@ __device__ __forceinline__ void tile_prefix(const ScanCtl &c, uint32_t tile, uin
         ts[tile].agg_v = agg_v;
         ts[tile].agg_q = agg_q;
         if (tile == 0) {
-            ts[tile].inc_v = agg_v;
-            ts[tile].inc_q = agg_q;
+            ts[tile].inc_v = (c.carry ? c.carry[0] : 0ull) + agg_v;
+            ts[tile].inc_q = (c.carry ? c.carry[1] : 0ull) + agg_q;
             __threadfence();
             st_release(&ts[tile].flag, 2u);
         } else {
@@ -76,6 +80,7 @@ __device__ __forceinline__ void tile_prefix(const ScanCtl &c, uint32_t tile, uin
     if (threadIdx.x < 32) {
         const int lane = threadIdx.x;
         unsigned long long ex_v = 0, ex_q = 0;
+        if (tile == 0 && c.carry) { ex_v = c.carry[0]; ex_q = c.carry[1]; }
         if (tile > 0) {
             long long base = (long long)tile - 1;
             bool done = false;

@@ -136,6 +136,72 @@ def test_reference_shaped_module_api():
     assert _bits_equal(v, r["vertices"]) and np.array_equal(t, r["triangles"])
 
 
+def _streamed_case(kind):
+    from framework_gb300 import fields
+    if kind == "u16":
+        vol = fields.value_noise_u16((150, 70, 261), base_period=16, seed=12)
+        return fields.as_u16_numpy(vol), 32768.0
+    return fields.gaussian_blobs((140, 90, 300), seed=5).numpy(), 0.5
+
+
+def _host_out(V, Q, pinned):
+    import torch
+    if pinned:
+        return (torch.empty((V, 3), dtype=torch.float32, pin_memory=True).numpy(),
+                torch.empty((Q, 4), dtype=torch.int32, pin_memory=True).numpy(),
+                torch.empty((2 * Q, 3), dtype=torch.int32, pin_memory=True).numpy())
+    return np.empty((V, 3), np.float32), np.empty((Q, 4), np.int32), np.empty((2 * Q, 3), np.int32)
+
+
+@pytest.mark.parametrize("kind", ["u16", "f32"])
+def test_run_into_streamed(kind):
+    """dmc_run_into in z slabs (upload, extraction and download overlapped)
+    returns the unstreamed mesh bit for bit for several slab counts, with and
+    without triangles, into pinned and pageable buffers.  A fresh context
+    (no device output buffers yet), device buffers grown for a smaller mesh,
+    and host buffers that are too small all behave as unstreamed."""
+    import framework_gb300 as fg
+    host, iso = _streamed_case(kind)
+    mn, mx = (-1.0, 0.5, 2.0), (3.0, 4.0, 11.0)
+    with fg.Extractor(0) as ex:
+        ex.set_option(fg.OPT_STREAM_SLABS, 1)
+        m = ex.run(host, mn, mx, iso, triangles=True)
+        V, Q = len(m.vertices), len(m.quads)
+        assert V > 10000 and Q > 5000
+        ref = (m.vertices.view(np.uint32), m.quads, m.triangles)
+
+    def check(ex, bufs, tris=True):
+        hv, hq, ht = bufs
+        hv.fill(-1), hq.fill(-1), ht.fill(-1)
+        assert ex.run_into(host, hv, hq, ht if tris else None, mn, mx, iso) == (V, Q)
+        assert np.array_equal(hv.view(np.uint32), ref[0]) and np.array_equal(hq.view(np.uint32), ref[1])
+        if tris:
+            assert np.array_equal(ht.view(np.uint32), ref[2])
+
+    with fg.Extractor(0) as ex:
+        # device buffers grown for a small mesh first: the streamed call finds them short
+        small = host[:20, :30, :40].copy()
+        ms = ex.run(small, None, None, iso)
+        sv, sq = len(ms.vertices), len(ms.quads)
+        ex.run_into(small, np.empty((sv, 3), np.float32), np.empty((sq, 4), np.int32), None, None, None, iso)
+        for slabs in (4, 2, 3, 7, 16):
+            ex.set_option(fg.OPT_STREAM_SLABS, slabs)
+            for pinned in (True, False):
+                bufs = _host_out(V, Q, pinned)
+                check(ex, bufs)
+                check(ex, bufs, tris=False)
+            st = ex.stats()
+            assert (st["n_vertices"], st["n_quads"]) == (V, Q)
+        hv, hq, ht = _host_out(V, Q, True)
+        with pytest.raises(fg.DMCError) as e:
+            ex.run_into(host, hv[:V - 1], hq, ht, mn, mx, iso)
+        assert e.value.status == 3 and e.value.counts == (V, Q)
+        with pytest.raises(fg.DMCError) as e:
+            ex.run_into(host, hv, hq[:Q - 1], None, mn, mx, iso)
+        assert e.value.status == 3 and e.value.counts == (V, Q)
+        check(ex, (hv, hq, ht))       # usable afterwards
+
+
 def test_run_into_matches_run(extractor):
     """dmc_run_into (caller host buffers, here page-locked) gives dmc_run's mesh."""
     import torch
