@@ -174,6 +174,17 @@ __device__ __forceinline__ uint16_t elem4(uint2 v, int q)
 }
 __device__ __forceinline__ float elem4(float4 v, int q) { return q == 0 ? v.x : q == 1 ? v.y : q == 2 ? v.z : v.w; }
 
+// Two uint16 samples per word (bits 0-15 and 16-31): bits 15 and 31 of the
+// result say whether each is <= the matching half of m; mh = m | 0x80008000.
+// (mh - (v & 0x7fff7fff)) cannot borrow across the halves, and its bit 15 of
+// each half is (m >= v) over the low 15 bits; the top bits of m and v decide
+// the rest.  Only bits 15 and 31 are meaningful.
+__device__ __forceinline__ uint32_t le_u16x2(uint32_t v, uint32_t m, uint32_t mh)
+{
+    const uint32_t d = mh - (v & 0x7fff7fffu);
+    return (m & ~v) | (~(m ^ v) & d);
+}
+
 // Column masks of point plane p for the lane's columns x0+lane+32j and the two
 // halo columns x0+W, x0+W+1: bit r = sample (x, y0+r, p) below the isovalue,
 // rows 0..33.  Samples outside the volume read as 0 (their cells are never
@@ -204,6 +215,7 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
     // batched path (8 rows of loads in flight) whatever its position.
     const uint32_t rmask = nrow >= 32 ? 0xffffffffu : ((1u << nrow) - 1u);
     const uint32_t hmask = nrow > 32 ? ((1u << (nrow - 32)) - 1u) : 0u;
+    uint32_t rmask_lt = rmask, hmask_lt = hmask, rmask_le = rmask, hmask_le = hmask;
     // All 128 columns in range and rows aligned for 4-sample loads
     // (warp-uniform): lane l takes the adjacent columns 4l..4l+3 of a row in
     // one load.  Otherwise lane l takes columns l, l+32, l+64, l+96.
@@ -212,35 +224,84 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
     if (vec) {
         const T *vb = vol + (plane0 + y0) * sx + x0 + 4 * lane;
         using V = decltype(load4(vb));
+        if constexpr (std::is_same<T, uint16_t>::value) {
+            // Two samples per 32-bit word, compared by le_u16x2 against t-1
+            // (v < t <=> v <= t-1; t = 0 leaves nothing below).  Each row's
+            // result bits (15 and 31) enter the accumulators from the top,
+            // which shift right by one per row: after 16 rows, row j of the
+            // half sits at bit j (even column) and 16+j (odd column).
+            const uint32_t m_lt = (thr - 1u) & 0xffffu, m_le = (thr_le - 1u) & 0xffffu;
+            const uint32_t M_lt = m_lt * 0x10001u, M_le = m_le * 0x10001u;
+            const uint32_t MH_lt = M_lt | 0x80008000u, MH_le = M_le | 0x80008000u;
+            if (thr == 0) rmask_lt = hmask_lt = 0;
+            if (thr_le == 0) rmask_le = hmask_le = 0;
 #pragma unroll 1
-        for (uint32_t r0 = 0; r0 < 32; r0 += 8) {
-            V v[8];
+            for (uint32_t h = 0; h < 2; ++h) {
+                uint32_t ax = 0, ay = 0, bx = 0, by = 0;   // lt of columns (0,1) and (2,3); le of the same
 #pragma unroll
-            for (int i = 0; i < 8; ++i) v[i] = r0 + i < nrow ? load4(vb + (uint64_t)(r0 + i) * sx) : V{};
+                for (uint32_t r0 = 0; r0 < 16; r0 += 8) {
+                    V v[8];
 #pragma unroll
-            for (int i = 0; i < 8; ++i)
+                    for (int i = 0; i < 8; ++i) {
+                        const uint32_t r = 16 * h + r0 + i;
+                        v[i] = r < nrow ? load4(vb + (uint64_t)r * sx) : V{};
+                    }
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        ax = (ax >> 1) | (le_u16x2(v[i].x, M_lt, MH_lt) & 0x80008000u);
+                        ay = (ay >> 1) | (le_u16x2(v[i].y, M_lt, MH_lt) & 0x80008000u);
+                        bx = (bx >> 1) | (le_u16x2(v[i].x, M_le, MH_le) & 0x80008000u);
+                        by = (by >> 1) | (le_u16x2(v[i].y, M_le, MH_le) & 0x80008000u);
+                    }
+                }
+                const uint32_t sh = 16 * h;
+                lo[0] |= (ax & 0xffffu) << sh; lo[1] |= (ax >> 16) << sh;
+                lo[2] |= (ay & 0xffffu) << sh; lo[3] |= (ay >> 16) << sh;
+                elo[0] |= (bx & 0xffffu) << sh; elo[1] |= (bx >> 16) << sh;
+                elo[2] |= (by & 0xffffu) << sh; elo[3] |= (by >> 16) << sh;
+            }
+            uint32_t ax = 0, ay = 0, bx = 0, by = 0;      // rows 32, 33 end at bits 14, 15 (30, 31)
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const V v = 32u + i < nrow ? load4(vb + (uint64_t)(32 + i) * sx) : V{};
+                ax = (ax >> 1) | (le_u16x2(v.x, M_lt, MH_lt) & 0x80008000u);
+                ay = (ay >> 1) | (le_u16x2(v.y, M_lt, MH_lt) & 0x80008000u);
+                bx = (bx >> 1) | (le_u16x2(v.x, M_le, MH_le) & 0x80008000u);
+                by = (by >> 1) | (le_u16x2(v.y, M_le, MH_le) & 0x80008000u);
+            }
+            hi[0] = (ax >> 14) & 3u; hi[1] = ax >> 30; hi[2] = (ay >> 14) & 3u; hi[3] = ay >> 30;
+            ehi[0] = (bx >> 14) & 3u; ehi[1] = bx >> 30; ehi[2] = (by >> 14) & 3u; ehi[3] = by >> 30;
+        } else {
+#pragma unroll 1
+            for (uint32_t r0 = 0; r0 < 32; r0 += 8) {
+                V v[8];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) v[i] = r0 + i < nrow ? load4(vb + (uint64_t)(r0 + i) * sx) : V{};
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const T t = elem4(v[i], q);
+                        lo[q] |= below(t, iso, thr) << (r0 + i);
+                        elo[q] |= at_or_below(t, iso, thr_le) << (r0 + i);
+                    }
+            }
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const V v = 32u + i < nrow ? load4(vb + (uint64_t)(32 + i) * sx) : V{};
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    const T t = elem4(v[i], q);
-                    lo[q] |= below(t, iso, thr) << (r0 + i);
-                    elo[q] |= at_or_below(t, iso, thr_le) << (r0 + i);
+                    const T t = elem4(v, q);
+                    hi[q] |= below(t, iso, thr) << i;
+                    ehi[q] |= at_or_below(t, iso, thr_le) << i;
                 }
-        }
-#pragma unroll
-        for (int i = 0; i < 2; ++i) {
-            const V v = 32u + i < nrow ? load4(vb + (uint64_t)(32 + i) * sx) : V{};
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const T t = elem4(v, q);
-                hi[q] |= below(t, iso, thr) << i;
-                ehi[q] |= at_or_below(t, iso, thr_le) << i;
             }
         }
         // columns 4l..4l+3: two 16-byte stores per mask
-        const uint4 t0 = make_uint4(lo[0] & rmask, hi[0] & hmask, lo[1] & rmask, hi[1] & hmask);
-        const uint4 t1 = make_uint4(lo[2] & rmask, hi[2] & hmask, lo[3] & rmask, hi[3] & hmask);
-        const uint4 e0 = make_uint4(elo[0] & rmask, ehi[0] & hmask, elo[1] & rmask, ehi[1] & hmask);
-        const uint4 e1 = make_uint4(elo[2] & rmask, ehi[2] & hmask, elo[3] & rmask, ehi[3] & hmask);
+        const uint4 t0 = make_uint4(lo[0] & rmask_lt, hi[0] & hmask_lt, lo[1] & rmask_lt, hi[1] & hmask_lt);
+        const uint4 t1 = make_uint4(lo[2] & rmask_lt, hi[2] & hmask_lt, lo[3] & rmask_lt, hi[3] & hmask_lt);
+        const uint4 e0 = make_uint4(elo[0] & rmask_le, ehi[0] & hmask_le, elo[1] & rmask_le, ehi[1] & hmask_le);
+        const uint4 e1 = make_uint4(elo[2] & rmask_le, ehi[2] & hmask_le, elo[3] & rmask_le, ehi[3] & hmask_le);
         uint4 *lt4 = reinterpret_cast<uint4 *>(&m.lt[4 * lane]), *le4 = reinterpret_cast<uint4 *>(&m.le[4 * lane]);
         lt4[0] = t0; lt4[1] = t1; le4[0] = e0; le4[1] = e1;
         if (gm) {   // all 128 columns are in the volume here, so ncolr >= 128
