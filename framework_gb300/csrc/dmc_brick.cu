@@ -188,8 +188,10 @@ __device__ __forceinline__ uint32_t le_u16x2(uint32_t v, uint32_t m, uint32_t mh
 // Column masks of point plane p for the lane's columns x0+lane+32j and the two
 // halo columns x0+W, x0+W+1: bit r = sample (x, y0+r, p) below the isovalue,
 // rows 0..33.  Samples outside the volume read as 0 (their cells are never
-// active).  Loads go out 32 per lane before their results are used, and the
-// next plane's rows are prefetched into L2.  With gm set, the masks also go
+// active).  Loads go out 8 rows per lane before their results are used; the
+// next plane is not prefetched into L2 (all resident warps' planes together
+// outrun the L2, and prefetched lines were evicted before their use, which
+// read the volume 1.9 times instead of 1.35).  With gm set, the masks also go
 // to the mask store chunk gm (ncolr columns per mask).
 template <class T>
 __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint32_t thr, uint32_t thr_le, uint32_t x0,
@@ -201,15 +203,6 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
     const uint32_t nrow = pz ? min(34u, pts.y - y0) : 0u;
     const uint64_t sx = pts.x;
     const uint64_t plane0 = (uint64_t)p * pts.y;
-    if (p + 1 < pts.z && (uint32_t)lane < nrow) {
-        // next plane, this lane's row: the lines of the brick's own columns.
-        // The two halo columns are left to demand loads: prefetching their
-        // line would pull in a whole line of the next brick's columns, which
-        // is usually evicted before that brick is swept.
-        const char *nxt = reinterpret_cast<const char *>(vol + (plane0 + pts.y + y0 + lane) * sx + x0);
-        const uint32_t bytes = min((uint32_t)W, pts.x - x0) * (uint32_t)sizeof(T);
-        for (uint32_t o = 0; o < bytes; o += 128) asm volatile("prefetch.global.L2 [%0];" ::"l"(nxt + o));
-    }
     // Rows past the volume (or past 34) and columns past it give 0 bits: the
     // loads are predicated and the bits masked, so every brick takes the same
     // batched path (8 rows of loads in flight) whatever its position.
@@ -369,23 +362,6 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
             m.le[W + hc] = e;
             if (gm && W + hc < ncolr) { gm[W + hc] = t; gm[ncolr + W + hc] = e; }
         }
-    }
-}
-
-// L2 prefetch of the brick's 33 sample rows (own columns) of point plane p,
-// which the corner gathers of the emit sweep read.  Every address lies in
-// the row: its first byte, then the starts of the following 128-byte lines.
-template <class T>
-__device__ __forceinline__ void prefetch_rows(const T *vol, uint3 pts, uint32_t x0, uint32_t y0, uint32_t p, int lane)
-{
-    const uint32_t nrow = min((uint32_t)HROWS, pts.y - y0);
-    const uint32_t bytes = min((uint32_t)W, pts.x - x0) * (uint32_t)sizeof(T);
-    for (uint32_t r = lane; r < nrow; r += 32) {
-        const char *row = reinterpret_cast<const char *>(vol + ((uint64_t)p * pts.y + y0 + r) * pts.x + x0);
-        const uintptr_t a = reinterpret_cast<uintptr_t>(row), end = a + bytes;
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(row));
-        for (uintptr_t l = (a & ~(uintptr_t)127) + 128; l < end; l += 128)
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(l));
     }
 }
 
@@ -721,14 +697,13 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 4) brick_sweep(cons
         // masks from the samples and keeps them in the mask store (each
         // plane once: a brick's last plane only when it is the volume's
         // last).  The emit sweep copies them back, one plane ahead, and reads
-        // samples only for the corner gathers, prefetched into L2.
+        // samples only for its corner gathers (demand loads: an L2 prefetch
+        // of whole planes read 1.9 times the bytes the gathers need).
         const uint32_t ncolr = mask_cols(g, x0);
         if (EMIT) {
             fetch_masks(masks, g, xs, yb, x0, z0, S.mask[z0 & 1], &S.mbar[z0 & 1], lane);
             fetch_masks(masks, g, xs, yb, x0, z0 + 1, S.mask[(z0 + 1) & 1], &S.mbar[(z0 + 1) & 1], lane);
             pend = 3u;
-            prefetch_rows(vol, g.pts, x0, y0, z0, lane);
-            prefetch_rows(vol, g.pts, x0, y0, z0 + 1, lane);
             if (!wait_slot(z0 & 1)) return;
         } else {
             load_plane<T>(vol, g.pts, g.iso, g.iso_u16, g.isole_u16, x0, y0, z0, S.mask[z0 & 1], lane,
@@ -751,7 +726,6 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 4) brick_sweep(cons
                         S.segv[cur][r][0] = own.x; S.segv[cur][r][1] = nxt.x; S.segq[cur][r] = own.y;
                     }
                     if (!wait_slot((k + 1) & 1)) return;
-                    if (k + 2 <= z1) prefetch_rows(vol, g.pts, x0, y0, k + 2, lane);
                 } else {
                     const bool keep = k + 1 < z1 || z1 == g.cells.z;
                     load_plane<T>(vol, g.pts, g.iso, g.iso_u16, g.isole_u16, x0, y0, k + 1, S.mask[(k + 1) & 1], lane,
