@@ -103,7 +103,8 @@ struct alignas(16) WarpSmem : SweepSmem {
     uint16_t lst1[CAP];                // list of plane slot 1
     uint32_t segv[2][HROWS][2];        // vertex offset of (row, own / next segment)
     uint32_t segq[2][HROWS];           // quad offset of (row, own segment)
-    uint32_t qwork[QBUF];              // quads of one round: entry | edge << 16 | wanted edges << 18
+    uint32_t qwork[QBUF];              // quads of one round of owner cells: owner lane | edge << 5 | wanted edges << 7
+    uint4 orec[32];                    // owners of the round, by lane: (entry | rank r1 << 16, r2 | r3 << 16, first quad, cell | info << 16)
     uint32_t ent[2][CAP];              // packed cell: vrel 11 | qrel 10 | cfg 8 | lut2 1
     uint8_t info[2][CAP];              // own-edge bipolar/ccw bits
     uint64_t mbar[2];                  // completion of the bulk copies into mask[0] / mask[1]
@@ -875,12 +876,31 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 4) brick_sweep(cons
                         const int r = e >> 8, c = e & 0xff;
                         if (r < ROWS && c < W) {
                             const uint32_t x = x0 + c, y = y0 + r;
-                            const uint32_t cfg = cell_cfg(M.ent(prv, i));
+                            const uint32_t d = M.ent(prv, i);
+                            const uint32_t cfg = cell_cfg(d);
                             const uint32_t info = M.info(prv, i);
 #pragma unroll
                             for (int s = 0; s < 3; ++s)
                                 if ((info & (1u << s)) && owned_quad_in_volume(s, x, y, kp, g.cells) && owned_sign_change(cfg, s))
                                     want |= 1u << s;
+                            if (want) {
+                                // The ring cells of the owner's quads, by list index: the
+                                // owner (c, r) of plane k-1, (c, r+1) of plane k-1, (c, r)
+                                // and (c, r+1) of plane k, each possibly followed by its
+                                // +x neighbour, the next entry of its row.  The three
+                                // ranks are taken once here for all of the owner's quads.
+                                const uint32_t qc = (uint32_t)c >> 5, bm = (1u << (c & 31)) - 1u;
+                                const uint32_t m0 = qc > 0 ? ~0u : bm, m1 = qc > 1 ? ~0u : (qc == 1 ? bm : 0u);
+                                const uint32_t m2 = qc > 2 ? ~0u : (qc == 2 ? bm : 0u), m3 = qc == 3 ? bm : 0u;
+                                auto rank = [&](int pl, int rr) -> uint32_t {
+                                    const uint4 w = *reinterpret_cast<const uint4 *>(S.xrow[pl][rr]);
+                                    return S.rowstart[pl][rr] + __popc(w.x & m0) + __popc(w.y & m1) + __popc(w.z & m2) +
+                                           __popc(w.w & m3);
+                                };
+                                const uint32_t r1 = rank(prv, r + 1), r2 = rank(cur, r), r3 = rank(cur, r + 1);
+                                S.orec[lane] = make_uint4(i | (r1 << 16), r2 | (r3 << 16), S.segq[prv][r] + cell_qrel(d),
+                                                          e | (info << 16));
+                            }
                         }
                     }
                     const uint32_t nq = __popc(want);
@@ -891,32 +911,24 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 4) brick_sweep(cons
                         while (w) {
                             const int s = __ffs(w) - 1;
                             w &= w - 1;
-                            S.qwork[pos++] = i | ((uint32_t)s << 16) | (want << 18);
+                            S.qwork[pos++] = (uint32_t)lane | ((uint32_t)s << 5) | (want << 7);
                         }
                     }
                     __syncwarp();
                     for (uint32_t qb = 0; qb < qtot; qb += 32) {
                         if (qb + lane < qtot) {
                             const uint32_t item = S.qwork[qb + lane];
-                            const uint32_t oi = item & 0xffffu;
-                            const int s = (int)((item >> 16) & 3u);
-                            const uint32_t owant = item >> 18;
-                            const uint32_t e = M.lst(prv, oi);
-                            const int r = e >> 8, c = e & 0xff;
-                            const uint32_t d = M.ent(prv, oi);
-                            const uint32_t info = M.info(prv, oi);
-                            const uint64_t q = (uint64_t)S.segq[prv][r] + cell_qrel(d) + __popc(owant & ((1u << s) - 1u));
+                            const int s = (int)((item >> 5) & 3u);
+                            const uint32_t owant = item >> 7;
+                            const uint4 o = S.orec[item & 31u];
+                            const int r = (o.w >> 8) & 0xff, c = o.w & 0xff;
+                            const uint32_t info = o.w >> 16;
+                            const uint64_t q = (uint64_t)o.z + __popc(owant & ((1u << s) - 1u));
                             if (q >= out.qcap) {
                                 atomicOr(err, DEV_ERR_OVERFLOW);
                             } else {
                                 const uint32_t ring = s == 0 ? kRing6 : (s == 1 ? kRing9 : kRing10);
                                 const bool ccw = (info >> (s + 3)) & 1u;
-                                // The four ring cells are ranked independently (their
-                                // lookups overlap); each rank is branch-free: the list
-                                // start of its row plus the active cells left of column c.
-                                const uint32_t qc = (uint32_t)c >> 5, bm = (1u << (c & 31)) - 1u;
-                                const uint32_t m0 = qc > 0 ? ~0u : bm, m1 = qc > 1 ? ~0u : (qc == 1 ? bm : 0u);
-                                const uint32_t m2 = qc > 2 ? ~0u : (qc == 2 ? bm : 0u), m3 = qc == 3 ? bm : 0u;
                                 uint32_t idx[4];
                                 bool bad = false;
 #pragma unroll
@@ -925,10 +937,10 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 4) brick_sweep(cons
                                     const uint32_t sl = (ring >> (8 * kk)) & 0xffu;
                                     const int pl = (sl & 1u) ? cur : prv;
                                     const uint32_t plus = (sl >> 3) & 1u, rr = (uint32_t)r + ((sl >> 4) & 1u);
-                                    // ring cell (c + plus, rr) of plane pl follows (c, rr) in its list
-                                    const uint4 w = *reinterpret_cast<const uint4 *>(S.xrow[pl][rr]);
-                                    const uint32_t li = S.rowstart[pl][rr] + __popc(w.x & m0) + __popc(w.y & m1) +
-                                                        __popc(w.z & m2) + __popc(w.w & m3) + plus;
+                                    // base entry (sl bits 1-2): owner, r1, r2, r3; then its +x neighbour
+                                    const uint32_t bsel = (sl >> 1) & 3u;
+                                    const uint32_t bw = bsel < 2 ? o.x : o.y;
+                                    const uint32_t li = ((bsel & 1u) ? (bw >> 16) : (bw & 0xffffu)) + plus;
                                     const bool ok = li < S.rowstart[pl][HROWS];
                                     const uint32_t rd = ok ? M.ent(pl, li) : 0u;
                                     const uint32_t m = lut_m(tab, cell_cfg(rd), cell_l2(rd), (int)ring_edge(s, kk));
@@ -938,7 +950,7 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 4) brick_sweep(cons
                                 if (bad) atomicOr(err, DEV_ERR_BOUNDS);
                                 reinterpret_cast<uint4 *>(out.quads)[q] = make_uint4(idx[0], idx[1], idx[2], idx[3]);
                                 if (out.tris) {
-                                    uint32_t *tp = out.tris + 6 * q;
+                                    uint32_t *tp = out.tris + 6 * q;   // 4-byte stores: callers' buffers need only 4-byte alignment
                                     tp[0] = idx[0]; tp[1] = idx[1]; tp[2] = idx[2];
                                     tp[3] = idx[2]; tp[4] = idx[3]; tp[5] = idx[0];
                                 }
