@@ -47,7 +47,7 @@ constexpr int NWB_EMIT = 8;               // of the emit sweep: 2 blocks per SM
 constexpr int nwb(bool emit) { return emit ? NWB_EMIT : NWB_COUNT; }
 constexpr int kMaxSlabs = 16;             // z slabs of a streamed host extraction
 constexpr int QBUF = 96;                  // quads of one round of owner cells (3 per cell)
-constexpr int SCAN_NT = 256, SCAN_ITEMS = 8, SCAN_TILE = SCAN_NT * SCAN_ITEMS;
+constexpr int SCAN_NT = 512, SCAN_ITEMS = 8, SCAN_TILE = SCAN_NT * SCAN_ITEMS;   // 4096 segments per tile: half the look-back chain of 2048
 
 // One volume of an extraction (a plain call has one, a batch many).
 struct Geom {
