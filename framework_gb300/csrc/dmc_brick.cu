@@ -1534,8 +1534,21 @@ dmc_status brick_extract(Ctx *ctx, const BrickItem *items, uint32_t n, const Bri
     } else {
         if ((s = enqueue_front(ctx, b, d_res, true, nb, false, st)) != DMC_OK) return s;
         ctx->evk_used = 1;
-        // totals decide whether the caller's buffers are large enough; the
-        // per-volume offsets are final already
+        if (!o.sizing_only) {
+            // The emit sweep follows at once: it checks every write against the
+            // capacities on the device, so no host round trip sits between the
+            // sweeps.  Too small buffers give DMC_ERR_OUTPUT_OVERFLOW with the
+            // totals (their contents are then undefined).
+            if ((s = enqueue_back(ctx, b, eo, d_res, true, nb, false, st)) != DMC_OK) return s;
+            ctx->evk_used = 2;
+            CUDA_TRY(cudaStreamSynchronize(st));
+            stats_from_ctl(ctx);
+            if (o.n_vertices) *o.n_vertices = ctx->h_ctl->totals[0];
+            if (o.n_quads) *o.n_quads = ctx->h_ctl->totals[1];
+            if (o.h_results) std::copy(stage_results(b), stage_results(b) + n, o.h_results);
+            return ctl_status(ctx->h_ctl);
+        }
+        // sizing: the totals and the per-volume offsets are final after the scan
         CUDA_TRY(cudaMemcpyAsync(ctx->h_ctl, ctx->d_ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaMemcpyAsync(stage_results(b), d_res, sizeof(dmc_batch_result) * (size_t)n, cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
@@ -1546,13 +1559,7 @@ dmc_status brick_extract(Ctx *ctx, const BrickItem *items, uint32_t n, const Bri
         if (o.n_quads) *o.n_quads = Q;
         if (V >= 0xFFFFFFFFull || Q >= 0xFFFFFFFFull) return DMC_ERR_OUTPUT_OVERFLOW;
         if (o.h_results) std::copy(stage_results(b), stage_results(b) + n, o.h_results);
-        if (o.sizing_only) return DMC_OK;
-        if (V > o.vcap || Q > o.qcap) return DMC_ERR_OUTPUT_OVERFLOW;
-        if ((s = enqueue_back(ctx, b, eo, d_res, true, nb, false, st)) != DMC_OK) return s;
-        ctx->evk_used = 2;
-        CUDA_TRY(cudaStreamSynchronize(st));
-        stats_from_ctl(ctx);
-        return ctl_status(ctx->h_ctl);
+        return DMC_OK;
     }
     CUDA_TRY(cudaEventRecord(b.done, st));
     b.in_flight = true;

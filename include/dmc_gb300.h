@@ -137,7 +137,8 @@ void dmc_mesh_free(dmc_mesh *mesh);
  * buffers are caller-owned device memory with the given capacities (in
  * vertices / quads).  d_triangles may be NULL.  On DMC_ERR_OUTPUT_OVERFLOW the
  * counts are still reported in *n_vertices / *n_quads so the caller can
- * retry.  With all three output pointers NULL the call only counts: it
+ * retry; writes stay within the capacities, and the buffers' contents are
+ * undefined.  With all three output pointers NULL the call only counts: it
  * returns DMC_OK with the totals and writes no mesh.  num_smooth > 0 smooths
  * as dmc_run does and needs d_quads along with d_vertices.  `stream` is a
  * cudaStream_t (NULL: the context's stream).  The call returns after the mesh
@@ -209,8 +210,9 @@ typedef struct {
  * NULL).
  *
  * flags == 0: returns when the meshes are complete, with the totals in
- * *n_vertices / *n_quads; DMC_ERR_OUTPUT_OVERFLOW (no mesh written, totals
- * and results still reported) when they exceed the capacities.  With all
+ * *n_vertices / *n_quads; DMC_ERR_OUTPUT_OVERFLOW (totals and results still
+ * reported; every write stays within the capacities, but the buffers' contents
+ * are undefined) when they exceed the capacities.  With all
  * three output pointers NULL the call only counts: DMC_OK, totals and
  * per-volume results, no mesh.  DMC_BATCH_ASYNC / DMC_BATCH_GRAPH: enqueue on
  * `stream` and return at once; results, n_vertices and n_quads may be NULL and
