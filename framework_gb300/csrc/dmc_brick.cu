@@ -1433,9 +1433,9 @@ static dmc_status retarget_graph(Ctx *ctx, BatchState &b, const brick::EmitOut &
 static dmc_status stage_plan(Ctx *ctx, BatchState &b, const BrickItem *items, uint32_t n, uint64_t nb[2])
 {
     using namespace brick;
-    // planes per brick: long sweeps amortise the z halo, but the last wave of
-    // bricks leaves warps idle, so keep at least six bricks per warp (down
-    // to two planes per brick)
+    // planes per brick: long sweeps amortise the z halo, but uneven bricks
+    // leave warps idle at the end, so keep at least twelve bricks per resident
+    // warp (down to two planes per brick; 4 on a 1024^3 volume)
     uint32_t zc = ctx->brick_zc ? ctx->brick_zc : 32;
     if (!ctx->brick_zc) {
         for (;;) {
@@ -1444,7 +1444,7 @@ static dmc_status stage_plan(Ctx *ctx, BatchState &b, const BrickItem *items, ui
                 const uint3 c = items[i].cells;
                 nb += (uint64_t)((c.x + W - 1) / W) * ((c.y + ROWS - 1) / ROWS) * ((c.z + zc - 1) / zc);
             }
-            if (zc <= 2 || nb >= 6ull * (uint64_t)sweep_warps(b)) break;
+            if (zc <= 2 || nb >= 12ull * (uint64_t)sweep_warps(b)) break;
             zc >>= 1;
         }
     }
