@@ -742,54 +742,69 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 4) brick_sweep(cons
                 }
                 uint64_t hact = 0;
                 if (EMIT && lane == 0 && x0 + W < g.cells.x) hact = active_rows(mk[W], mk[W + 1], mk1[W], mk1[W + 1]) & rowmask;
-                // bit transpose: lane r gets row r's active cells in x order
-                uint32_t xr[GROUPS], x32[GROUPS];
-                uint32_t cnt = 0, cnt32 = 0;
-#pragma unroll
-                for (int j = 0; j < GROUPS; ++j) {
-                    xr[j] = warp_transpose32((uint32_t)act[j], lane);
-                    cnt += __popc(xr[j]);
-                    x32[j] = EMIT ? __ballot_sync(0xffffffffu, (act[j] >> 32) & 1ull) : 0u;
-                    cnt32 += __popc(x32[j]);
-                }
-                if (EMIT) {
-                    hact = __shfl_sync(0xffffffffu, hact, 0);
-                    cnt += (uint32_t)((hact >> lane) & 1ull);
-                    cnt32 += (uint32_t)((hact >> 32) & 1ull);
-                }
-                *reinterpret_cast<uint4 *>(S.xrow[cur][lane]) = make_uint4(xr[0], xr[1], xr[2], xr[3]);
-                if (EMIT && lane == 0) *reinterpret_cast<uint4 *>(S.xrow[cur][32]) = make_uint4(x32[0], x32[1], x32[2], x32[3]);
-                const uint32_t inc = warp_incl_scan(cnt, lane);
-                const uint32_t tot32 = __shfl_sync(0xffffffffu, inc, 31);
-                const uint32_t start = inc - cnt;
-                S.rowstart[cur][lane] = (uint16_t)start;
-                if (lane == 0) { S.rowstart[cur][32] = (uint16_t)tot32; S.rowstart[cur][33] = (uint16_t)(tot32 + cnt32); S.hact[cur] = hact; }
-                L = tot32 + cnt32;
-                // lane r lists row r in x order (lane 0 also row 32)
-                {
-                    uint32_t pos = start;
-#pragma unroll
-                    for (int j = 0; j < GROUPS; ++j) {
-                        uint32_t w = xr[j];
-                        while (w) {
-                            const int l = __ffs(w) - 1;
-                            w &= w - 1;
-                            M.lst(lp, pos++) = (uint16_t)((lane << 8) | (32 * j + l));
-                        }
+                // emit sweep: a plane without active cells (common on sparse
+                // surfaces) skips the transposes, the scan and the list (in
+                // the count sweep the extra branch cost more than it saved)
+                const bool any_act = !EMIT || __any_sync(0xffffffffu, (act[0] | act[1] | act[2] | act[3] | hact) != 0ull);
+                if (!any_act) {
+                    *reinterpret_cast<uint4 *>(S.xrow[cur][lane]) = make_uint4(0u, 0u, 0u, 0u);
+                    S.rowstart[cur][lane] = 0;
+                    if (lane == 0) {
+                        if (EMIT) *reinterpret_cast<uint4 *>(S.xrow[cur][32]) = make_uint4(0u, 0u, 0u, 0u);
+                        S.rowstart[cur][32] = 0;
+                        S.rowstart[cur][33] = 0;
+                        S.hact[cur] = 0;
                     }
-                    if (EMIT && ((hact >> lane) & 1ull)) M.lst(lp, pos++) = (uint16_t)((lane << 8) | W);
-                    if (EMIT && lane == 0) {
-                        pos = tot32;
-#pragma unroll
+                } else {
+                    // bit transpose: lane r gets row r's active cells in x order
+                    uint32_t xr[GROUPS], x32[GROUPS];
+                    uint32_t cnt = 0, cnt32 = 0;
+    #pragma unroll
+                    for (int j = 0; j < GROUPS; ++j) {
+                        xr[j] = warp_transpose32((uint32_t)act[j], lane);
+                        cnt += __popc(xr[j]);
+                        x32[j] = EMIT ? __ballot_sync(0xffffffffu, (act[j] >> 32) & 1ull) : 0u;
+                        cnt32 += __popc(x32[j]);
+                    }
+                    if (EMIT) {
+                        hact = __shfl_sync(0xffffffffu, hact, 0);
+                        cnt += (uint32_t)((hact >> lane) & 1ull);
+                        cnt32 += (uint32_t)((hact >> 32) & 1ull);
+                    }
+                    *reinterpret_cast<uint4 *>(S.xrow[cur][lane]) = make_uint4(xr[0], xr[1], xr[2], xr[3]);
+                    if (EMIT && lane == 0) *reinterpret_cast<uint4 *>(S.xrow[cur][32]) = make_uint4(x32[0], x32[1], x32[2], x32[3]);
+                    const uint32_t inc = warp_incl_scan(cnt, lane);
+                    const uint32_t tot32 = __shfl_sync(0xffffffffu, inc, 31);
+                    const uint32_t start = inc - cnt;
+                    S.rowstart[cur][lane] = (uint16_t)start;
+                    if (lane == 0) { S.rowstart[cur][32] = (uint16_t)tot32; S.rowstart[cur][33] = (uint16_t)(tot32 + cnt32); S.hact[cur] = hact; }
+                    L = tot32 + cnt32;
+                    // lane r lists row r in x order (lane 0 also row 32)
+                    {
+                        uint32_t pos = start;
+    #pragma unroll
                         for (int j = 0; j < GROUPS; ++j) {
-                            uint32_t w = x32[j];
+                            uint32_t w = xr[j];
                             while (w) {
                                 const int l = __ffs(w) - 1;
                                 w &= w - 1;
-                                M.lst(lp, pos++) = (uint16_t)((32 << 8) | (32 * j + l));
+                                M.lst(lp, pos++) = (uint16_t)((lane << 8) | (32 * j + l));
                             }
                         }
-                        if ((hact >> 32) & 1ull) M.lst(lp, pos++) = (uint16_t)((32 << 8) | W);
+                        if (EMIT && ((hact >> lane) & 1ull)) M.lst(lp, pos++) = (uint16_t)((lane << 8) | W);
+                        if (EMIT && lane == 0) {
+                            pos = tot32;
+    #pragma unroll
+                            for (int j = 0; j < GROUPS; ++j) {
+                                uint32_t w = x32[j];
+                                while (w) {
+                                    const int l = __ffs(w) - 1;
+                                    w &= w - 1;
+                                    M.lst(lp, pos++) = (uint16_t)((32 << 8) | (32 * j + l));
+                                }
+                            }
+                            if ((hact >> 32) & 1ull) M.lst(lp, pos++) = (uint16_t)((32 << 8) | W);
+                        }
                     }
                 }
                 __syncwarp();
