@@ -42,7 +42,8 @@ constexpr int HROWS = ROWS + 1;           // with the halo row
 constexpr int MAXL = HROWS * (W + 1);     // most active cells one plane of a brick can hold
 constexpr int CAP = 256;                  // entries kept in shared memory per plane
 constexpr int OVF = MAXL - CAP;           // entries per plane that spill to global scratch
-constexpr int NWB_COUNT = 8;              // warps per block of the count sweep (independent): 4 blocks per SM
+constexpr int NWB_COUNT = 8;              // warps per block of the count sweep (independent): 3 blocks per SM at 80
+                                          // registers (4 blocks at 64 spilled and ran 10% slower)
 constexpr int NWB_EMIT = 8;               // of the emit sweep: 2 blocks per SM
 constexpr int nwb(bool emit) { return emit ? NWB_EMIT : NWB_COUNT; }
 constexpr int kMaxSlabs = 16;             // z slabs of a streamed host extraction
@@ -629,7 +630,7 @@ __device__ __forceinline__ uint32_t ring_edge(int s, int kk)
 // Active cells are compacted per plane in output order and processed 32 at a
 // time, one per lane; quads are compacted the same way.
 template <class T, bool EMIT>
-__global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 4) brick_sweep(const BatchHead *__restrict__ head, uint32_t group,
+__global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 3) brick_sweep(const BatchHead *__restrict__ head, uint32_t group,
                                                         BrickRange range, const DeviceTables *__restrict__ tabp,
                                                         uint2 *__restrict__ seg_cnt, EmitOut out,
                                                         Spill *__restrict__ spill, uint64_t *masks, uint32_t *ticket,
