@@ -122,20 +122,42 @@ struct Spill {                          // per warp slot, global memory
     uint8_t info[2][OVF];
 };
 
+// A plane's entries: the first CAP in shared memory, the rest in the warp's
+// global spill slot.  Separate shared and global accesses (rather than one
+// reference that may point to either) keep the common case on shared-memory
+// instructions.
 struct WarpMem {
     WarpSmem *s;
     Spill *g;
-    __device__ __forceinline__ uint32_t &ent(int p, uint32_t i)
+    __device__ __forceinline__ uint32_t ent(int p, uint32_t i) const
     {
-        return i < CAP ? s->ent[p][i] : g->ent[p][i - CAP];
+        uint32_t v;
+        if (i < CAP) v = s->ent[p][i]; else v = g->ent[p][i - CAP];
+        return v;
     }
-    __device__ __forceinline__ uint16_t &lst(int p, uint32_t i)
+    __device__ __forceinline__ void set_ent(int p, uint32_t i, uint32_t v)
     {
-        return i < CAP ? (p ? s->lst1 : s->lst0)[i] : g->lst[p][i - CAP];
+        if (i < CAP) s->ent[p][i] = v; else g->ent[p][i - CAP] = v;
     }
-    __device__ __forceinline__ uint8_t &info(int p, uint32_t i)
+    __device__ __forceinline__ uint32_t lst(int p, uint32_t i) const
     {
-        return i < CAP ? s->info[p][i] : g->info[p][i - CAP];
+        uint32_t v;
+        if (i < CAP) v = (p ? s->lst1 : s->lst0)[i]; else v = g->lst[p][i - CAP];
+        return v;
+    }
+    __device__ __forceinline__ void set_lst(int p, uint32_t i, uint32_t v)
+    {
+        if (i < CAP) (p ? s->lst1 : s->lst0)[i] = (uint16_t)v; else g->lst[p][i - CAP] = (uint16_t)v;
+    }
+    __device__ __forceinline__ uint32_t info(int p, uint32_t i) const
+    {
+        uint32_t v;
+        if (i < CAP) v = s->info[p][i]; else v = g->info[p][i - CAP];
+        return v;
+    }
+    __device__ __forceinline__ void set_info(int p, uint32_t i, uint32_t v)
+    {
+        if (i < CAP) s->info[p][i] = (uint8_t)v; else g->info[p][i - CAP] = (uint8_t)v;
     }
 };
 
@@ -789,10 +811,10 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 3) brick_sweep(cons
                             while (w) {
                                 const int l = __ffs(w) - 1;
                                 w &= w - 1;
-                                M.lst(lp, pos++) = (uint16_t)((lane << 8) | (32 * j + l));
+                                M.set_lst(lp, pos++, (lane << 8) | (32 * j + l));
                             }
                         }
-                        if (EMIT && ((hact >> lane) & 1ull)) M.lst(lp, pos++) = (uint16_t)((lane << 8) | W);
+                        if (EMIT && ((hact >> lane) & 1ull)) M.set_lst(lp, pos++, (lane << 8) | W);
                         if (EMIT && lane == 0) {
                             pos = tot32;
     #pragma unroll
@@ -801,10 +823,10 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 3) brick_sweep(cons
                                 while (w) {
                                     const int l = __ffs(w) - 1;
                                     w &= w - 1;
-                                    M.lst(lp, pos++) = (uint16_t)((32 << 8) | (32 * j + l));
+                                    M.set_lst(lp, pos++, (32 << 8) | (32 * j + l));
                                 }
                             }
-                            if ((hact >> 32) & 1ull) M.lst(lp, pos++) = (uint16_t)((32 << 8) | W);
+                            if ((hact >> 32) & 1ull) M.set_lst(lp, pos++, (32 << 8) | W);
                         }
                     }
                 }
@@ -848,8 +870,8 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 3) brick_sweep(cons
                     const uint32_t rb = S.rowbase[r];
                     const uint32_t vrel = c == W ? 0u : (ex & 0xffffu) - (rb & 0xffffu);
                     const uint32_t qrel = (ex >> 16) - (rb >> 16);
-                    M.ent(cur, i) = pack_cell(vrel, qrel, cfg, l2);
-                    M.info(cur, i) = (uint8_t)info;
+                    M.set_ent(cur, i, pack_cell(vrel, qrel, cfg, l2));
+                    M.set_info(cur, i, info);
                     if (own && k < z1) {
                         const uint64_t vb = (uint64_t)S.segv[cur][r][0] + vrel;
                         if (vb + nv > out.vcap) {
