@@ -533,20 +533,6 @@ __device__ __forceinline__ uint32_t cell_qrel(uint32_t p) { return (p >> 11) & 0
 __device__ __forceinline__ uint32_t cell_cfg(uint32_t p) { return (p >> 21) & 0xffu; }
 __device__ __forceinline__ bool cell_l2(uint32_t p) { return (p >> 29) & 1u; }
 
-// List index of active cell (c, r) of the plane stored at parity p.
-__device__ __forceinline__ uint32_t entry_of(const SweepSmem &s, int p, int r, int c)
-{
-    if (c == W) return s.rowstart[p][r + 1] - 1u;
-    const uint4 w = *reinterpret_cast<const uint4 *>(s.xrow[p][r]);
-    const uint32_t q = (uint32_t)c >> 5, below_mask = (1u << (c & 31)) - 1u;
-    uint32_t idx = s.rowstart[p][r];
-    idx += q > 0 ? __popc(w.x) : __popc(w.x & below_mask);
-    if (q >= 1) idx += q > 1 ? __popc(w.y) : __popc(w.y & below_mask);
-    if (q >= 2) idx += q > 2 ? __popc(w.z) : __popc(w.z & below_mask);
-    if (q >= 3) idx += __popc(w.w & below_mask);
-    return idx;
-}
-
 __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane)
 {
 #pragma unroll
