@@ -346,7 +346,7 @@ dmc_status dmc_set_option(dmc_ctx *ctx, dmc_option opt, int64_t value)
         ctx->c.brick_zc = (uint32_t)value;
         return DMC_OK;
     case DMC_OPT_STREAM_SLABS:
-        if (value < 0 || value > 16) return DMC_ERR_INVALID_ARG;
+        if (value < 0 || value > 32) return DMC_ERR_INVALID_ARG;
         ctx->c.stream_slabs = (uint32_t)value;
         return DMC_OK;
     }
@@ -420,7 +420,7 @@ static dmc_status run_streamed(dmc_ctx *ctx, const dmc_volume *vol, const float 
     uint32_t slabs = c->stream_slabs;
     if (slabs == 0) {
         if (bytes < (64ull << 20)) return kNotStreamed;
-        slabs = (uint32_t)std::min<uint64_t>(16, std::max<uint64_t>(2, bytes / (160ull << 20)));   // 12 at 2 GiB
+        slabs = (uint32_t)std::min<uint64_t>(32, std::max<uint64_t>(2, bytes / (96ull << 20)));   // 21 at 2 GiB
     }
     // the context's device output buffers as they are: too small ones make
     // the caller take the plain path, which grows them

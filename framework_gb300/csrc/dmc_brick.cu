@@ -46,7 +46,8 @@ constexpr int NWB_COUNT = 8;              // warps per block of the count sweep 
                                           // registers (4 blocks at 64 spilled and ran 10% slower)
 constexpr int NWB_EMIT = 8;               // of the emit sweep: 2 blocks per SM
 constexpr int nwb(bool emit) { return emit ? NWB_EMIT : NWB_COUNT; }
-constexpr int kMaxSlabs = 16;             // z slabs of a streamed host extraction
+constexpr int kMaxSlabs = 32;             // z slabs of a streamed host extraction
+constexpr int kTickets = 4 + 3 * kMaxSlabs; // work tickets: 4 for a batch, 3 per streamed slab
 constexpr int QBUF = 96;                  // quads of one round of owner cells (3 per cell)
 constexpr int SCAN_NT = 512, SCAN_ITEMS = 8, SCAN_TILE = SCAN_NT * SCAN_ITEMS;   // 4096 segments per tile: half the look-back chain of 2048
 
@@ -1008,7 +1009,7 @@ __global__ void batch_prep(const BatchHead *__restrict__ head, TileState *tiles,
 {
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
     for (uint32_t t = tid; t < head->n_tiles; t += nth) tiles[t] = TileState{};
-    if (tid < 64) tickets[tid] = 0;
+    if (tid < kTickets) tickets[tid] = 0;
     if (tid < sizeof(DevCtl) / 4) reinterpret_cast<uint32_t *>(ctl)[tid] = 0;
     const Geom *vols = batch_geoms(head);
     for (uint32_t v = blockIdx.x; v < head->n; v += gridDim.x) {
@@ -1271,7 +1272,7 @@ static dmc_status batch_layout(Ctx *ctx, BatchState &b, uint32_t items, uint64_t
     const size_t o_mask = carve(8 * b.cap_mask);
     const size_t o_coord = carve(4 * b.cap_coord);
     const size_t o_res = carve(sizeof(dmc_batch_result) * (size_t)b.cap_items);
-    const size_t o_tk = carve(256);
+    const size_t o_tk = carve(4 * kTickets);
     if (b.in_flight) return DMC_ERR_INVALID_ARG;
     dmc_status s = ctx_reserve_scratch(ctx, off);
     if (s != DMC_OK) return s;

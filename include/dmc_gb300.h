@@ -241,7 +241,7 @@ typedef enum {
     DMC_OPT_BRICK_PLANES = 1,  /* z planes per brick, 1..256; 0 chooses from the batch size */
     DMC_OPT_STREAM_SLABS = 2   /* dmc_run_into in z slabs (upload, extraction and download
                                   overlap): 0 automatic (volumes of 64 MiB and more, one slab
-                                  per 160 MiB, 2..16), 1 never, 2..16 that many slabs */
+                                  per 96 MiB, 2..32), 1 never, 2..32 that many slabs */
 } dmc_option;
 
 dmc_status dmc_set_option(dmc_ctx *ctx, dmc_option opt, int64_t value);

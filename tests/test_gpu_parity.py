@@ -184,7 +184,7 @@ def test_run_into_streamed(kind):
         ms = ex.run(small, None, None, iso)
         sv, sq = len(ms.vertices), len(ms.quads)
         ex.run_into(small, np.empty((sv, 3), np.float32), np.empty((sq, 4), np.int32), None, None, None, iso)
-        for slabs in (4, 2, 3, 7, 16):
+        for slabs in (4, 2, 3, 7, 16, 32):
             ex.set_option(fg.OPT_STREAM_SLABS, slabs)
             for pinned in (True, False):
                 bufs = _host_out(V, Q, pinned)
