@@ -1303,6 +1303,19 @@ static dmc_batch_result *stage_results(BatchState &b)
     return (dmc_batch_result *)((uint8_t *)b.h_stage + b.plan_bytes);
 }
 
+// Blocks of a sweep launch: the resident grid, or fewer when the launch has
+// fewer bricks than resident warps, so that small extractions do not start
+// (and stage tables in) hundreds of idle blocks.  A captured graph keeps the
+// full grid: it replays batches of any size.
+static int sweep_blocks(const BatchState &b, int t, bool emit, uint64_t nbricks, bool full_grid)
+{
+    using namespace brick;
+    const int full = b.grid[t][emit ? 1 : 0];
+    if (full_grid) return full;
+    const uint64_t nwb = emit ? NWB_EMIT : NWB_COUNT;
+    return (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)full, (nbricks + nwb - 1) / nwb));
+}
+
 // Front half: plan upload, prep, count sweeps, scan, per-volume offsets.
 // Sweeps of a sample type without bricks are skipped unless `all` (a graph
 // must serve any later mix of types).
@@ -1315,12 +1328,12 @@ static dmc_status enqueue_front(Ctx *ctx, BatchState &b, dmc_batch_result *d_res
     CUDA_TRY(cudaGetLastError());
     if (timed) CUDA_TRY(cudaEventRecord(ctx->evk[0], st));
     if (all || nb[0]) {
-        brick_sweep<float, false><<<b.grid[0][0], 32 * NWB_COUNT, kCountSmem, st>>>(
+        brick_sweep<float, false><<<sweep_blocks(b, 0, false, nb[0], all), 32 * NWB_COUNT, kCountSmem, st>>>(
             b.d_plan, 0, BrickRange{0, kAllBricks}, ctx->d_tab, b.seg_cnt, EmitOut{}, b.spill, b.masks, &b.tickets[0], ctx->d_ctl->counters, &ctx->d_ctl->err);
         CUDA_TRY(cudaGetLastError());
     }
     if (all || nb[1]) {
-        brick_sweep<uint16_t, false><<<b.grid[1][0], 32 * NWB_COUNT, kCountSmem, st>>>(
+        brick_sweep<uint16_t, false><<<sweep_blocks(b, 1, false, nb[1], all), 32 * NWB_COUNT, kCountSmem, st>>>(
             b.d_plan, 1, BrickRange{0, kAllBricks}, ctx->d_tab, b.seg_cnt, EmitOut{}, b.spill, b.masks, &b.tickets[1], ctx->d_ctl->counters, &ctx->d_ctl->err);
         CUDA_TRY(cudaGetLastError());
     }
@@ -1328,7 +1341,9 @@ static dmc_status enqueue_front(Ctx *ctx, BatchState &b, dmc_batch_result *d_res
     ScanCtl ctl;
     ctl.tiles = b.tiles; ctl.ticket = &ctx->d_ctl->ticket; ctl.err = &ctx->d_ctl->err;
     ctl.totals = ctx->d_ctl->totals; ctl.n_tiles = 0;
-    seg_scan<<<2 * ctx->num_sms, SCAN_NT, 0, st>>>(b.d_plan, b.seg_cnt, ctl, b.seg_off, 0ull, ~0ull);
+    const uint32_t n_tiles = ((const BatchHead *)b.h_stage)->n_tiles;
+    const int scan_blocks = all ? 2 * ctx->num_sms : (int)std::max<uint32_t>(1u, std::min<uint32_t>(2u * ctx->num_sms, n_tiles));
+    seg_scan<<<scan_blocks, SCAN_NT, 0, st>>>(b.d_plan, b.seg_cnt, ctl, b.seg_off, 0ull, ~0ull);
     CUDA_TRY(cudaGetLastError());
     volume_results<<<4, 128, 0, st>>>(b.d_plan, b.seg_cnt, b.seg_off, ctx->d_ctl->totals, d_res);
     CUDA_TRY(cudaGetLastError());
@@ -1343,12 +1358,12 @@ static dmc_status enqueue_back(Ctx *ctx, BatchState &b, const brick::EmitOut &eo
     using namespace brick;
     if (timed) CUDA_TRY(cudaEventRecord(ctx->evk[3], st));
     if (all || nb[0]) {
-        brick_sweep<float, true><<<b.grid[0][1], 32 * NWB_EMIT, kEmitSmem, st>>>(
+        brick_sweep<float, true><<<sweep_blocks(b, 0, true, nb[0], all), 32 * NWB_EMIT, kEmitSmem, st>>>(
             b.d_plan, 0, BrickRange{0, kAllBricks}, ctx->d_tab, nullptr, eo, b.spill, b.masks, &b.tickets[2], ctx->d_ctl->counters, &ctx->d_ctl->err);
         CUDA_TRY(cudaGetLastError());
     }
     if (all || nb[1]) {
-        brick_sweep<uint16_t, true><<<b.grid[1][1], 32 * NWB_EMIT, kEmitSmem, st>>>(
+        brick_sweep<uint16_t, true><<<sweep_blocks(b, 1, true, nb[1], all), 32 * NWB_EMIT, kEmitSmem, st>>>(
             b.d_plan, 1, BrickRange{0, kAllBricks}, ctx->d_tab, nullptr, eo, b.spill, b.masks, &b.tickets[3], ctx->d_ctl->counters, &ctx->d_ctl->err);
         CUDA_TRY(cudaGetLastError());
     }
@@ -1618,10 +1633,10 @@ static void launch_sweep(Ctx *ctx, BatchState &b, bool emit, brick::BrickRange r
     using namespace brick;
     const uint32_t grp = std::is_same<T, float>::value ? 0 : 1;
     if (emit)
-        brick_sweep<T, true><<<b.grid[grp][1], 32 * NWB_EMIT, kEmitSmem, st>>>(
+        brick_sweep<T, true><<<sweep_blocks(b, grp, true, r.cnt, false), 32 * NWB_EMIT, kEmitSmem, st>>>(
             b.d_plan, grp, r, ctx->d_tab, nullptr, eo, b.spill, b.masks, ticket, ctx->d_ctl->counters, &ctx->d_ctl->err);
     else
-        brick_sweep<T, false><<<b.grid[grp][0], 32 * NWB_COUNT, kCountSmem, st>>>(
+        brick_sweep<T, false><<<sweep_blocks(b, grp, false, r.cnt, false), 32 * NWB_COUNT, kCountSmem, st>>>(
             b.d_plan, grp, r, ctx->d_tab, b.seg_cnt, EmitOut{}, b.spill, b.masks, ticket, ctx->d_ctl->counters, &ctx->d_ctl->err);
 }
 
@@ -1711,8 +1726,9 @@ dmc_status brick_run_streamed(Ctx *ctx, const ExtractArgs &a, const StreamIO &io
             ScanCtl ctl;
             ctl.tiles = b.tiles + toff[i]; ctl.ticket = &b.tickets[4 + 3 * i + 2]; ctl.err = &ctx->d_ctl->err;
             ctl.totals = ctx->d_ctl->totals; ctl.n_tiles = 0; ctl.carry = ctx->d_ctl->totals;
-            seg_scan<<<2 * ctx->num_sms, SCAN_NT, 0, st>>>(b.d_plan, b.seg_cnt, ctl, b.seg_off, (uint64_t)z[i] * segs_z,
-                                                           (uint64_t)(z[i + 1] - z[i]) * segs_z);
+            const uint64_t nt = toff[i + 1] - toff[i];
+            seg_scan<<<(int)std::max<uint64_t>(1, std::min<uint64_t>(2ull * ctx->num_sms, nt)), SCAN_NT, 0, st>>>(
+                b.d_plan, b.seg_cnt, ctl, b.seg_off, (uint64_t)z[i] * segs_z, (uint64_t)(z[i + 1] - z[i]) * segs_z);
             snap_totals<<<1, 32, 0, st>>>(ctx->d_ctl, b.d_snap + 4 * i);
             CUDA_TRY(cudaGetLastError());
             CUDA_TRY(cudaEventRecord(b.ev_tot[i], st));
