@@ -38,6 +38,7 @@ ABI_SYMBOLS = [
     "dmc_extract_batch", "dmc_batch_wait", "dmc_set_option", "dmc_extract_device_noalloc",
     "dmc_server_create", "dmc_server_destroy", "dmc_server_add_volume", "dmc_server_submit", "dmc_server_wait",
     "dmc_server_release", "dmc_server_get_stats", "dmc_server_replay", "dmc_write_obj", "dmc_compact_mesh",
+    "dmc_shard_count", "dmc_shard_emit",
 ]
 BATCH_ASYNC, BATCH_GRAPH = 0x1, 0x2
 OPT_BRICK_PLANES = 1
@@ -144,6 +145,11 @@ def load_library(build_if_missing=True):
                                     ctypes.c_void_p]
     L.dmc_batch_wait.argtypes = [ctypes.c_void_p, P(_BatchResult), P(ctypes.c_uint64), P(ctypes.c_uint64)]
     L.dmc_set_option.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int64]
+    L.dmc_shard_count.argtypes = [ctypes.c_void_p, P(_Volume), ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                  P(ctypes.c_float), P(ctypes.c_float), ctypes.c_float, P(ctypes.c_uint64),
+                                  P(ctypes.c_uint64), ctypes.c_void_p]
+    L.dmc_shard_emit.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p,
+                                 ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p]
     L.dmc_compact_mesh.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
                                    ctypes.c_void_p, ctypes.c_void_p, P(ctypes.c_uint64), ctypes.c_void_p]
     L.dmc_write_obj.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
@@ -365,6 +371,42 @@ class Extractor:
                                           out_vertices.data_ptr(), ctypes.byref(n), _stream_handle(stream)),
                "dmc_compact_mesh")
         return out_vertices[:int(n.value)]
+
+    def shard_count(self, local, nz, z_begin, z_end, xyz_min=None, xyz_max=None, iso=0.0, stream=None):
+        """``dmc_shard_count``: this rank's part of a sharded extraction.
+
+        ``local`` is a contiguous CUDA tensor [planes, y, x] (float32, or int16
+        holding uint16 bit patterns) with the point planes
+        ``shard.point_planes(nz, z_begin, z_end)`` of a volume with ``nz``
+        point planes; ``z_begin`` / ``z_end`` are cell planes of the whole
+        volume, whose default extent is (0, 0, 0)..(x-1, y-1, nz-1).  Returns
+        this rank's (n_vertices, n_quads)."""
+        t = local
+        if not t.is_cuda or not t.is_contiguous() or t.dim() != 3:
+            raise DMCError(1, "local planes must be a contiguous 3-D CUDA tensor")
+        dt = {"float32": 0, "int16": 1, "uint16": 1}.get(str(t.dtype).replace("torch.", ""))
+        if dt is None:
+            raise DMCError(1, "volume tensor dtype must be float32 or (u)int16")
+        vol = _volume_struct(t.data_ptr(), dt, (t.shape[2], t.shape[1], t.shape[0]))
+        mn, mx = _default_extent((t.shape[2], t.shape[1], nz), xyz_min, xyz_max)
+        nv, nq = ctypes.c_uint64(), ctypes.c_uint64()
+        _check(self._lib.dmc_shard_count(self._h, ctypes.byref(vol), int(nz), int(z_begin), int(z_end), _f3(mn),
+                                         _f3(mx), ctypes.c_float(iso), ctypes.byref(nv), ctypes.byref(nq),
+                                         _stream_handle(stream)), "dmc_shard_count")
+        return int(nv.value), int(nq.value)
+
+    def shard_emit(self, vertex_offset, vertices, quads, triangles=None, stream=None):
+        """``dmc_shard_emit``: writes the part counted by ``shard_count`` into
+        CUDA tensors (float32 [V,3], int32/uint32 [Q,4], optional [2Q,3]),
+        quad indices offset by ``vertex_offset`` (the vertices of all earlier
+        ranks)."""
+        qcap = quads.numel() // 4
+        if triangles is not None:
+            qcap = min(qcap, triangles.numel() // 6)
+        _check(self._lib.dmc_shard_emit(self._h, int(vertex_offset), vertices.data_ptr(), vertices.numel() // 3,
+                                        quads.data_ptr(), qcap,
+                                        triangles.data_ptr() if triangles is not None else None,
+                                        _stream_handle(stream)), "dmc_shard_emit")
 
     def set_option(self, option, value):
         """``dmc_set_option``: e.g. ``set_option(OPT_BRICK_PLANES, 16)``; 0 restores the automatic choice."""

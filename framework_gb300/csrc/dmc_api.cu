@@ -129,14 +129,12 @@ static dmc_status finish(dmc_ctx *ctx, cudaStream_t st)
     CUDA_TRY(cudaEventRecord(c->ev1, st));
     CUDA_TRY(cudaMemcpyAsync(c->h_ctl, c->d_ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-    c->stats.device_ms = ms;
+    event_ms(&c->stats.device_ms, c->ev0, c->ev1);
     if (c->evk_used >= 1) {
-        cudaEventElapsedTime(&c->stats.count_ms, c->evk[0], c->evk[1]);
-        cudaEventElapsedTime(&c->stats.scan_ms, c->evk[1], c->evk[2]);
+        event_ms(&c->stats.count_ms, c->evk[0], c->evk[1]);
+        event_ms(&c->stats.scan_ms, c->evk[1], c->evk[2]);
     }
-    if (c->evk_used >= 2) cudaEventElapsedTime(&c->stats.emit_ms, c->evk[3], c->evk[4]);
+    if (c->evk_used >= 2) event_ms(&c->stats.emit_ms, c->evk[3], c->evk[4]);
     c->evk_used = 0;
     uint32_t err = c->h_ctl->err;
     if (err & DEV_ERR_TIMEOUT) return DMC_ERR_TIMEOUT;
@@ -314,11 +312,11 @@ dmc_status dmc_extract_batch(dmc_ctx *ctx, const dmc_batch_item *items, uint32_t
         return DMC_OK;
     }
     cudaEventSynchronize(c->ev1);
-    cudaEventElapsedTime(&c->stats.device_ms, c->ev0, c->ev1);
+    event_ms(&c->stats.device_ms, c->ev0, c->ev1);
     if (c->evk_used >= 2) {
-        cudaEventElapsedTime(&c->stats.count_ms, c->evk[0], c->evk[1]);
-        cudaEventElapsedTime(&c->stats.scan_ms, c->evk[1], c->evk[2]);
-        cudaEventElapsedTime(&c->stats.emit_ms, c->evk[3], c->evk[4]);
+        event_ms(&c->stats.count_ms, c->evk[0], c->evk[1]);
+        event_ms(&c->stats.scan_ms, c->evk[1], c->evk[2]);
+        event_ms(&c->stats.emit_ms, c->evk[3], c->evk[4]);
     }
     c->evk_used = 0;
     return DMC_OK;
@@ -332,8 +330,52 @@ dmc_status dmc_batch_wait(dmc_ctx *ctx, dmc_batch_result *results, uint64_t *n_v
     c->batch_pending = false;
     if (cudaSetDevice(c->device) != cudaSuccess) return DMC_ERR_CUDA;
     dmc_status s = brick_wait(c, results, n_vertices, n_quads);
-    float ms = 0.f;
-    if (cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess) c->stats.device_ms = ms;
+    event_ms(&c->stats.device_ms, c->ev0, c->ev1);
+    return s;
+}
+
+dmc_status dmc_shard_count(dmc_ctx *ctx, const dmc_volume *local, uint32_t nz, uint32_t z_begin, uint32_t z_end,
+                           const float xyz_min[3], const float xyz_max[3], float iso,
+                           uint64_t *n_vertices, uint64_t *n_quads, void *stream)
+{
+    if (!ctx || !local || !n_vertices || !n_quads) return DMC_ERR_INVALID_ARG;
+    *n_vertices = 0; *n_quads = 0;
+    if (nz < 2 || z_begin >= z_end || z_end > nz - 1) return DMC_ERR_INVALID_ARG;
+    const uint32_t p0 = z_begin > 0 ? z_begin - 1 : 0, p1 = std::min<uint32_t>(z_end + 3, nz);
+    if (local->dims[2] != p1 - p0) return DMC_ERR_INVALID_ARG;
+    dmc_volume whole = *local;
+    whole.dims[2] = nz;
+    ExtractArgs a;
+    dmc_status s = make_args(&whole, xyz_min, xyz_max, iso, a);
+    if (s != DMC_OK) return s;
+    if (!brick_supports(a)) return DMC_ERR_UNSUPPORTED;
+    Ctx *c = &ctx->c;
+    if (c->batch_pending) return DMC_ERR_INVALID_ARG;
+    if (cudaSetDevice(c->device) != cudaSuccess) return DMC_ERR_CUDA;
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    BrickItem it;
+    it.data = local->data; it.dtype = local->dtype; it.pts = a.pts; it.cells = a.cells; it.iso = a.iso;
+    it.mn = a.mn; it.rng = a.rng;
+    c->stats = dmc_stats{};
+    c->stats.algo = DMC_ALGO_BRICK;
+    s = brick_shard_count(c, it, p0, z_begin, z_end, n_vertices, n_quads, st);
+    event_ms(&c->stats.device_ms, c->ev0, c->ev1);
+    return s;
+}
+
+dmc_status dmc_shard_emit(dmc_ctx *ctx, uint64_t vertex_offset, float *d_vertices, uint64_t vertex_capacity,
+                          uint32_t *d_quads, uint64_t quad_capacity, uint32_t *d_triangles, void *stream)
+{
+    if (!ctx) return DMC_ERR_INVALID_ARG;
+    if ((vertex_capacity && !d_vertices) || (quad_capacity && !d_quads)) return DMC_ERR_INVALID_ARG;
+    Ctx *c = &ctx->c;
+    if (c->batch_pending) return DMC_ERR_INVALID_ARG;
+    if (cudaSetDevice(c->device) != cudaSuccess) return DMC_ERR_CUDA;
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    BrickOut o{};
+    o.verts = d_vertices; o.vcap = vertex_capacity; o.quads = d_quads; o.qcap = quad_capacity; o.tris = d_triangles;
+    dmc_status s = brick_shard_emit(c, vertex_offset, o, st);
+    if (s == DMC_OK) event_ms(&c->stats.emit_ms, c->ev0, c->ev1);
     return s;
 }
 

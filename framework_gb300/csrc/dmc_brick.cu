@@ -569,11 +569,17 @@ struct EmitOut {
 // one).  The host writes it to pinned memory and one copy moves it to the
 // device, so the kernels take every batch-dependent size from here and a
 // captured graph replays any batch that fits the scratch layout.
-// Bricks [lo, lo + cnt) of a launch's numbering (cnt = kAllBricks: all of them).
+// Bricks [lo, lo + cnt) of a launch's numbering (cnt = kAllBricks: all of
+// them).  The count sweep processes only cell planes below zlim (a sharded
+// extraction counts the next shard's first plane this way), and with
+// kNoStats adds nothing to the active / LUT2 / dropped-quad counters.
 struct BrickRange {
     uint32_t lo, cnt;
+    uint32_t zlim = 0xffffffffu;
+    uint32_t flags = 0;
 };
 constexpr uint32_t kAllBricks = 0xffffffffu;
+constexpr uint32_t kNoStats = 1u;
 
 struct alignas(64) BatchHead {
     unsigned long long nbricks[2];   // bricks of the f32 / u16 volumes
@@ -702,7 +708,7 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 3) brick_sweep(cons
         const uint32_t z1 = min(z0 + g.zc, g.cells.z);
         const uint64_t rowmask = ((1ull << min(NR, g.cells.y - y0)) - 1ull);
         // the emit sweep also visits plane z1: quads of plane z1-1 reference it
-        const uint32_t kend = EMIT ? z1 : z1 - 1;
+        const uint32_t kend = EMIT ? z1 : min(z1, range.zlim) - 1;
 
         // Point planes z0..z1 of the brick.  The count sweep computes their
         // masks from the samples and keeps them in the mask store (each
@@ -738,7 +744,9 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 3) brick_sweep(cons
                     }
                     if (!wait_slot((k + 1) & 1)) return;
                 } else {
-                    const bool keep = k + 1 < z1 || z1 == g.cells.z;
+                    // (a plane-limited count also keeps its last plane: the emit
+                    // sweep of the shard below reads it)
+                    const bool keep = k + 1 < z1 || z1 == g.cells.z || k + 1 >= range.zlim;
                     load_plane<T>(vol, g.pts, g.iso, g.iso_u16, g.isole_u16, x0, y0, k + 1, S.mask[(k + 1) & 1], lane,
                                   keep ? mask_chunk(masks, g, xs, yb, k + 1) : nullptr, ncolr);
                 }
@@ -988,7 +996,7 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 3) brick_sweep(cons
             __syncwarp();
         }
     }
-    if (!EMIT) {
+    if (!EMIT && !(range.flags & kNoStats)) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             n_l2 += __shfl_xor_sync(0xffffffffu, n_l2, o);
@@ -1195,6 +1203,11 @@ struct BatchState {
     cudaEvent_t ev_start = nullptr;
     cudaEvent_t ev_in[brick::kMaxSlabs]{}, ev_tot[brick::kMaxSlabs]{}, ev_emit[brick::kMaxSlabs]{};
     unsigned long long *h_snap = nullptr, *d_snap = nullptr;
+    // sharded extraction between its two phases: sample type, z-brick range, bricks per z layer
+    bool shard_ready = false;
+    int sh_grp = 0;
+    uint32_t sh_zb0 = 0, sh_zb1 = 0;
+    uint64_t sh_bxy = 0;
     // batch in flight
     bool in_flight = false;
     uint32_t n_inflight = 0;
@@ -1467,10 +1480,8 @@ static dmc_status retarget_graph(Ctx *ctx, BatchState &b, const brick::EmitOut &
     return DMC_OK;
 }
 
-// Chooses the planes per brick and writes the plan (head and one Geom per
-// volume: the f32 volumes, then the u16 ones) to the pinned staging, after
-// carving the scratch for it.  nb: bricks of each sample type.
-static dmc_status stage_plan(Ctx *ctx, BatchState &b, const BrickItem *items, uint32_t n, uint64_t nb[2])
+// Planes per brick: the context's option, or the automatic choice.
+static uint32_t pick_zc(Ctx *ctx, const BatchState &b, const BrickItem *items, uint32_t n)
 {
     using namespace brick;
     // planes per brick: long sweeps amortise the z halo, but uneven bricks
@@ -1488,6 +1499,17 @@ static dmc_status stage_plan(Ctx *ctx, BatchState &b, const BrickItem *items, ui
             zc >>= 1;
         }
     }
+    return zc;
+}
+
+// Chooses the planes per brick and writes the plan (head and one Geom per
+// volume: the f32 volumes, then the u16 ones) to the pinned staging, after
+// carving the scratch for it.  nb: bricks of each sample type.
+static dmc_status stage_plan(Ctx *ctx, BatchState &b, const BrickItem *items, uint32_t n, uint64_t nb[2],
+                             uint32_t zc_force = 0)
+{
+    using namespace brick;
+    const uint32_t zc = zc_force ? zc_force : pick_zc(ctx, b, items, n);
     // descriptors: the f32 volumes, then the u16 ones (one launch per type)
     uint64_t nseg = 0, ncoord = 0, nmask = 0;
     nb[0] = nb[1] = 0;
@@ -1767,13 +1789,133 @@ dmc_status brick_run_streamed(Ctx *ctx, const ExtractArgs &a, const StreamIO &io
     }
     CUDA_TRY(cudaStreamSynchronize(st));
     CUDA_TRY(cudaStreamSynchronize(b.s_out));
-    float ms = 0.f;
-    if (cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) == cudaSuccess) ctx->stats.device_ms = ms;
+    event_ms(&ctx->stats.device_ms, ctx->ev0, ctx->ev1);
     stats_from_ctl(ctx);
     if (ctx->h_ctl->err & DEV_ERR_OVERFLOW) *dev_short = true;
     if (*dev_short) return DMC_ERR_OUTPUT_OVERFLOW;
     if ((s = ctl_status(ctx->h_ctl)) != DMC_OK) return s;
     return host_short ? DMC_ERR_OUTPUT_OVERFLOW : DMC_OK;
+}
+
+// Sharded extraction of one volume across ranks in z slabs (the volume's
+// cell planes [z_begin, z_end) on this rank).  it.pts / it.cells are the
+// whole volume's; it.data points to this rank's copy of the point planes
+// from plane0 on, which must cover [z_begin - 1, z_end + 3) within the
+// volume: one plane below for the 2B/3B test of the first cell plane; above,
+// the next shard's first cell plane (whose offsets the quads of the last
+// plane reference) with its own 2B/3B test.
+//
+// Phase 1 (brick_shard_count): the count sweep over the shard's bricks, a
+// plane-limited count of the next shard's first plane (no counters), and
+// the scan of the shard's segments plus that plane, from zero.  The shard's
+// totals are the offsets at the next shard's first plane.
+// Phase 2 (brick_shard_emit): with the vertex offset of all earlier shards
+// (an exclusive scan of the totals across ranks), the emit sweep writes the
+// shard's vertices and quads at local positions, quad indices made global.
+// In rank order the parts form the unsharded mesh: the same bricks, the same
+// segment order, the same scan in pieces.
+dmc_status brick_shard_count(Ctx *ctx, const BrickItem &item, uint32_t plane0, uint32_t z_begin, uint32_t z_end,
+                             uint64_t *V, uint64_t *Q, cudaStream_t st)
+{
+    using namespace brick;
+    BatchState *bp = nullptr;
+    dmc_status s = batch_state(ctx, &bp);
+    if (s != DMC_OK) return s;
+    BatchState &b = *bp;
+    if (b.in_flight) return DMC_ERR_INVALID_ARG;
+    b.shard_ready = false;
+    const uint3 cells = item.cells;
+    if (z_begin >= z_end || z_end > cells.z) return DMC_ERR_INVALID_ARG;
+    // bricks of this shard's size, then as deep as both shard boundaries allow
+    BrickItem shard = item;
+    shard.cells.z = z_end - z_begin;
+    uint32_t zc = pick_zc(ctx, b, &shard, 1);
+    while (zc > 1 && (z_begin % zc != 0 || (z_end != cells.z && z_end % zc != 0))) zc >>= 1;
+    // the kernels index the volume by global plane: shift the base by plane0 planes
+    const uint64_t plane_bytes = (uint64_t)item.pts.x * item.pts.y * (item.dtype == DMC_F32 ? 4u : 2u);
+    BrickItem it = item;
+    it.data = reinterpret_cast<const void *>(reinterpret_cast<uintptr_t>(item.data) - (uintptr_t)(plane0 * plane_bytes));
+    uint64_t nb[2] = {0, 0};
+    if ((s = stage_plan(ctx, b, &it, 1, nb, zc)) != DMC_OK) return s;
+    BatchHead *head = (BatchHead *)b.h_stage;
+    const Geom &g = *(const Geom *)(head + 1);
+    const int grp = it.dtype == DMC_F32 ? 0 : 1;
+    const uint64_t bxy = (uint64_t)g.nxs * g.nyb, segs_z = (uint64_t)cells.y * g.nxs;
+    const uint32_t zb0 = z_begin / zc, zb1 = z_end == cells.z ? g.nzb : z_end / zc;
+    const bool halo = z_end < cells.z;
+
+    CUDA_TRY(cudaEventRecord(ctx->ev0, st));
+    CUDA_TRY(cudaMemcpyAsync(b.d_plan, b.h_stage, b.plan_bytes, cudaMemcpyHostToDevice, st));
+    batch_prep<<<2 * ctx->num_sms, 256, 0, st>>>(b.d_plan, b.tiles, b.tickets, ctx->d_ctl);
+    CUDA_TRY(cudaGetLastError());
+    EmitOut none{};
+    const BrickRange own{(uint32_t)(zb0 * bxy), (uint32_t)((zb1 - zb0) * bxy)};
+    if (grp == 0) launch_sweep<float>(ctx, b, false, own, none, &b.tickets[0], st);
+    else launch_sweep<uint16_t>(ctx, b, false, own, none, &b.tickets[1], st);
+    if (halo) {
+        BrickRange next{(uint32_t)(zb1 * bxy), (uint32_t)bxy};
+        next.zlim = z_end + 1;
+        next.flags = kNoStats;
+        if (grp == 0) launch_sweep<float>(ctx, b, false, next, none, &b.tickets[4], st);
+        else launch_sweep<uint16_t>(ctx, b, false, next, none, &b.tickets[4], st);
+    }
+    CUDA_TRY(cudaGetLastError());
+    ScanCtl ctl;
+    ctl.tiles = b.tiles; ctl.ticket = &b.tickets[5]; ctl.err = &ctx->d_ctl->err;
+    ctl.totals = ctx->d_ctl->totals; ctl.n_tiles = 0;
+    const uint64_t seg0 = (uint64_t)z_begin * segs_z, nseg = (uint64_t)(z_end - z_begin + (halo ? 1 : 0)) * segs_z;
+    const uint64_t nt = (nseg + SCAN_TILE - 1) / SCAN_TILE;
+    seg_scan<<<(int)std::max<uint64_t>(1, std::min<uint64_t>(2ull * ctx->num_sms, nt)), SCAN_NT, 0, st>>>(
+        b.d_plan, b.seg_cnt, ctl, b.seg_off, seg0, nseg);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(ctx->h_ctl, ctx->d_ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, st));
+    // the shard's totals: the offsets where the next shard's first plane starts
+    uint2 *h_off = reinterpret_cast<uint2 *>(stage_results(b));
+    if (halo)
+        CUDA_TRY(cudaMemcpyAsync(h_off, b.seg_off + (uint64_t)z_end * segs_z, sizeof(uint2), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaEventRecord(ctx->ev1, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    stats_from_ctl(ctx);
+    const uint32_t err = ctx->h_ctl->err;
+    if (err & DEV_ERR_TIMEOUT) return DMC_ERR_TIMEOUT;
+    if (err & DEV_ERR_BOUNDS) return DMC_ERR_DEVICE_CHECK;
+    const uint64_t tv = halo ? h_off->x : ctx->h_ctl->totals[0], tq = halo ? h_off->y : ctx->h_ctl->totals[1];
+    ctx->stats.n_vertices = tv;
+    ctx->stats.n_quads = tq;
+    if (V) *V = tv;
+    if (Q) *Q = tq;
+    if (ctx->h_ctl->totals[0] >= 0xFFFFFFFFull || ctx->h_ctl->totals[1] >= 0xFFFFFFFFull) return DMC_ERR_OUTPUT_OVERFLOW;
+    b.shard_ready = true;
+    b.sh_grp = grp; b.sh_zb0 = zb0; b.sh_zb1 = zb1; b.sh_bxy = bxy;
+    return DMC_OK;
+}
+
+dmc_status brick_shard_emit(Ctx *ctx, uint64_t vertex_offset, const BrickOut &o, cudaStream_t st)
+{
+    using namespace brick;
+    BatchState *b = ctx->batch;
+    if (!b || !b->shard_ready || b->in_flight) return DMC_ERR_INVALID_ARG;
+    // quad indices: local vertex index + vertex_offset (the emit subtracts vbase)
+    Geom *hg = (Geom *)((BatchHead *)b->h_stage + 1);
+    hg->vbase = (uint32_t)(0u - (uint32_t)vertex_offset);
+    Geom *dg = (Geom *)(b->d_plan + 1);
+    CUDA_TRY(cudaEventRecord(ctx->ev0, st));
+    CUDA_TRY(cudaMemcpyAsync(&dg->vbase, &hg->vbase, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    EmitOut eo;
+    eo.seg_off = b->seg_off; eo.verts = o.verts; eo.vcap = o.vcap; eo.quads = o.quads; eo.qcap = o.qcap; eo.tris = o.tris;
+    const BrickRange own{(uint32_t)(b->sh_zb0 * b->sh_bxy), (uint32_t)((b->sh_zb1 - b->sh_zb0) * b->sh_bxy)};
+    if (b->sh_grp == 0) launch_sweep<float>(ctx, *b, true, own, eo, &b->tickets[2], st);
+    else launch_sweep<uint16_t>(ctx, *b, true, own, eo, &b->tickets[3], st);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(ctx->h_ctl, ctx->d_ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaEventRecord(ctx->ev1, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    b->shard_ready = false;      // the emit sweep consumed the tickets
+    const uint32_t err = ctx->h_ctl->err;
+    if (err & DEV_ERR_TIMEOUT) return DMC_ERR_TIMEOUT;
+    if (err & DEV_ERR_OVERFLOW) return DMC_ERR_OUTPUT_OVERFLOW;
+    if (err & DEV_ERR_BOUNDS) return DMC_ERR_DEVICE_CHECK;
+    return DMC_OK;
 }
 
 dmc_status brick_wait(Ctx *ctx, dmc_batch_result *h_results, uint64_t *n_vertices, uint64_t *n_quads)

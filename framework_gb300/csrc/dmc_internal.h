@@ -70,6 +70,16 @@ struct ExtractArgs {
 
 dmc_status ctx_reserve_scratch(Ctx *ctx, size_t bytes);
 
+// Milliseconds between two recorded events into *ms (unchanged when the
+// query fails, e.g. an event that was never recorded).  A failed query's
+// error is cleared, so that it cannot surface in a later launch check.
+inline void event_ms(float *ms, cudaEvent_t a, cudaEvent_t b)
+{
+    float v = 0.f;
+    if (cudaEventElapsedTime(&v, a, b) == cudaSuccess) *ms = v;
+    else (void)cudaGetLastError();
+}
+
 // One volume of a brick-path extraction.
 struct BrickItem {
     const void *data;          // device samples
@@ -112,6 +122,11 @@ struct StreamIO {
 // downloaded; the totals are in the context's stats).
 dmc_status brick_run_streamed(Ctx *ctx, const ExtractArgs &a, const StreamIO &io, uint32_t slabs, bool *dev_short,
                               cudaStream_t st);
+// Sharded extraction (dmc_shard_count / dmc_shard_emit): item describes the
+// whole volume, item.data this rank's point planes from plane0 on.
+dmc_status brick_shard_count(Ctx *ctx, const BrickItem &item, uint32_t plane0, uint32_t z_begin, uint32_t z_end,
+                             uint64_t *V, uint64_t *Q, cudaStream_t st);
+dmc_status brick_shard_emit(Ctx *ctx, uint64_t vertex_offset, const BrickOut &o, cudaStream_t st);
 // Completes an asynchronous batch: waits for it and checks its status.
 dmc_status brick_wait(Ctx *ctx, dmc_batch_result *h_results, uint64_t *n_vertices, uint64_t *n_quads);
 dmc_status upload_tables(Ctx *ctx);

@@ -236,6 +236,32 @@ dmc_status dmc_extract_batch(dmc_ctx *ctx, const dmc_batch_item *items, uint32_t
  * results (host, may be NULL) and the totals, and returns its status. */
 dmc_status dmc_batch_wait(dmc_ctx *ctx, dmc_batch_result *results, uint64_t *n_vertices, uint64_t *n_quads);
 
+/* ---- sharded extraction of one volume across ranks (no reference
+ * counterpart) ------------------------------------------------------------
+ *
+ * The volume's cell planes are split into z ranges, one per rank (one GPU
+ * each).  Rank r holds its cell planes [z_begin, z_end) of a volume with nz
+ * point planes, as the point planes [max(z_begin - 1, 0), min(z_end + 3, nz))
+ * in its own device memory: `local` describes them (dims[0], dims[1] those
+ * of the volume, dims[2] the local plane count).  The planes beyond its cells
+ * are halo: one below for the 2B/3B test of its first plane, and above, the
+ * next rank's first cell plane (whose offsets the quads of its last plane
+ * reference) with its 2B/3B test.
+ *
+ * dmc_shard_count counts the rank's part and returns its vertex and quad
+ * totals.  The ranks exchange them (an exclusive scan: the vertices and quads
+ * of all earlier ranks), and dmc_shard_emit writes the part into device
+ * buffers: vertices and quads (triangles optional) at local positions, quad
+ * indices global (local vertex index + vertex_offset).  Concatenated in rank
+ * order the parts equal the unsharded mesh bit for bit.  The emit must follow
+ * the count on the same context, with the local planes unchanged; on too
+ * small buffers it returns DMC_ERR_OUTPUT_OVERFLOW with undefined contents. */
+dmc_status dmc_shard_count(dmc_ctx *ctx, const dmc_volume *local, uint32_t nz, uint32_t z_begin, uint32_t z_end,
+                           const float xyz_min[3], const float xyz_max[3], float iso,
+                           uint64_t *n_vertices, uint64_t *n_quads, void *stream);
+dmc_status dmc_shard_emit(dmc_ctx *ctx, uint64_t vertex_offset, float *d_vertices, uint64_t vertex_capacity,
+                          uint32_t *d_quads, uint64_t quad_capacity, uint32_t *d_triangles, void *stream);
+
 /* Tuning knobs (no reference counterpart). */
 typedef enum {
     DMC_OPT_BRICK_PLANES = 1,  /* z planes per brick, 1..256; 0 chooses from the batch size */

@@ -33,7 +33,7 @@ def _combine_worker(rank, world, port, out):
 
 def test_combine_ranks_gloo():
     import torch.multiprocessing as mp
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()   # no fork of this multi-threaded process
     out = mgr.dict()
     mp.spawn(_combine_worker, args=(2, _free_port(), out), nprocs=2, join=True)
     assert out[0] == out[1] == (2.0, 30.0)
@@ -58,3 +58,42 @@ def test_reference_arm_under_torchrun_two_ranks():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port"
+
+
+def _shard_exchange_worker(rank, world, port, out):
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    sys.path.insert(0, ROOT)
+    from framework_gb300 import shard
+    totals = shard.exchange_totals(10 + rank, 100 + 7 * rank, dist)
+    out[rank] = (totals, shard.exclusive_offsets(totals, rank))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_shard_exchange_gloo():
+    """The one collective of a sharded extraction: every rank gets all ranks'
+    totals in rank order, and its exclusive offsets from them."""
+    import torch.multiprocessing as mp
+    mgr = mp.get_context("spawn").Manager()   # no fork of this multi-threaded process
+    out = mgr.dict()
+    mp.spawn(_shard_exchange_worker, args=(2, _free_port(), out), nprocs=2, join=True)
+    assert out[0] == ([(10, 100), (11, 107)], (0, 0))
+    assert out[1] == ([(10, 100), (11, 107)], (10, 100))
+
+
+def test_shard_ranges_and_halo():
+    sys.path.insert(0, ROOT)
+    from framework_gb300 import shard
+    for cz, world, align in [(1023, 8, 32), (1023, 3, 32), (100, 7, 32), (9, 9, 32), (5000, 4, 64), (260, 5, 32)]:
+        r = shard.shard_ranges(cz, world, align)
+        assert len(r) == world and r[0][0] == 0 and r[-1][1] == cz
+        assert all(a < b for a, b in r) and all(r[i][1] == r[i + 1][0] for i in range(world - 1))
+        if cz >= world * align:
+            assert all(b % align == 0 for _, b in r[:-1])
+    assert shard.point_planes(1024, 0, 100) == (0, 103)
+    assert shard.point_planes(1024, 100, 1023) == (99, 1024)
+    assert shard.point_planes(1024, 500, 520) == (499, 523)
+    assert shard.exchange_totals(5, 6) == [(5, 6)]
+    assert shard.exclusive_offsets([(1, 2), (3, 4), (5, 6)], 2) == (4, 6)
