@@ -1,15 +1,18 @@
 // Brick path: persistent warps sweep bricks of the volume along z.
 //
 // A brick is 128 cell columns x 32 cell rows x a run of z planes and belongs
-// to one warp.  Lane l owns columns l, l+32, l+64, l+96: every warp load is a
-// contiguous 32-sample run of one row, and loads are issued 32 at a time per
-// lane.  For every point plane a lane keeps one bit per sample, "below the
-// isovalue", in a 64-bit mask per column (rows 0..33).  A cell's
-// configuration is a few shifts on the masks of two columns in two planes,
-// and activity for all rows of a column takes ~12 bitwise operations, so only
-// active cells (a few percent) take the per-cell path.  A 32x32 bit transpose
-// turns the column masks into each row's active cells in x order.  Warps never
-// wait for each other: there is no block-level barrier in the sweep.
+// to one warp.  For every point plane the warp keeps two bits per sample,
+// "below" and "at or below the isovalue", in 64-bit masks per column (rows
+// 0..33).  The count sweep builds them from the samples: each lane loads four
+// adjacent samples of a row at a time, 8 rows in flight, and compares them (two
+// uint16 samples per word at once).  It also keeps them in a global mask
+// store, from which the emit sweep copies them back with cp.async.bulk
+// instead of reading the samples again.  A cell's configuration is a few
+// shifts on the masks of two columns in two planes, and activity for all
+// rows of a column takes ~12 bitwise operations, so only active cells (a few
+// percent) take the per-cell path.  A 32x32 bit transpose turns the column
+// masks into each row's active cells in x order.  Warps never wait for each
+// other: there is no block-level barrier in the sweep.
 //
 // Output order is the reference's (ascending cell index, x fastest,
 // utils.hpp:72), so the active cells of one plane, row and 128-column
