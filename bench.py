@@ -524,21 +524,29 @@ def run_served(args, rank, world, dist=None):
     clk = clocks.stop()
     # every rank serves its own request stream: whole-job capacity is the sum
     _, total_rps = combine_ranks(0.0, m["served"]["capacity_rps"], dist, "cuda")
-    # end to end: a burst of requests, each mesh copied to host memory and released
+    # end to end: a burst of requests, each mesh copied into page-locked host
+    # buffers (reused; sized from the warm-up meshes, grown if ever short) and released
     vid, iso, _ = request_trace(vols, 128, 0, seed=4)
     d2h = 0
     with fg.Server(0, vertex_arena=SERVED_VERTEX_ARENA, quad_arena=SERVED_QUAD_ARENA) as srv:
         idmap = [srv.add_volume(d["volume"]) for d in vols]
+        vmax = qmax = 1
         for v in range(len(vols)):                     # warm up: each volume once
             r = srv.submit(idmap[v], 0.5 * (vols[v]["lo"] + vols[v]["hi"]))
-            srv.wait(r, timeout=600.0)
+            res = srv.wait(r, timeout=600.0)
+            vmax, qmax = max(vmax, res["n_vertices"]), max(qmax, res["n_quads"])
             srv.release(r)
+        hv = torch.empty((2 * vmax, 3), dtype=torch.float32, pin_memory=True)
+        hq = torch.empty((2 * qmax, 4), dtype=torch.int32, pin_memory=True)
         t0 = time.perf_counter()
         rids = [srv.submit(idmap[v], float(x)) for v, x in zip(vid, iso)]
         for r in rids:
             res = srv.wait(r, timeout=600.0)
-            vv, qq, _ = srv.fetch(res)
-            d2h += vv.nbytes + qq.nbytes
+            if res["n_vertices"] > len(hv) or res["n_quads"] > len(hq):
+                hv = torch.empty((res["n_vertices"], 3), dtype=torch.float32, pin_memory=True)
+                hq = torch.empty((res["n_quads"], 4), dtype=torch.int32, pin_memory=True)
+            nv, nq = srv.fetch_into(res, hv, hq)
+            d2h += 12 * nv + 16 * nq
             srv.release(r)
         e2e_s = time.perf_counter() - t0
     if rank != 0:
@@ -559,7 +567,8 @@ def run_served(args, rank, world, dist=None):
                    "l2": "pool %.2f GB > L2" % (nbytes / 1e9)},
         "cpu_baseline": cpu,
         "e2e": {"value": round(len(rids) / e2e_s, 2), "unit": "requests/s", "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": int(d2h / len(rids)), "note": "pool resident on the device; per request the mesh is copied to host"},
+                "d2h_bytes_per_step": int(d2h / len(rids)),
+                "note": "pool resident on the device; per request the mesh is copied into page-locked host buffers (Server.fetch_into)"},
         "gpu_launches": 7 * m["served"]["stats"]["batches"],
         "clocks": clk,
     }

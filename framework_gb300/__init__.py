@@ -591,6 +591,34 @@ class Server:
         v, q, t = self.tensors(result)
         return v.cpu().numpy(), q.cpu().numpy().view(np.uint32), (t.cpu().numpy().view(np.uint32) if t is not None else None)
 
+    def fetch_into(self, result, vertices, quads, triangles=None):
+        """Copies a result's mesh into caller-owned host buffers: numpy
+        arrays or CPU tensors with at least (V, 3) / (Q, 4) / (2Q, 3) rows.
+        Page-locked ones (e.g. numpy views of pinned torch tensors) copy at
+        the full host-link rate, and nothing is allocated per call.  Returns
+        (n_vertices, n_quads); raises DMCError(OUTPUT_OVERFLOW) with
+        ``.counts`` when a buffer is too small."""
+        import torch
+        v, q, t = self.tensors(result)
+        nv, nq = v.shape[0], q.shape[0]
+        if len(vertices) < nv or len(quads) < nq or (triangles is not None and t is not None and len(triangles) < 2 * nq):
+            e = DMCError(3, "fetch_into")
+            e.counts = (nv, nq)
+            raise e
+
+        def host(a, dtype):
+            # same bits, as the device tensor's dtype (uint32 arrays as int32)
+            if isinstance(a, torch.Tensor):
+                return a.view(dtype)
+            return torch.from_numpy(a.view(np.float32 if dtype == torch.float32 else np.int32))
+        if nv:
+            host(vertices, torch.float32)[:nv].copy_(v)
+        if nq:
+            host(quads, torch.int32)[:nq].copy_(q)
+            if triangles is not None and t is not None:
+                host(triangles, torch.int32)[:2 * nq].copy_(t)
+        return nv, nq
+
     def release(self, request_id):
         _check(self._lib.dmc_server_release(self._h, int(request_id)), "dmc_server_release")
 

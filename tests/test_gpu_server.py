@@ -157,3 +157,31 @@ def test_replay_load_generator(pool_case):
         stats = srv.stats()
     assert (st == 0).all() and (lat > 0).all() and (lat < 30).all()
     assert stats["completed"] == len(reqs)
+
+
+def test_fetch_into_host_buffers(pool_case):
+    """Server.fetch_into copies a result into caller buffers (pinned torch
+    tensors, plain numpy arrays) with the same bits as fetch; short buffers
+    give OUTPUT_OVERFLOW with the counts."""
+    import torch
+    import framework_gb300 as fg
+    vols, reqs, alone = pool_case
+    with fg.Server(0, vertex_arena=1 << 26, quad_arena=1 << 25, triangles=True) as srv:
+        ids = [srv.add_volume(d["volume"], d["xyz_min"], d["xyz_max"]) for d in vols]
+        for v, iso in reqs[:6]:
+            rid = srv.submit(ids[v], iso)
+            res = srv.wait(rid, timeout=120.0)
+            want = alone[(v, iso)]
+            nv, nq = len(want[0]), len(want[1])
+            hv = torch.empty((nv + 5, 3), dtype=torch.float32, pin_memory=True)
+            hq = torch.empty((nq + 5, 4), dtype=torch.int32, pin_memory=True)
+            ht = np.empty((2 * nq + 5, 3), np.uint32)
+            assert srv.fetch_into(res, hv, hq, ht) == (nv, nq)
+            assert np.array_equal(hv[:nv].numpy().view(np.uint32), want[0].view(np.uint32))
+            assert np.array_equal(hq[:nq].numpy().view(np.uint32), want[1])
+            assert np.array_equal(ht[:2 * nq], want[2])
+            if nq > 1:
+                with pytest.raises(fg.DMCError) as e:
+                    srv.fetch_into(res, hv, hq[:nq - 1])
+                assert e.value.status == 3 and e.value.counts == (nv, nq)
+            srv.release(rid)
