@@ -298,21 +298,64 @@ def run_batch(args, rank, world, dist=None):
             ex.extract_device(d["volume"], iso=d["iso"], vertices=vbuf, quads=qbuf)
     torch.cuda.synchronize()
     plain_s = (time.perf_counter() - t0) / plain_reps
-    # end to end: pinned host volumes in, host meshes out, per step
+    # end to end: pinned host volumes in, host meshes out, per step.  The
+    # volumes go up, through and down in 8 groups on two contexts (asynchronous
+    # batches), so that one group's upload, another's extraction and a third's
+    # download overlap; the meshes land at their whole-batch offsets.
     host_pool = torch.empty(pool.shape, dtype=pool.dtype, pin_memory=True)
     host_pool.copy_(pool)
     hv = torch.empty((V, 3), dtype=torch.float32, pin_memory=True)
     hq = torch.empty((Q, 4), dtype=torch.int32, pin_memory=True)
     e2e_steps = max(1, min(args.e2e_steps, args.steps))
+    ex2 = fg.Extractor(local, algo="brick")
+    ex2.set_option(fg.OPT_BRICK_PLANES, int(tune["planes"]))
+    exs = (ex, ex2)
+    n_groups = 8
+    groups = []
+    for g in range(n_groups):
+        a, b = g * n // n_groups, (g + 1) * n // n_groups
+        lo = (vols[a]["volume"].data_ptr() - pool.data_ptr()) // 4
+        hi = (vols[b]["volume"].data_ptr() - pool.data_ptr()) // 4 if b < n else pool.numel()
+        v0, q0 = int(res[a][0]), int(res[a][2])
+        v1 = int(res[b - 1][0] + res[b - 1][1])
+        q1 = int(res[b - 1][2] + res[b - 1][3])
+        groups.append((a, b, lo, hi, v0, v1, q0, q1))
+    s_up, s_dn = torch.cuda.Stream(), torch.cuda.Stream()
+    s_ex = (torch.cuda.Stream(), torch.cuda.Stream())
+
+    def pipelined_pass():
+        busy = [False, False]
+        for g, (a, b, lo, hi, v0, v1, q0, q1) in enumerate(groups):
+            c = g % 2
+            if busy[c]:
+                exs[c].batch_wait()              # the group two back on this context
+            up = torch.cuda.Event()
+            with torch.cuda.stream(s_up):
+                pool[lo:hi].copy_(host_pool[lo:hi], non_blocking=True)
+                up.record(s_up)
+            s_ex[c].wait_event(up)
+            exs[c].extract_batch(vols[a:b], vbuf[v0:v1], qbuf[q0:q1], mode="async", stream=s_ex[c])
+            busy[c] = True
+            done = torch.cuda.Event()
+            done.record(s_ex[c])
+            s_dn.wait_event(done)
+            with torch.cuda.stream(s_dn):
+                hv[v0:v1].copy_(vbuf[v0:v1], non_blocking=True)
+                hq[q0:q1].copy_(qbuf[q0:q1], non_blocking=True)
+        for c in (0, 1):
+            if busy[c]:
+                exs[c].batch_wait()
+        torch.cuda.synchronize()
+
+    pipelined_pass()                             # warm-up (second context, streams)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        pool.copy_(host_pool, non_blocking=True)
-        ex.extract_batch(vols, vbuf, qbuf, mode="graph")
-        ex.batch_wait()
-        hv.copy_(vbuf, non_blocking=True)
-        hq.copy_(qbuf, non_blocking=True)
-        torch.cuda.synchronize()
+        pipelined_pass()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
+    # the host meshes are the whole batch's, bit for bit
+    ex.extract_batch(vols, vbuf, qbuf)
+    assert torch.equal(hv, vbuf.cpu()) and torch.equal(hq, qbuf.cpu())
+    ex2.close()
     line = None
     if rank == 0:
         hbm, peak_kind = peaks()
@@ -342,7 +385,9 @@ def run_batch(args, rank, world, dist=None):
                          "pipeline_frac": round(alg_bytes / (ms * 1e-3) / 1e9 / hbm, 4)},
             "cpu_baseline": cpu,
             "e2e": {"value": round(n / e2e_s, 2), "unit": "volumes/s", "h2d_bytes_per_step": 4 * N,
-                    "d2h_bytes_per_step": 12 * V + 16 * Q, "steps": e2e_steps},
+                    "d2h_bytes_per_step": 12 * V + 16 * Q, "steps": e2e_steps,
+                    "call": "dmc_extract_batch (asynchronous, 8 groups on two contexts) with page-locked "
+                            "host volumes and meshes; uploads, batches and downloads overlap"},
             "gpu_launches": 7 * args.steps,
             "clocks": clk,
         }
