@@ -1208,6 +1208,7 @@ struct BatchState {
     unsigned long long *h_snap = nullptr, *d_snap = nullptr;
     // sharded extraction between its two phases: sample type, z-brick range, bricks per z layer
     bool shard_ready = false;
+    uint64_t sh_scratch_gen = 0;       // the scratch the count phase left its plan and offsets in
     int sh_grp = 0;
     uint32_t sh_zb0 = 0, sh_zb1 = 0;
     uint64_t sh_bxy = 0;
@@ -1577,6 +1578,7 @@ dmc_status brick_extract(Ctx *ctx, const BrickItem *items, uint32_t n, const Bri
     if (s != DMC_OK) return s;
     BatchState &b = *bp;
     if (b.in_flight) return DMC_ERR_INVALID_ARG;
+    b.shard_ready = false;          // this call replaces a sharded count's plan
     uint64_t nb[2] = {0, 0};
     if ((s = stage_plan(ctx, b, items, n, nb)) != DMC_OK) return s;
 
@@ -1686,6 +1688,7 @@ dmc_status brick_run_streamed(Ctx *ctx, const ExtractArgs &a, const StreamIO &io
     if (s != DMC_OK) return s;
     BatchState &b = *bp;
     if (b.in_flight) return DMC_ERR_INVALID_ARG;
+    b.shard_ready = false;          // this call replaces a sharded count's plan
     if ((s = stream_state(b)) != DMC_OK) return s;
     BrickItem it;
     it.data = a.vol; it.dtype = a.dtype; it.pts = a.pts; it.cells = a.cells; it.iso = a.iso; it.mn = a.mn; it.rng = a.rng;
@@ -1889,6 +1892,7 @@ dmc_status brick_shard_count(Ctx *ctx, const BrickItem &item, uint32_t plane0, u
     if (Q) *Q = tq;
     if (ctx->h_ctl->totals[0] >= 0xFFFFFFFFull || ctx->h_ctl->totals[1] >= 0xFFFFFFFFull) return DMC_ERR_OUTPUT_OVERFLOW;
     b.shard_ready = true;
+    b.sh_scratch_gen = ctx->scratch_gen;
     b.sh_grp = grp; b.sh_zb0 = zb0; b.sh_zb1 = zb1; b.sh_bxy = bxy;
     return DMC_OK;
 }
@@ -1897,7 +1901,8 @@ dmc_status brick_shard_emit(Ctx *ctx, uint64_t vertex_offset, const BrickOut &o,
 {
     using namespace brick;
     BatchState *b = ctx->batch;
-    if (!b || !b->shard_ready || b->in_flight) return DMC_ERR_INVALID_ARG;
+    // the count phase must be the context's last brick call, with its scratch still in place
+    if (!b || !b->shard_ready || b->in_flight || b->sh_scratch_gen != ctx->scratch_gen) return DMC_ERR_INVALID_ARG;
     // quad indices: local vertex index + vertex_offset (the emit subtracts vbase)
     Geom *hg = (Geom *)((BatchHead *)b->h_stage + 1);
     hg->vbase = (uint32_t)(0u - (uint32_t)vertex_offset);

@@ -100,3 +100,17 @@ def test_shard_errors(extractor):
     with pytest.raises(fg.DMCError) as e:          # too small buffers
         extractor.shard_emit(0, v, q)
     assert e.value.status == 3
+    # another extraction between the phases replaces the count's plan
+    extractor.shard_count(vol[0:nz].contiguous(), nz, 0, nz - 1, None, None, iso)
+    extractor.extract_device(vol, iso=iso)
+    vb = torch.empty((nv, 3), device="cuda")
+    qb = torch.empty((nq, 4), dtype=torch.int32, device="cuda")
+    with pytest.raises(fg.DMCError) as e:
+        extractor.shard_emit(0, vb, qb)
+    assert e.value.status == 1
+    # a whole-volume shard is the whole mesh
+    extractor.shard_count(vol[0:nz].contiguous(), nz, 0, nz - 1, None, None, iso)
+    extractor.shard_emit(0, vb, qb)
+    wv, wq, _ = _whole(extractor, vol, iso, None, None)
+    assert np.array_equal(vb.cpu().numpy().view(np.uint32), wv.view(np.uint32))
+    assert np.array_equal(qb.cpu().numpy(), wq)
