@@ -468,7 +468,7 @@ def _warm(srv, idmap, vols):
     srv.replay(idmap, iso, np.zeros(len(vols)))
 
 
-def served_measure(vols, n_req=600, quick=False):
+def served_measure(vols, n_req=600, quick=False, device=0):
     """Saturation throughput and a Poisson load sweep for the batched server
     and the plain per-request server on the same traces."""
     import numpy as np
@@ -476,7 +476,7 @@ def served_measure(vols, n_req=600, quick=False):
     out = {}
     servers = {"served": dict(lanes=2, max_batch=64), "plain": dict(plain=True)}
     for name, kw in servers.items():
-        with fg.Server(0, vertex_arena=SERVED_VERTEX_ARENA, quad_arena=SERVED_QUAD_ARENA, **kw) as srv:
+        with fg.Server(device, vertex_arena=SERVED_VERTEX_ARENA, quad_arena=SERVED_QUAD_ARENA, **kw) as srv:
             ids = [srv.add_volume(d["volume"]) for d in vols]
             idmap = np.array(ids, np.uint32)
             _warm(srv, idmap, vols)
@@ -503,7 +503,7 @@ def served_measure(vols, n_req=600, quick=False):
     for label, name, rate in loads:
         kw = servers[name]
         n = max(200, min(n_req, int(rate * (4.0 if not quick else 2.0))))
-        with fg.Server(0, vertex_arena=SERVED_VERTEX_ARENA, quad_arena=SERVED_QUAD_ARENA, **kw) as srv:
+        with fg.Server(device, vertex_arena=SERVED_VERTEX_ARENA, quad_arena=SERVED_QUAD_ARENA, **kw) as srv:
             idmap = np.array([srv.add_volume(d["volume"]) for d in vols], np.uint32)
             _warm(srv, idmap, vols)
             vid, iso, arr = request_trace(vols, n, rate, seed=3)
@@ -560,12 +560,13 @@ def run_served(args, rank, world, dist=None):
     import numpy as np
     import torch
     import framework_gb300 as fg
+    local = int(os.environ.get("LOCAL_RANK", "0"))   # this rank's GPU (the current device)
     vols = make_pool("cuda")
     N = sum(d["volume"].numel() for d in vols)
     nbytes = sum(d["volume"].numel() * d["volume"].element_size() for d in vols)
-    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks = ClockSampler(local)
     clocks.start()
-    m = served_measure(vols, n_req=max(200, 60 * args.steps))
+    m = served_measure(vols, n_req=max(200, 60 * args.steps), device=local)
     clk = clocks.stop()
     # every rank serves its own request stream: whole-job capacity is the sum
     _, total_rps = combine_ranks(0.0, m["served"]["capacity_rps"], dist, "cuda")
@@ -573,7 +574,7 @@ def run_served(args, rank, world, dist=None):
     # buffers (reused; sized from the warm-up meshes, grown if ever short) and released
     vid, iso, _ = request_trace(vols, 128, 0, seed=4)
     d2h = 0
-    with fg.Server(0, vertex_arena=SERVED_VERTEX_ARENA, quad_arena=SERVED_QUAD_ARENA) as srv:
+    with fg.Server(local, vertex_arena=SERVED_VERTEX_ARENA, quad_arena=SERVED_QUAD_ARENA) as srv:
         idmap = [srv.add_volume(d["volume"]) for d in vols]
         vmax = qmax = 1
         for v in range(len(vols)):                     # warm up: each volume once
