@@ -49,7 +49,7 @@ def _load(path):
 
 def _save(path, data):
     os.makedirs(os.path.dirname(path), exist_ok=True)
-    tmp = path + ".tmp"
+    tmp = "%s.%d.tmp" % (path, os.getpid())   # ranks of one job may save at the same time
     with open(tmp, "w") as f:
         json.dump(data, f, indent=1, sort_keys=True)
     os.replace(tmp, path)
