@@ -91,6 +91,21 @@ def test_noise_u16_medium(algo_extractor):
     _check(ex.run(vol, iso=32768.0), r)
 
 
+@pytest.mark.parametrize("iso", [-3.0, 0.0, 0.5, 1.0, 1.5, 32767.5, 32768.0, 65534.5, 65535.0, 65535.5, 70000.0])
+def test_u16_thresholds_wide(algo_extractor, iso):
+    """uint16 volumes wide enough (x a multiple of 4, at least 128 columns) for
+    the brick path's four-samples-per-load, two-per-word compare, at isovalues
+    on and between the extreme sample values (nothing or everything below;
+    "at or below" differing from "below")."""
+    ex, _ = algo_extractor
+    rng = np.random.default_rng(77)
+    shape = (23, 37, 256)
+    vol = np.array([0, 1, 32768, 65535], np.uint16)[rng.integers(0, 4, shape)]
+    some = rng.random(shape) < 0.2                      # and a fifth anywhere in the range
+    vol[some] = rng.integers(0, 65536, int(some.sum())).astype(np.uint16)
+    _check(ex.run(vol, iso=iso), oracle.extract(vol, iso=iso))
+
+
 def test_blobs_128(algo_extractor):
     from framework_gb300 import fields
     ex, _ = algo_extractor
