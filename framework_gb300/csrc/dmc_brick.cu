@@ -1200,6 +1200,10 @@ struct BatchState {
     cudaGraphNode_t emit_node[2] = {nullptr, nullptr};
     cudaKernelNodeParams emit_params[2]{};
     brick::EmitOut g_out{};
+    // the count sweeps and the scan, whose grids are resized to each batch
+    cudaGraphNode_t count_node[2] = {nullptr, nullptr}, scan_node = nullptr;
+    cudaKernelNodeParams count_params[2]{}, scan_params{};
+    int g_grid[2][2] = {{0, 0}, {0, 0}}, g_scan_grid = 0;   // grids the instantiated graph runs now
     // streamed host extraction: copy streams, per-slab events and mapped
     // snapshots of the running totals (vertices, quads, error word per slab)
     cudaStream_t s_in = nullptr, s_out = nullptr;
@@ -1423,6 +1427,8 @@ static dmc_status capture_graph(Ctx *ctx, BatchState &b, const brick::EmitOut &e
     if (b.gexec) { cudaGraphExecDestroy(b.gexec); b.gexec = nullptr; }
     if (b.graph) { cudaGraphDestroy(b.graph); b.graph = nullptr; }
     b.emit_node[0] = b.emit_node[1] = nullptr;
+    b.count_node[0] = b.count_node[1] = nullptr;
+    b.scan_node = nullptr;
     cudaGraph_t graph = nullptr;
     CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     dmc_status cs = enqueue_front(ctx, b, b.d_res, false, nb, true, ctx->stream);
@@ -1430,7 +1436,7 @@ static dmc_status capture_graph(Ctx *ctx, BatchState &b, const brick::EmitOut &e
     cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
     if (cs != DMC_OK) { if (graph) cudaGraphDestroy(graph); return cs; }
     CUDA_TRY(ce);
-    // the emit nodes, found by kernel
+    // the sweep and scan nodes, found by kernel
     size_t nn = 0;
     CUDA_TRY(cudaGraphGetNodes(graph, nullptr, &nn));
     std::vector<cudaGraphNode_t> nodes(nn);
@@ -1442,11 +1448,22 @@ static dmc_status capture_graph(Ctx *ctx, BatchState &b, const brick::EmitOut &e
         cudaKernelNodeParams kp;
         CUDA_TRY(cudaGraphKernelNodeGetParams(nd, &kp));
         for (int g = 0; g < 2; ++g) {
-            const void *fn = g ? (const void *)brick_sweep<uint16_t, true> : (const void *)brick_sweep<float, true>;
-            if (kp.func == fn) { b.emit_node[g] = nd; b.emit_params[g] = kp; }
+            const void *fe = g ? (const void *)brick_sweep<uint16_t, true> : (const void *)brick_sweep<float, true>;
+            const void *fc = g ? (const void *)brick_sweep<uint16_t, false> : (const void *)brick_sweep<float, false>;
+            if (kp.func == fe) { b.emit_node[g] = nd; b.emit_params[g] = kp; }
+            if (kp.func == fc) { b.count_node[g] = nd; b.count_params[g] = kp; }
         }
+        if (kp.func == (const void *)seg_scan) { b.scan_node = nd; b.scan_params = kp; }
     }
-    if (!b.emit_node[0] || !b.emit_node[1]) { cudaGraphDestroy(graph); return DMC_ERR_CUDA; }
+    if (!b.emit_node[0] || !b.emit_node[1] || !b.count_node[0] || !b.count_node[1] || !b.scan_node) {
+        cudaGraphDestroy(graph);
+        return DMC_ERR_CUDA;
+    }
+    for (int g = 0; g < 2; ++g) {
+        b.g_grid[g][0] = (int)b.count_params[g].gridDim.x;
+        b.g_grid[g][1] = (int)b.emit_params[g].gridDim.x;
+    }
+    b.g_scan_grid = (int)b.scan_params.gridDim.x;
     ce = cudaGraphInstantiate(&b.gexec, graph, 0);
     if (ce != cudaSuccess) { cudaGraphDestroy(graph); CUDA_TRY(ce); }
     b.graph = graph;
@@ -1457,11 +1474,34 @@ static dmc_status capture_graph(Ctx *ctx, BatchState &b, const brick::EmitOut &e
 }
 
 // Points the graph's emit sweeps at other output buffers (same arguments as
-// the launches in enqueue_back, with a new EmitOut).
-static dmc_status retarget_graph(Ctx *ctx, BatchState &b, const brick::EmitOut &eo)
+// the launches in enqueue_back, with a new EmitOut) and sizes the sweep and
+// scan grids to this batch's bricks and tiles (a small batch then starts no
+// idle persistent blocks).  Nodes are rewritten only when something changed.
+static dmc_status retarget_graph(Ctx *ctx, BatchState &b, const brick::EmitOut &eo, const uint64_t nb[2])
 {
     using namespace brick;
-    if (same_out(eo, b.g_out)) return DMC_OK;
+    const uint32_t n_tiles = ((const BatchHead *)b.h_stage)->n_tiles;
+    const int scan_grid = (int)std::max<uint32_t>(1u, std::min<uint32_t>(2u * ctx->num_sms, n_tiles));
+    if (scan_grid != b.g_scan_grid) {
+        cudaKernelNodeParams kp = b.scan_params;
+        kp.gridDim = dim3((unsigned)scan_grid);
+        CUDA_TRY(cudaGraphExecKernelNodeSetParams(b.gexec, b.scan_node, &kp));
+        b.g_scan_grid = scan_grid;
+    }
+    bool emit_grid_changed = false;
+    int want[2][2];
+    for (int g = 0; g < 2; ++g) {
+        want[g][0] = sweep_blocks(b, g, false, nb[g], false);
+        want[g][1] = sweep_blocks(b, g, true, nb[g], false);
+        if (want[g][0] != b.g_grid[g][0]) {
+            cudaKernelNodeParams kp = b.count_params[g];
+            kp.gridDim = dim3((unsigned)want[g][0]);
+            CUDA_TRY(cudaGraphExecKernelNodeSetParams(b.gexec, b.count_node[g], &kp));
+            b.g_grid[g][0] = want[g][0];
+        }
+        emit_grid_changed |= want[g][1] != b.g_grid[g][1];
+    }
+    if (same_out(eo, b.g_out) && !emit_grid_changed) return DMC_OK;
     for (uint32_t g = 0; g < 2; ++g) {
         const BatchHead *a_head = b.d_plan;
         uint32_t a_group = g;
@@ -1478,7 +1518,9 @@ static dmc_status retarget_graph(Ctx *ctx, BatchState &b, const brick::EmitOut &
         cudaKernelNodeParams kp = b.emit_params[g];
         kp.kernelParams = args;
         kp.extra = nullptr;
+        kp.gridDim = dim3((unsigned)want[g][1]);
         CUDA_TRY(cudaGraphExecKernelNodeSetParams(b.gexec, b.emit_node[g], &kp));
+        b.g_grid[g][1] = want[g][1];
     }
     b.g_out = eo;
     return DMC_OK;
@@ -1591,7 +1633,7 @@ dmc_status brick_extract(Ctx *ctx, const BrickItem *items, uint32_t n, const Bri
         if (!b.gexec || b.g_layout_id != b.layout_id || b.g_stage_gen != b.stage_gen) {
             if ((s = capture_graph(ctx, b, eo, nb)) != DMC_OK) return s;
         }
-        if ((s = retarget_graph(ctx, b, eo)) != DMC_OK) return s;
+        if ((s = retarget_graph(ctx, b, eo, nb)) != DMC_OK) return s;
         CUDA_TRY(cudaGraphLaunch(b.gexec, st));
         if (o.d_results)
             CUDA_TRY(cudaMemcpyAsync(o.d_results, b.d_res, sizeof(dmc_batch_result) * (size_t)n, cudaMemcpyDeviceToDevice, st));
