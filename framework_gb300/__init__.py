@@ -184,6 +184,29 @@ def _check(status, what=""):
         raise DMCError(status, what)
 
 
+class _MeshBuffers:
+    """Owns the host buffers of one dmc_run mesh.  Each numpy array handed out
+    keeps this object alive through its buffer, so dmc_mesh_free runs when
+    the last of them is collected."""
+
+    def __init__(self, lib, mesh):
+        self._lib, self._mesh = lib, mesh
+
+    def array(self, ptr, ctype, rows, cols):
+        n = rows * cols
+        if n == 0:
+            return np.zeros((0, cols), dtype=np.dtype(ctype))
+        buf = (ctype * n).from_address(ctypes.addressof(ptr.contents))
+        buf._owner = self
+        return np.frombuffer(buf, dtype=np.dtype(ctype)).reshape(rows, cols)
+
+    def __del__(self):
+        try:
+            self._lib.dmc_mesh_free(ctypes.byref(self._mesh))
+        except Exception:
+            pass
+
+
 class Mesh:
     """Extraction result in host memory: vertices (V,3) float32, quads (Q,4)
     uint32 and, when requested, triangles (2Q,3) uint32 in the reference's
@@ -276,15 +299,13 @@ class Extractor:
         m = _Mesh()
         _check(self._lib.dmc_run(self._h, ctypes.byref(vol), _f3(mn), _f3(mx), ctypes.c_float(iso),
                                  int(num_smooth), 1 if triangles else 0, ctypes.byref(m)), "dmc_run")
-        try:
-            V, Q = int(m.n_vertices), int(m.n_quads)
-            verts = np.ctypeslib.as_array(m.vertices, shape=(3 * V,)).reshape(V, 3).copy() if V else np.zeros((0, 3), np.float32)
-            quads = np.ctypeslib.as_array(m.quads, shape=(4 * Q,)).reshape(Q, 4).copy() if Q else np.zeros((0, 4), np.uint32)
-            tris = None
-            if triangles:
-                tris = np.ctypeslib.as_array(m.triangles, shape=(6 * Q,)).reshape(2 * Q, 3).copy() if Q else np.zeros((0, 3), np.uint32)
-        finally:
-            self._lib.dmc_mesh_free(ctypes.byref(m))
+        # the arrays wrap the library's buffers (no copy); they are released
+        # with dmc_mesh_free once the last array referring to them is gone
+        owner = _MeshBuffers(self._lib, m)
+        V, Q = int(m.n_vertices), int(m.n_quads)
+        verts = owner.array(m.vertices, ctypes.c_float, V, 3)
+        quads = owner.array(m.quads, ctypes.c_uint32, Q, 4)
+        tris = owner.array(m.triangles, ctypes.c_uint32, 2 * Q, 3) if triangles else None
         return Mesh(verts, quads, tris, self.stats())
 
     def run_into(self, volume, vertices, quads, triangles=None, xyz_min=None, xyz_max=None, iso=0.0, num_smooth=0):
@@ -293,19 +314,23 @@ class Extractor:
         ``volume`` is a numpy [z,y,x] float32/uint16 array; ``vertices``
         (float32 [V,3]), ``quads`` (uint32/int32 [Q,4]) and ``triangles``
         ([2Q,3] or None) are host arrays, e.g. numpy views of pinned torch
-        tensors.  Returns (n_vertices, n_quads); raises DMCError carrying the
-        needed counts in ``.counts`` when the buffers are too small."""
+        tensors.  ``quads`` may be None when ``triangles`` is given: the
+        reference's outputs, vertices and triangles.  Returns (n_vertices,
+        n_quads); raises DMCError carrying the needed counts in ``.counts``
+        when the buffers are too small."""
         arr, vol = _host_volume(volume)
         mn, mx = _default_extent(vol.dims, xyz_min, xyz_max)
+        if quads is None and triangles is None:
+            raise DMCError(1, "run_into needs a quad or a triangle buffer")
         for name, b in (("vertices", vertices), ("quads", quads), ("triangles", triangles)):
             if b is not None and not b.flags["C_CONTIGUOUS"]:
                 raise DMCError(1, "%s must be C-contiguous" % name)
-        qcap = quads.size // 4
-        if triangles is not None:
-            qcap = min(qcap, triangles.size // 6)
+        caps = ([quads.size // 4] if quads is not None else []) + ([triangles.size // 6] if triangles is not None else [])
+        qcap = min(caps)
         nv, nq = ctypes.c_uint64(), ctypes.c_uint64()
         rc = self._lib.dmc_run_into(self._h, ctypes.byref(vol), _f3(mn), _f3(mx), ctypes.c_float(iso), int(num_smooth),
-                                    vertices.ctypes.data, vertices.size // 3, quads.ctypes.data, qcap,
+                                    vertices.ctypes.data, vertices.size // 3,
+                                    quads.ctypes.data if quads is not None else None, qcap,
                                     triangles.ctypes.data if triangles is not None else None,
                                     ctypes.byref(nv), ctypes.byref(nq))
         if rc != 0:

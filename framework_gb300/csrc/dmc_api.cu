@@ -2,7 +2,9 @@
 // device forms of the extraction.
 #include <stdlib.h>
 #include <string.h>
+#include <unistd.h>
 #include <new>
+#include <thread>
 #include "dmc_internal.h"
 #include <vector>
 
@@ -493,6 +495,39 @@ static dmc_status download(dmc_ctx *ctx, uint64_t V, uint64_t Q, float *hv, uint
     return DMC_OK;
 }
 
+// Write one byte per page of freshly allocated host buffers, from several
+// threads.  The pages of a large malloc are mapped on first touch; taking
+// those faults in parallel here is many times faster than taking them one at
+// a time inside the device-to-host copy (or the driver's staging copy).
+static void touch_pages(void *const *bufs, const uint64_t *bytes, int n)
+{
+    const long ps = sysconf(_SC_PAGESIZE);
+    const uint64_t page = ps > 0 ? (uint64_t)ps : 4096;
+    uint64_t total = 0;
+    for (int i = 0; i < n; ++i) total += bytes[i];
+    unsigned nt = std::thread::hardware_concurrency();
+    nt = std::min<unsigned>(nt ? nt : 1, 32);
+    if (total < (32ull << 20) || nt < 2) return;   // small meshes: the copy takes the faults
+    const uint64_t share = (total / nt + page - 1) / page * page;
+    auto work = [=](uint64_t lo, uint64_t hi) {
+        uint64_t base = 0;
+        for (int i = 0; i < n; ++i) {
+            const uint64_t b0 = std::max(lo, base), b1 = std::min(hi, base + bytes[i]);
+            for (uint64_t o = b0; o < b1; o += page) ((volatile char *)bufs[i])[o - base] = 0;
+            base += bytes[i];
+        }
+    };
+    std::vector<std::thread> th;
+    try {
+        for (unsigned k = 1; k < nt && k * share < total; ++k)
+            th.emplace_back(work, k * share, std::min(total, (k + 1) * share));
+    } catch (...) {
+        // no more threads: the ones started and this one cover what they can
+    }
+    work(0, std::min(total, share));
+    for (auto &t : th) t.join();
+}
+
 dmc_status dmc_run(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min[3], const float xyz_max[3],
                    float iso, uint32_t num_smooth, int want_triangles, dmc_mesh *out)
 {
@@ -506,6 +541,9 @@ dmc_status dmc_run(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min[3], 
     out->quads = (uint32_t *)malloc(Q ? 16 * Q : 1);
     if (want_triangles) out->triangles = (uint32_t *)malloc(Q ? 24 * Q : 1);
     if (!out->vertices || !out->quads || (want_triangles && !out->triangles)) { dmc_mesh_free(out); return DMC_ERR_OOM; }
+    void *bufs[3] = {out->vertices, out->quads, out->triangles};
+    const uint64_t sizes[3] = {12 * V, 16 * Q, want_triangles ? 24 * Q : 0};
+    touch_pages(bufs, sizes, 3);
     return download(ctx, V, Q, out->vertices, out->quads, want_triangles ? out->triangles : nullptr);
 }
 
@@ -515,7 +553,7 @@ dmc_status dmc_run_into(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min
                         uint64_t *n_vertices, uint64_t *n_quads)
 {
     if (!ctx || !n_vertices || !n_quads) return DMC_ERR_INVALID_ARG;
-    if ((vertex_capacity && !h_vertices) || (quad_capacity && !h_quads)) return DMC_ERR_INVALID_ARG;
+    if ((vertex_capacity && !h_vertices) || (quad_capacity && !h_quads && !h_triangles)) return DMC_ERR_INVALID_ARG;
     *n_vertices = 0; *n_quads = 0;
     uint64_t V = 0, Q = 0;
     bool dev_short = false;

@@ -1828,7 +1828,8 @@ dmc_status brick_run_streamed(Ctx *ctx, const ExtractArgs &a, const StreamIO &io
             if (tv > pv)
                 CUDA_TRY(cudaMemcpyAsync(io.hv + 3 * pv, a.verts + 3 * pv, 12 * (tv - pv), cudaMemcpyDeviceToHost, b.s_out));
             if (tq > pq) {
-                CUDA_TRY(cudaMemcpyAsync(io.hq + 4 * pq, a.quads + 4 * pq, 16 * (tq - pq), cudaMemcpyDeviceToHost, b.s_out));
+                if (io.hq)
+                    CUDA_TRY(cudaMemcpyAsync(io.hq + 4 * pq, a.quads + 4 * pq, 16 * (tq - pq), cudaMemcpyDeviceToHost, b.s_out));
                 if (io.ht)
                     CUDA_TRY(cudaMemcpyAsync(io.ht + 6 * pq, a.tris + 6 * pq, 24 * (tq - pq), cudaMemcpyDeviceToHost, b.s_out));
             }

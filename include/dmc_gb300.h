@@ -119,11 +119,15 @@ dmc_status dmc_run(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min[3], 
 /* dmc_run into caller-owned HOST buffers (no reference counterpart; same
  * extraction): vertices (3 floats each), quads (4 indices) and, when
  * h_triangles is not NULL, triangles (6 indices per quad) with the given
- * capacities in vertices / quads.  Nothing is allocated per call, and with
- * page-locked (pinned) buffers both copies run at the full host-link rate:
- * the form to use when meshes are large or calls frequent.  When the mesh is
- * larger than the capacities the call returns DMC_ERR_OUTPUT_OVERFLOW with
- * the needed counts in *n_vertices / *n_quads and copies nothing. */
+ * capacities in vertices / quads.  h_quads may be NULL when h_triangles is
+ * not: the call then returns what dmc::run_dmc returns, vertices and
+ * triangles, and quad_capacity bounds the triangles (two per quad).
+ * Nothing is allocated per call, and with page-locked (pinned) buffers both
+ * copies run at the full host-link rate: the form to use when meshes are
+ * large or calls frequent.  When the mesh is larger than the capacities the
+ * call returns DMC_ERR_OUTPUT_OVERFLOW with the needed counts in
+ * *n_vertices / *n_quads; writes stay within the capacities, and the
+ * buffers' contents are undefined. */
 dmc_status dmc_run_into(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min[3], const float xyz_max[3],
                         float iso, uint32_t num_smooth, float *h_vertices, uint64_t vertex_capacity,
                         uint32_t *h_quads, uint64_t quad_capacity, uint32_t *h_triangles,

@@ -185,11 +185,15 @@ def test_run_into_streamed(kind):
         assert V > 10000 and Q > 5000
         ref = (m.vertices.view(np.uint32), m.quads, m.triangles)
 
-    def check(ex, bufs, tris=True):
+    def check(ex, bufs, tris=True, quads=True):
         hv, hq, ht = bufs
         hv.fill(-1), hq.fill(-1), ht.fill(-1)
-        assert ex.run_into(host, hv, hq, ht if tris else None, mn, mx, iso) == (V, Q)
-        assert np.array_equal(hv.view(np.uint32), ref[0]) and np.array_equal(hq.view(np.uint32), ref[1])
+        assert ex.run_into(host, hv, hq if quads else None, ht if tris else None, mn, mx, iso) == (V, Q)
+        assert np.array_equal(hv.view(np.uint32), ref[0])
+        if quads:
+            assert np.array_equal(hq.view(np.uint32), ref[1])
+        else:
+            assert (hq.view(np.uint32) == 0xFFFFFFFF).all()   # not written
         if tris:
             assert np.array_equal(ht.view(np.uint32), ref[2])
 
@@ -205,6 +209,7 @@ def test_run_into_streamed(kind):
                 bufs = _host_out(V, Q, pinned)
                 check(ex, bufs)
                 check(ex, bufs, tris=False)
+                check(ex, bufs, quads=False)   # the reference's outputs: vertices and triangles
             st = ex.stats()
             assert (st["n_vertices"], st["n_quads"]) == (V, Q)
         hv, hq, ht = _host_out(V, Q, True)
@@ -242,3 +247,31 @@ def test_run_into_matches_run(extractor):
     with pytest.raises(fg.DMCError) as e:
         extractor.run_into(host, pv[:V - 1], pq, None, (-1, 0, 2), (5, 4, 9), 32768.0)
     assert e.value.status == 3 and e.value.counts == (V, Q)
+    # vertices and triangles only, as dmc::run_dmc returns them
+    pt = np.full((2 * Q, 3), 0xFFFFFFFF, np.uint32)
+    assert extractor.run_into(host, pv, None, pt, (-1, 0, 2), (5, 4, 9), 32768.0) == (V, Q)
+    assert np.array_equal(pt, m.triangles)
+    with pytest.raises(fg.DMCError) as e:
+        extractor.run_into(host, pv, None, pt[:2 * Q - 2], (-1, 0, 2), (5, 4, 9), 32768.0)
+    assert e.value.status == 3 and e.value.counts == (V, Q)
+    with pytest.raises(fg.DMCError):
+        extractor.run_into(host, pv, None, None, (-1, 0, 2), (5, 4, 9), 32768.0)
+
+
+def test_run_arrays_own_the_mesh(extractor):
+    """dmc_run's arrays wrap the library's buffers without a copy; each one
+    stays valid on its own after the Mesh and the other arrays are gone."""
+    import gc
+    from framework_gb300 import fields
+    vol = fields.value_noise_u16((96, 80, 72), base_period=12, seed=4)
+    host = fields.as_u16_numpy(vol)
+    r = oracle.extract(host, iso=30000.0)
+    m = extractor.run(host, iso=30000.0, triangles=True)
+    tris = m.triangles[1:]
+    verts = m.vertices
+    del m
+    gc.collect()
+    big = [np.ones(1 << 20, np.float64) for _ in range(8)]   # reuse freed memory, if any was freed
+    assert np.array_equal(verts.view(np.uint32), r["vertices"].view(np.uint32))
+    assert np.array_equal(tris, r["triangles"][1:]) and not verts.flags["OWNDATA"]
+    del big
