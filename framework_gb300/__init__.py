@@ -12,6 +12,7 @@ All extraction runs in the CUDA library; there is no CPU fallback.  Importing
 works without a GPU, but every call that extracts fails loudly when the
 library or a CUDA device is missing.
 """
+import contextlib
 import ctypes
 import os
 
@@ -616,13 +617,19 @@ class Server:
         v, q, t = self.tensors(result)
         return v.cpu().numpy(), q.cpu().numpy().view(np.uint32), (t.cpu().numpy().view(np.uint32) if t is not None else None)
 
-    def fetch_into(self, result, vertices, quads, triangles=None):
+    def fetch_into(self, result, vertices, quads, triangles=None, stream=None):
         """Copies a result's mesh into caller-owned host buffers: numpy
         arrays or CPU tensors with at least (V, 3) / (Q, 4) / (2Q, 3) rows.
         Page-locked ones (e.g. numpy views of pinned torch tensors) copy at
         the full host-link rate, and nothing is allocated per call.  Returns
         (n_vertices, n_quads); raises DMCError(OUTPUT_OVERFLOW) with
-        ``.counts`` when a buffer is too small."""
+        ``.counts`` when a buffer is too small.
+
+        With ``stream`` (a torch.cuda.Stream) the copies are only enqueued
+        there, after the work already queued on it: the call returns at once,
+        and the caller synchronises the stream (or an event recorded on it)
+        before it reads the buffers or releases the request, whose device
+        memory the copies read."""
         import torch
         v, q, t = self.tensors(result)
         nv, nq = v.shape[0], q.shape[0]
@@ -636,12 +643,14 @@ class Server:
             if isinstance(a, torch.Tensor):
                 return a.view(dtype)
             return torch.from_numpy(a.view(np.float32 if dtype == torch.float32 else np.int32))
-        if nv:
-            host(vertices, torch.float32)[:nv].copy_(v)
-        if nq:
-            host(quads, torch.int32)[:nq].copy_(q)
-            if triangles is not None and t is not None:
-                host(triangles, torch.int32)[:2 * nq].copy_(t)
+        nb = stream is not None
+        with torch.cuda.stream(stream) if nb else contextlib.nullcontext():
+            if nv:
+                host(vertices, torch.float32)[:nv].copy_(v, non_blocking=nb)
+            if nq:
+                host(quads, torch.int32)[:nq].copy_(q, non_blocking=nb)
+                if triangles is not None and t is not None:
+                    host(triangles, torch.int32)[:2 * nq].copy_(t, non_blocking=nb)
         return nv, nq
 
     def release(self, request_id):

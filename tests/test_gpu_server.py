@@ -185,3 +185,45 @@ def test_fetch_into_host_buffers(pool_case):
                     srv.fetch_into(res, hv, hq[:nq - 1])
                 assert e.value.status == 3 and e.value.counts == (nv, nq)
             srv.release(rid)
+
+
+def test_fetch_into_on_stream(pool_case):
+    """fetch_into with a stream only enqueues the copies: a burst of results
+    fetched into a ring of pinned buffers, each request released after an
+    event on the copy stream, gives every mesh with fetch's bits."""
+    import torch
+    import framework_gb300 as fg
+    vols, reqs, alone = pool_case
+    cs = torch.cuda.Stream()
+    with fg.Server(0, vertex_arena=1 << 26, quad_arena=1 << 25, triangles=True) as srv:
+        ids = [srv.add_volume(d["volume"], d["xyz_min"], d["xyz_max"]) for d in vols]
+        vmax = max(len(w[0]) for w in alone.values()) + 1
+        qmax = max(len(w[1]) for w in alone.values()) + 1
+        bufs = [(torch.empty((vmax, 3), dtype=torch.float32, pin_memory=True),
+                 torch.empty((qmax, 4), dtype=torch.int32, pin_memory=True),
+                 torch.empty((2 * qmax, 3), dtype=torch.int32, pin_memory=True)) for _ in range(3)]
+        rids = [srv.submit(ids[v], iso) for v, iso in reqs]
+        pending = []
+        for i, (rid, key) in enumerate(zip(rids, reqs)):
+            if len(pending) == 3:
+                _check_fetched(srv, *pending.pop(0), alone)
+            hv, hq, ht = bufs[i % 3]
+            res = srv.wait(rid, timeout=120.0)
+            n = srv.fetch_into(res, hv, hq, ht, stream=cs)
+            ev = torch.cuda.Event()
+            ev.record(cs)
+            pending.append((rid, key, n, ev, (hv, hq, ht)))
+        for p in pending:
+            _check_fetched(srv, *p, alone)
+
+
+def _check_fetched(srv, rid, key, n, ev, bufs, alone):
+    ev.synchronize()
+    srv.release(rid)
+    hv, hq, ht = bufs
+    want = alone[key]
+    nv, nq = n
+    assert (nv, nq) == (len(want[0]), len(want[1]))
+    assert np.array_equal(hv[:nv].numpy().view(np.uint32), want[0].view(np.uint32))
+    assert np.array_equal(hq[:nq].numpy().view(np.uint32), want[1])
+    assert np.array_equal(ht[:2 * nq].numpy().view(np.uint32), want[2])
