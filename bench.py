@@ -301,7 +301,11 @@ def run_batch(args, rank, world, dist=None):
     # end to end: pinned host volumes in, host meshes out, per step.  The
     # volumes go up, through and down in 8 groups on two contexts (asynchronous
     # batches), so that one group's upload, another's extraction and a third's
-    # download overlap; the meshes land at their whole-batch offsets.
+    # download overlap.  Each group extracts into a device region of 1.25 times
+    # its counts in the step before (the sizing pass for the first step); once
+    # batch_wait has returned a group's counts, exactly its mesh is copied
+    # down, after the meshes of the groups before it.  (The batch is the same
+    # every step, so the regions are sized once.)
     host_pool = torch.empty(pool.shape, dtype=pool.dtype, pin_memory=True)
     host_pool.copy_(pool)
     hv = torch.empty((V, 3), dtype=torch.float32, pin_memory=True)
@@ -316,43 +320,59 @@ def run_batch(args, rank, world, dist=None):
         a, b = g * n // n_groups, (g + 1) * n // n_groups
         lo = (vols[a]["volume"].data_ptr() - pool.data_ptr()) // 4
         hi = (vols[b]["volume"].data_ptr() - pool.data_ptr()) // 4 if b < n else pool.numel()
-        v0, q0 = int(res[a][0]), int(res[a][2])
-        v1 = int(res[b - 1][0] + res[b - 1][1])
-        q1 = int(res[b - 1][2] + res[b - 1][3])
-        groups.append((a, b, lo, hi, v0, v1, q0, q1))
+        groups.append((a, b, lo, hi))
+    sizing = [(int(res[b - 1][0] + res[b - 1][1] - res[a][0]), int(res[b - 1][2] + res[b - 1][3] - res[a][2]))
+              for a, b, _, _ in groups]
+    caps = [(v * 5 // 4 + 64, q * 5 // 4 + 64) for v, q in sizing]
+    cv = [sum(c[0] for c in caps[:g]) for g in range(n_groups)]
+    cq = [sum(c[1] for c in caps[:g]) for g in range(n_groups)]
+    del vbuf, qbuf
+    dv = torch.empty((cv[-1] + caps[-1][0], 3), dtype=torch.float32, device=f"cuda:{local}")
+    dq = torch.empty((cq[-1] + caps[-1][1], 4), dtype=torch.int32, device=f"cuda:{local}")
     s_up, s_dn = torch.cuda.Stream(), torch.cuda.Stream()
     s_ex = (torch.cuda.Stream(), torch.cuda.Stream())
+    e2e_bytes = [0, 0]
 
     def pipelined_pass():
-        busy = [False, False]
-        for g, (a, b, lo, hi, v0, v1, q0, q1) in enumerate(groups):
+        pend = [None, None]
+        off = [0, 0]
+
+        def finish(c):
+            g = pend[c]
+            nv_g, nq_g, _ = exs[c].batch_wait()
+            with torch.cuda.stream(s_dn):
+                hv[off[0]:off[0] + nv_g].copy_(dv[cv[g]:cv[g] + nv_g], non_blocking=True)
+                hq[off[1]:off[1] + nq_g].copy_(dq[cq[g]:cq[g] + nq_g], non_blocking=True)
+            off[0] += nv_g
+            off[1] += nq_g
+            pend[c] = None
+        t0 = time.perf_counter()
+        for g, (a, b, lo, hi) in enumerate(groups):
             c = g % 2
-            if busy[c]:
-                exs[c].batch_wait()              # the group two back on this context
+            if pend[c] is not None:
+                finish(c)                         # the group two back on this context
             up = torch.cuda.Event()
             with torch.cuda.stream(s_up):
                 pool[lo:hi].copy_(host_pool[lo:hi], non_blocking=True)
                 up.record(s_up)
             s_ex[c].wait_event(up)
-            exs[c].extract_batch(vols[a:b], vbuf[v0:v1], qbuf[q0:q1], mode="async", stream=s_ex[c])
-            busy[c] = True
-            done = torch.cuda.Event()
-            done.record(s_ex[c])
-            s_dn.wait_event(done)
-            with torch.cuda.stream(s_dn):
-                hv[v0:v1].copy_(vbuf[v0:v1], non_blocking=True)
-                hq[q0:q1].copy_(qbuf[q0:q1], non_blocking=True)
-        for c in (0, 1):
-            if busy[c]:
-                exs[c].batch_wait()
+            exs[c].extract_batch(vols[a:b], dv[cv[g]:cv[g] + caps[g][0]], dq[cq[g]:cq[g] + caps[g][1]],
+                                 mode="async", stream=s_ex[c])
+            pend[c] = g
+        for c in (n_groups % 2, (n_groups + 1) % 2):
+            if pend[c] is not None:
+                finish(c)
         torch.cuda.synchronize()
+        e2e_bytes[0], e2e_bytes[1] = off
+        return time.perf_counter() - t0
 
     pipelined_pass()                             # warm-up (second context, streams)
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        pipelined_pass()
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_s = sum(pipelined_pass() for _ in range(e2e_steps)) / e2e_steps
     # the host meshes are the whole batch's, bit for bit
+    assert tuple(e2e_bytes) == (V, Q)
+    del dv, dq
+    vbuf = torch.empty((V, 3), dtype=torch.float32, device=f"cuda:{local}")
+    qbuf = torch.empty((Q, 4), dtype=torch.int32, device=f"cuda:{local}")
     ex.extract_batch(vols, vbuf, qbuf)
     assert torch.equal(hv, vbuf.cpu()) and torch.equal(hq, qbuf.cpu())
     ex2.close()
@@ -387,7 +407,8 @@ def run_batch(args, rank, world, dist=None):
             "e2e": {"value": round(n / e2e_s, 2), "unit": "volumes/s", "h2d_bytes_per_step": 4 * N,
                     "d2h_bytes_per_step": 12 * V + 16 * Q, "steps": e2e_steps,
                     "call": "dmc_extract_batch (asynchronous, 8 groups on two contexts) with page-locked "
-                            "host volumes and meshes; uploads, batches and downloads overlap"},
+                            "host volumes and meshes; uploads, batches and downloads overlap; each group's "
+                            "download is sized by its own counts, after its batch_wait"},
             "gpu_launches": 7 * args.steps,
             "clocks": clk,
         }
