@@ -719,6 +719,13 @@ def main():
     N = vol.numel()
     ex = fg.Extractor(local, algo="brick")
     V, Q = ex.extract_device(vol, iso=iso)     # no output buffers: count only
+    # pre-screen: samples equal to the isovalue (the cases where the < and <=
+    # tests of the reference disagree)
+    if dtype == "uint16":
+        u = int(iso)
+        at_iso = int((vol == (u - 65536 if u >= 32768 else u)).sum()) if float(iso).is_integer() and 0 <= iso < 65536 else 0
+    else:
+        at_iso = int((vol == iso).sum())
     vbuf = torch.empty((max(V, 1), 3), device="cuda")
     qbuf = torch.empty((max(Q, 1), 4), dtype=torch.int32, device="cuda")
     stream = torch.cuda.current_stream()
@@ -731,12 +738,13 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    emit_ms, count_ms, scan_ms = [], [], []
+    emit_ms, count_ms, scan_ms, step_ms = [], [], [], []
     ev0.record(stream)
     for _ in range(args.steps):
         ex.extract_device(vol, iso=iso, vertices=vbuf, quads=qbuf)
         st = ex.stats()
         emit_ms.append(st["emit_ms"]); count_ms.append(st["count_ms"]); scan_ms.append(st["scan_ms"])
+        step_ms.append(st["device_ms"])
     ev1.record(stream)
     torch.cuda.synchronize()
     if dist:
@@ -787,6 +795,7 @@ def main():
         hbm, peak_kind = peaks()
         elem = 2 if dtype == "uint16" else 4
         alg_bytes = elem * N + 12 * V + 16 * Q
+        cells = (dims[0] - 1) * (dims[1] - 1) * (dims[2] - 1) * world
         emit_avg = sum(emit_ms) / len(emit_ms)
         achieved = alg_bytes / (emit_avg * 1e-3) / 1e9
         value = total_points / (ms * 1e-3) / 1e9
@@ -801,6 +810,9 @@ def main():
             "dtype": "u16" if dtype == "uint16" else "f32", "data": "synthetic",
             "config": {"workload": args.workload, "desc": desc, "dims": list(dims), "iso": iso,
                        "vertices": V, "quads": Q, "active_cells": st["n_active_cells"],
+                       "samples_at_iso": at_iso,
+                       "gcells_per_s": round(cells / (ms * 1e-3) / 1e9, 3),
+                       "ms_median": round(statistics.median(step_ms), 4),
                        "algo": "brick", "l2": "input larger than L2 (no flush needed)",
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "kernel_ms": {"count": round(sum(count_ms) / len(count_ms), 4),

@@ -316,16 +316,17 @@ __device__ __forceinline__ void cell_vertices(const DeviceTables &tab, const flo
     // crossing is emitted
     const uint32_t dual = niso == 1 ? (om ? om : cm) : 0u;
     const uint32_t owned = ((info & 1u) << 6) | ((info & 2u) << 8) | ((info & 4u) << 8);
-    float3 acc = make_float3(0.f, 0.f, 0.f), c6 = acc, c9 = acc, c10 = acc;
+    // an owned crossing goes out as soon as it is evaluated: after the niso
+    // dual vertices, in the order 6, 9, 10 (the order of the bits)
+    float *const own_out = out + 3 * niso;
+    float3 acc = make_float3(0.f, 0.f, 0.f);
     uint32_t n = 0, mm = dual | owned;
     while (mm) {
         const int e = __ffs(mm) - 1;
         mm &= mm - 1;
         const float3 c = crossing_any(e, v, g, iso);
         if ((dual >> e) & 1u) { acc = n ? add3(acc, c) : c; ++n; }
-        if (e == 6) c6 = c;
-        if (e == 9) c9 = c;
-        if (e == 10) c10 = c;
+        if ((owned >> e) & 1u) store3(own_out + 3 * __popc(owned & ((1u << e) - 1u)), c);
     }
     if (niso == 1) store3(out, div3(acc, n));
     else {
@@ -334,10 +335,6 @@ __device__ __forceinline__ void cell_vertices(const DeviceTables &tab, const flo
         for (int i = 0; i < 8; ++i) cv.v[i] = v[i];
         multi_patch_vertices(tab, cv, g, iso, cfg, lut2, niso, cm, om, out);
     }
-    uint32_t k = niso;
-    if (info & 1u) { store3(out + 3 * k, c6); ++k; }
-    if (info & 2u) { store3(out + 3 * k, c9); ++k; }
-    if (info & 4u) { store3(out + 3 * k, c10); ++k; }
 }
 
 // Device-side error codes (written with atomicOr to ctx error word).
