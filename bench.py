@@ -142,6 +142,42 @@ def profile_traffic(workload):
     return d.get(workload)
 
 
+def cpu_model():
+    """CPU model name of this host (lscpu), for the CPU baseline's record."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def cpu_single_thread_sample(vol_host, iso, target_s=3.0):
+    """The CPU restatement on one thread, on a z-slab sized for ~target_s.
+    Returns (GVoxels/s, sample text); leaves the oracle on all host threads."""
+    import numpy as np
+    import oracle
+    oracle.set_threads(1)
+    try:
+        nz = vol_host.shape[0]
+        planes = min(nz, 4)
+        t0 = time.perf_counter()
+        oracle.extract(np.ascontiguousarray(vol_host[:planes]), iso=iso)
+        dt = time.perf_counter() - t0
+        planes = max(planes, min(nz, int(planes * target_s / max(dt, 1e-3))))
+        sample = np.ascontiguousarray(vol_host[:planes])
+        t0 = time.perf_counter()
+        oracle.extract(sample, iso=iso)
+        dt = time.perf_counter() - t0
+    finally:
+        oracle.set_threads(os.cpu_count() or 1)
+    return sample.size / dt / 1e9, "z-slab of %d x %d x %d points (%.1f s)" % (
+        sample.shape[2], sample.shape[1], sample.shape[0], dt)
+
+
 def cpu_oracle_sample(vol_host, iso, target_s=10.0):
     """Time the CPU restatement with all host threads on a z-slab sample of
     the workload, sized for ~target_s of work.  Returns GVoxels/s, cores, sample text."""
@@ -202,7 +238,8 @@ def run_reference(args, rank):
         "vs_baseline": None, "dtype": "u16" if dtype == "uint16" else "f32", "data": "synthetic",
         "config": {"workload": args.workload, "desc": desc, "sample_points": int(sample.size)},
         "cpu_baseline": {"value": round(value, 4), "unit": "GVoxels/s", "cores": cores, "kind": "port",
-                         "sample": "z-slab %dx%dx%d of the workload" % (sample.shape[2], sample.shape[1], sample.shape[0])},
+                         "sample": "z-slab %dx%dx%d of the workload" % (sample.shape[2], sample.shape[1], sample.shape[0]),
+                         "cpu_model": cpu_model()},
         "e2e": {"value": round(value, 4), "unit": "GVoxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -802,7 +839,10 @@ def main():
         cpu = None
         if not args.no_cpu_baseline:
             v, cores, sample = cpu_oracle_sample(host, iso)
-            cpu = {"value": round(v, 4), "unit": "GVoxels/s", "cores": cores, "kind": "port", "sample": sample}
+            v1, sample1 = cpu_single_thread_sample(host, iso)
+            cpu = {"value": round(v, 4), "unit": "GVoxels/s", "cores": cores, "kind": "port", "sample": sample,
+                   "cpu_model": cpu_model(),
+                   "single_thread": {"value": round(v1, 4), "unit": "GVoxels/s", "sample": sample1}}
         line = {
             "metric": "GVoxels/s", "value": round(value, 3), "unit": "GVoxels/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
