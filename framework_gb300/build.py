@@ -73,7 +73,7 @@ def build(force=False, verbose=False):
             if log.strip():
                 print(log)
     tmp = LIB + ".tmp%d" % os.getpid()
-    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + [o for o, _ in results] + ["-lcudart", "-lpthread"]
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + [o for o, _ in results] + ["-lcudart", "-lpthread", "-ldl"]
     subprocess.check_call(cmd)
     os.replace(tmp, LIB)
     return LIB

@@ -240,6 +240,7 @@ dmc_status dmc_extract_device(dmc_ctx *ctx, const dmc_volume *vol, const float x
                               uint32_t *d_quads, uint64_t quad_capacity, uint32_t *d_triangles,
                               uint64_t *n_vertices, uint64_t *n_quads, void *stream)
 {
+    NvtxRange nvtx("dmc_extract_device");
     if (!ctx || !n_vertices || !n_quads) return DMC_ERR_INVALID_ARG;
     ExtractArgs a;
     dmc_status s = make_args(vol, xyz_min, xyz_max, iso, a);
@@ -274,6 +275,7 @@ dmc_status dmc_extract_batch(dmc_ctx *ctx, const dmc_batch_item *items, uint32_t
                              dmc_batch_result *d_results, dmc_batch_result *results, uint64_t *n_vertices,
                              uint64_t *n_quads, uint32_t flags, void *stream)
 {
+    NvtxRange nvtx("dmc_extract_batch");
     if (!ctx || !items || n_items == 0) return DMC_ERR_INVALID_ARG;
     if (flags & ~(DMC_BATCH_ASYNC | DMC_BATCH_GRAPH)) return DMC_ERR_INVALID_ARG;
     if ((vertex_capacity && !d_vertices) || (quad_capacity && !d_quads)) return DMC_ERR_INVALID_ARG;
@@ -326,6 +328,7 @@ dmc_status dmc_extract_batch(dmc_ctx *ctx, const dmc_batch_item *items, uint32_t
 
 dmc_status dmc_batch_wait(dmc_ctx *ctx, dmc_batch_result *results, uint64_t *n_vertices, uint64_t *n_quads)
 {
+    NvtxRange nvtx("dmc_batch_wait");
     if (!ctx) return DMC_ERR_INVALID_ARG;
     Ctx *c = &ctx->c;
     if (!c->batch_pending) return DMC_ERR_INVALID_ARG;
@@ -340,6 +343,7 @@ dmc_status dmc_shard_count(dmc_ctx *ctx, const dmc_volume *local, uint32_t nz, u
                            const float xyz_min[3], const float xyz_max[3], float iso,
                            uint64_t *n_vertices, uint64_t *n_quads, void *stream)
 {
+    NvtxRange nvtx("dmc_shard_count");
     if (!ctx || !local || !n_vertices || !n_quads) return DMC_ERR_INVALID_ARG;
     *n_vertices = 0; *n_quads = 0;
     if (nz < 2 || z_begin >= z_end || z_end > nz - 1) return DMC_ERR_INVALID_ARG;
@@ -368,6 +372,7 @@ dmc_status dmc_shard_count(dmc_ctx *ctx, const dmc_volume *local, uint32_t nz, u
 dmc_status dmc_shard_emit(dmc_ctx *ctx, uint64_t vertex_offset, float *d_vertices, uint64_t vertex_capacity,
                           uint32_t *d_quads, uint64_t quad_capacity, uint32_t *d_triangles, void *stream)
 {
+    NvtxRange nvtx("dmc_shard_emit");
     if (!ctx) return DMC_ERR_INVALID_ARG;
     if ((vertex_capacity && !d_vertices) || (quad_capacity && !d_quads)) return DMC_ERR_INVALID_ARG;
     Ctx *c = &ctx->c;
@@ -531,6 +536,7 @@ static void touch_pages(void *const *bufs, const uint64_t *bytes, int n)
 dmc_status dmc_run(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min[3], const float xyz_max[3],
                    float iso, uint32_t num_smooth, int want_triangles, dmc_mesh *out)
 {
+    NvtxRange nvtx("dmc_run");
     if (!ctx || !out) return DMC_ERR_INVALID_ARG;
     memset(out, 0, sizeof(*out));
     uint64_t V = 0, Q = 0;
@@ -552,6 +558,7 @@ dmc_status dmc_run_into(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_min
                         uint32_t *h_quads, uint64_t quad_capacity, uint32_t *h_triangles,
                         uint64_t *n_vertices, uint64_t *n_quads)
 {
+    NvtxRange nvtx("dmc_run_into");
     if (!ctx || !n_vertices || !n_quads) return DMC_ERR_INVALID_ARG;
     if ((vertex_capacity && !h_vertices) || (quad_capacity && !h_quads && !h_triangles)) return DMC_ERR_INVALID_ARG;
     *n_vertices = 0; *n_quads = 0;

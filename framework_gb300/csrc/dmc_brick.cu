@@ -1349,6 +1349,7 @@ static int sweep_blocks(const BatchState &b, int t, bool emit, uint64_t nbricks,
 static dmc_status enqueue_front(Ctx *ctx, BatchState &b, dmc_batch_result *d_res, bool timed, const uint64_t nb[2],
                                 bool all, cudaStream_t st)
 {
+    NvtxRange nvtx("dmc count sweep and scan (enqueue)");
     using namespace brick;
     CUDA_TRY(cudaMemcpyAsync(b.d_plan, b.h_stage, b.plan_bytes, cudaMemcpyHostToDevice, st));
     batch_prep<<<2 * ctx->num_sms, 256, 0, st>>>(b.d_plan, b.tiles, b.tickets, ctx->d_ctl);
@@ -1382,6 +1383,7 @@ static dmc_status enqueue_front(Ctx *ctx, BatchState &b, dmc_batch_result *d_res
 static dmc_status enqueue_back(Ctx *ctx, BatchState &b, const brick::EmitOut &eo, dmc_batch_result *d_res, bool timed,
                                const uint64_t nb[2], bool all, cudaStream_t st)
 {
+    NvtxRange nvtx("dmc emit sweep (enqueue)");
     using namespace brick;
     if (timed) CUDA_TRY(cudaEventRecord(ctx->evk[3], st));
     if (all || nb[0]) {
@@ -1729,6 +1731,7 @@ static void launch_sweep(Ctx *ctx, BatchState &b, bool emit, brick::BrickRange r
 dmc_status brick_run_streamed(Ctx *ctx, const ExtractArgs &a, const StreamIO &io, uint32_t slabs, bool *dev_short,
                               cudaStream_t st)
 {
+    NvtxRange nvtx("dmc streamed extraction");
     using namespace brick;
     *dev_short = false;
     BatchState *bp = nullptr;

@@ -2,10 +2,20 @@
 #pragma once
 #include <stdint.h>
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include "../../include/dmc_gb300.h"
 #include "dmc_device.cuh"
 
 namespace dmc {
+
+// A named NVTX range over a host scope, for profiler timelines (Nsight
+// Systems, ncu's NVTX filters).  Without a tool attached it costs a call.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 #define CUDA_TRY(expr)                                              \
     do {                                                            \

@@ -87,6 +87,7 @@ extern "C" dmc_status dmc_compact_mesh(dmc_ctx *handle, const float *d_vertices,
                                        uint32_t *d_quads, uint64_t n_quads, uint32_t *d_triangles,
                                        float *d_out_vertices, uint64_t *n_out_vertices, void *stream)
 {
+    dmc::NvtxRange nvtx("dmc_compact_mesh");
     if (!handle || !n_out_vertices || (n_vertices && (!d_vertices || !d_out_vertices)) || (n_quads && !d_quads))
         return DMC_ERR_INVALID_ARG;
     if (n_vertices >= 0xFFFFFFFFull) return DMC_ERR_UNSUPPORTED;

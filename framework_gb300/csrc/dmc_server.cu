@@ -33,6 +33,7 @@
 #include <cuda_runtime.h>
 #include "../../include/dmc_gb300.h"
 #include "dmc_arena.h"
+#include "dmc_internal.h"   // NvtxRange
 
 namespace {
 
@@ -115,6 +116,7 @@ void dmc_server::free_batch(Batch *b)
 // Forms a batch from the head of the FIFO and launches it on lane L.
 bool dmc_server::launch(Lane &L, std::unique_lock<std::mutex> &lk)
 {
+    dmc::NvtxRange nvtx("dmc_server batch launch");
     const uint32_t maxb = cfg.plain ? 1u : cfg.max_batch;
     const uint64_t vfree = va.largest_free(), qfree = qa.largest_free();
     uint64_t vsum = 0, qsum = 0;
@@ -186,6 +188,7 @@ bool dmc_server::launch(Lane &L, std::unique_lock<std::mutex> &lk)
 
 void dmc_server::complete(Lane &L, std::unique_lock<std::mutex> &lk)
 {
+    dmc::NvtxRange nvtx("dmc_server batch complete");
     uint64_t V = 0, Q = 0;
     dmc_status s = DMC_OK;
     lk.unlock();

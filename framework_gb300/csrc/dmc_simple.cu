@@ -557,6 +557,7 @@ extern "C" dmc_status dmc_extract_device_noalloc(const dmc_volume *vol, const fl
                                                  uint32_t *d_triangles, uint64_t *n_vertices, uint64_t *n_quads,
                                                  void *stream)
 {
+    dmc::NvtxRange nvtx("dmc_extract_device_noalloc");
     using namespace dmc;
     if (!vol || !vol->data || !xyz_min || !xyz_max || !n_vertices || !n_quads) return DMC_ERR_INVALID_ARG;
     if (vol->dtype != DMC_F32 && vol->dtype != DMC_U16) return DMC_ERR_INVALID_ARG;
