@@ -44,6 +44,7 @@ ABI_SYMBOLS = [
 BATCH_ASYNC, BATCH_GRAPH = 0x1, 0x2
 OPT_BRICK_PLANES = 1
 OPT_STREAM_SLABS = 2      # dmc_run_into in z slabs: 0 automatic, 1 never, 2..32 slabs
+OPT_FAIL_ALLOCS = 3       # test hook: the context's next n device allocations fail (DMC_ERR_OOM)
 
 
 class DMCError(RuntimeError):

@@ -13,22 +13,35 @@ namespace dmc {
 static thread_local cudaError_t g_last_cuda = cudaSuccess;
 void set_last_cuda_error(cudaError_t e) { g_last_cuda = e; }
 
+// The DMC_OPT_FAIL_ALLOCS hook: true while allocations are to fail.
+static bool fake_oom(Ctx *ctx)
+{
+    if (!ctx->fail_allocs) return false;
+    --ctx->fail_allocs;
+    return true;
+}
+
 dmc_status ctx_reserve_scratch(Ctx *ctx, size_t bytes)
 {
     if (bytes <= ctx->scratch_bytes) return DMC_OK;
-    if (ctx->scratch) { cudaFree(ctx->scratch); ctx->scratch = nullptr; ctx->scratch_bytes = 0; }
+    // Freeing the old scratch invalidates every layout carved from it (the
+    // batch plan, captured graphs, a sharded count), also when the new
+    // allocation then fails: the generation moves with the free.
+    if (ctx->scratch) { cudaFree(ctx->scratch); ctx->scratch = nullptr; ctx->scratch_bytes = 0; ++ctx->scratch_gen; }
     size_t want = bytes + bytes / 8;   // headroom: fewer re-allocations across calls
+    if (fake_oom(ctx)) return DMC_ERR_OOM;
     CUDA_TRY(cudaMalloc(&ctx->scratch, want));
     ctx->scratch_bytes = want;
     ++ctx->scratch_gen;
     return DMC_OK;
 }
 
-static dmc_status reserve(void **p, size_t *have, size_t bytes)
+static dmc_status reserve(Ctx *ctx, void **p, size_t *have, size_t bytes)
 {
     if (bytes <= *have) return DMC_OK;
     if (*p) { cudaFree(*p); *p = nullptr; *have = 0; }
     size_t want = bytes + bytes / 8 + 256;
+    if (fake_oom(ctx)) return DMC_ERR_OOM;
     CUDA_TRY(cudaMalloc(p, want));
     *have = want;
     return DMC_OK;
@@ -398,6 +411,10 @@ dmc_status dmc_set_option(dmc_ctx *ctx, dmc_option opt, int64_t value)
         if (value < 0 || value > 32) return DMC_ERR_INVALID_ARG;
         ctx->c.stream_slabs = (uint32_t)value;
         return DMC_OK;
+    case DMC_OPT_FAIL_ALLOCS:
+        if (value < 0 || value > 1000) return DMC_ERR_INVALID_ARG;
+        ctx->c.fail_allocs = (uint32_t)value;
+        return DMC_OK;
     }
     return DMC_ERR_INVALID_ARG;
 }
@@ -422,7 +439,7 @@ static dmc_status run_host(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_
     if (a.n_cells > 0) {
         // upload the host volume (dmc.cu:2077-2079)
         uint64_t bytes = volume_bytes(vol);
-        s = reserve(&c->d_vol, &c->d_vol_bytes, bytes);
+        s = reserve(c, &c->d_vol, &c->d_vol_bytes, bytes);
         if (s != DMC_OK) return s;
         CUDA_TRY(cudaMemcpyAsync(c->d_vol, vol->data, bytes, cudaMemcpyHostToDevice, st));
         a.vol = c->d_vol;
@@ -436,9 +453,9 @@ static dmc_status run_host(dmc_ctx *ctx, const dmc_volume *vol, const float xyz_
             s = run_path(ctx, a, st);
             if (s != DMC_ERR_OUTPUT_OVERFLOW || attempt == 1) break;
             if (*V >= 0xFFFFFFFFull || *Q >= 0xFFFFFFFFull) break;
-            if ((s = reserve(&ctx->out.v, &ctx->out.vb, 12 * (*V ? *V : 1))) != DMC_OK) return s;
-            if ((s = reserve(&ctx->out.q, &ctx->out.qb, 16 * (*Q ? *Q : 1))) != DMC_OK) return s;
-            if (want_triangles && (s = reserve(&ctx->out.t, &ctx->out.tb, 24 * (*Q ? *Q : 1))) != DMC_OK) return s;
+            if ((s = reserve(c, &ctx->out.v, &ctx->out.vb, 12 * (*V ? *V : 1))) != DMC_OK) return s;
+            if ((s = reserve(c, &ctx->out.q, &ctx->out.qb, 16 * (*Q ? *Q : 1))) != DMC_OK) return s;
+            if (want_triangles && (s = reserve(c, &ctx->out.t, &ctx->out.tb, 24 * (*Q ? *Q : 1))) != DMC_OK) return s;
             CUDA_TRY(cudaMemsetAsync(c->d_ctl, 0, sizeof(DevCtl), st));
         }
         if (s != DMC_OK) { finish(ctx, st); return s; }
@@ -475,7 +492,7 @@ static dmc_status run_streamed(dmc_ctx *ctx, const dmc_volume *vol, const float 
     // the caller take the plain path, which grows them
     if (!ctx->out.v || !ctx->out.q || (ht && !ctx->out.t)) { *dev_short = true; return DMC_ERR_OUTPUT_OVERFLOW; }
     if (cudaSetDevice(c->device) != cudaSuccess) return DMC_ERR_CUDA;
-    if ((s = reserve(&c->d_vol, &c->d_vol_bytes, bytes)) != DMC_OK) return s;
+    if ((s = reserve(c, &c->d_vol, &c->d_vol_bytes, bytes)) != DMC_OK) return s;
     c->stats = dmc_stats{};
     c->stats.algo = DMC_ALGO_BRICK;
     a.vol = c->d_vol;

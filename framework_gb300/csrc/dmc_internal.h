@@ -55,6 +55,7 @@ struct Ctx {
     uint64_t scratch_gen = 0;          // bumped whenever scratch moves (captured graphs hold its addresses)
     uint32_t brick_zc = 0;             // planes per brick (0: automatic)
     uint32_t stream_slabs = 0;         // host extraction in z slabs: 0 automatic, 1 never, n >= 2 n slabs
+    uint32_t fail_allocs = 0;          // test hook: device allocations still to fail (DMC_OPT_FAIL_ALLOCS)
     BatchState *batch = nullptr;
     bool batch_pending = false;        // an asynchronous batch awaits dmc_batch_wait
     size_t d_vol_bytes = 0;

@@ -266,12 +266,15 @@ dmc_status dmc_shard_count(dmc_ctx *ctx, const dmc_volume *local, uint32_t nz, u
 dmc_status dmc_shard_emit(dmc_ctx *ctx, uint64_t vertex_offset, float *d_vertices, uint64_t vertex_capacity,
                           uint32_t *d_quads, uint64_t quad_capacity, uint32_t *d_triangles, void *stream);
 
-/* Tuning knobs (no reference counterpart). */
+/* Tuning knobs and a test hook (no reference counterpart). */
 typedef enum {
     DMC_OPT_BRICK_PLANES = 1,  /* z planes per brick, 1..256; 0 chooses from the batch size */
-    DMC_OPT_STREAM_SLABS = 2   /* dmc_run_into in z slabs (upload, extraction and download
+    DMC_OPT_STREAM_SLABS = 2,  /* dmc_run_into in z slabs (upload, extraction and download
                                   overlap): 0 automatic (volumes of 64 MiB and more, one slab
                                   per 96 MiB, 2..32), 1 never, 2..32 that many slabs */
+    DMC_OPT_FAIL_ALLOCS = 3    /* test hook: the context's next n device allocations fail as
+                                  when the device is out of memory (the call returns
+                                  DMC_ERR_OOM; the buffer being grown is released); 0 off */
 } dmc_option;
 
 dmc_status dmc_set_option(dmc_ctx *ctx, dmc_option opt, int64_t value);
