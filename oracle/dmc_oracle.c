@@ -47,6 +47,7 @@
 #include "../framework_gb300/csrc/dmc_tables.inc"
 
 #define INVALID32 0xFFFFFFFFu
+#define SCAN_BLOCK 65536u   /* cells per block of the parallel exclusive scans */
 
 typedef struct {
     float *vertices;      /* 3 * n_vertices (precision 0) */
@@ -375,17 +376,38 @@ int oracle_dmc_ex(const void *vol, int dtype, const uint32_t dims[3], const floa
                 corners(&g, x, y, (uint64_t)z, v);
                 cfg[((uint64_t)z * g.cy + y) * g.cx + x] = config_of(v, iso);
             }
-    uint64_t A = 0;
-    for (uint64_t i = 0; i < C; ++i) {
-        uint8_t c = cfg[i];
-        map[i] = (c != 0 && c != 0xff) ? (uint32_t)A++ : INVALID32;
+    /* Active cells numbered in index1D order, exactly as one serial pass
+     * would: per-block counts in parallel, an exclusive prefix over the
+     * blocks, then each block numbers its own cells. */
+    const uint64_t nblk = (C + SCAN_BLOCK - 1) / SCAN_BLOCK;
+    uint64_t *boff = (uint64_t *)calloc(nblk + 1, sizeof(uint64_t));
+    if (!boff) { free(map); free(cfg); return 2; }
+    #pragma omp parallel for schedule(static)
+    for (int64_t b = 0; b < (int64_t)nblk; ++b) {
+        const uint64_t i0 = (uint64_t)b * SCAN_BLOCK, i1 = i0 + SCAN_BLOCK < C ? i0 + SCAN_BLOCK : C;
+        uint64_t n = 0;
+        for (uint64_t i = i0; i < i1; ++i) n += (cfg[i] != 0 && cfg[i] != 0xff);
+        boff[b + 1] = n;
     }
-    if (A >= INVALID32) { free(map); free(cfg); return 3; }
+    for (uint64_t b = 0; b < nblk; ++b) boff[b + 1] += boff[b];
+    const uint64_t A = boff[nblk];
+    if (A >= INVALID32) { free(boff); free(map); free(cfg); return 3; }
+    #pragma omp parallel for schedule(static)
+    for (int64_t b = 0; b < (int64_t)nblk; ++b) {
+        const uint64_t i0 = (uint64_t)b * SCAN_BLOCK, i1 = i0 + SCAN_BLOCK < C ? i0 + SCAN_BLOCK : C;
+        uint64_t k = boff[b];
+        for (uint64_t i = i0; i < i1; ++i) map[i] = (cfg[i] != 0 && cfg[i] != 0xff) ? (uint32_t)k++ : INVALID32;
+    }
     out->n_active = A;
     cell_rec *rec = (cell_rec *)calloc(A ? A : 1, sizeof(cell_rec));
-    if (!rec) { free(map); free(cfg); return 2; }
-    for (uint64_t i = 0; i < C; ++i)
-        if (map[i] != INVALID32) rec[map[i]].index1d = i;
+    if (!rec) { free(boff); free(map); free(cfg); return 2; }
+    #pragma omp parallel for schedule(static)
+    for (int64_t b = 0; b < (int64_t)nblk; ++b) {
+        const uint64_t i0 = (uint64_t)b * SCAN_BLOCK, i1 = i0 + SCAN_BLOCK < C ? i0 + SCAN_BLOCK : C;
+        for (uint64_t i = i0; i < i1; ++i)
+            if (map[i] != INVALID32) rec[map[i]].index1d = i;
+    }
+    free(boff);
 
     /* step 3: config + bipolar/ccw bits of owned edges 6 (2-6), 9 (5-6), 10 (7-6)
      * (dmc.cu:1173-1221) */
@@ -433,16 +455,32 @@ int oracle_dmc_ex(const void *vol, int dtype, const uint32_t dims[3], const floa
     }
     out->n_lut2 = n_lut2;
 
-    /* step 5: vertex counts and offsets (dmc.cu:1382-1424, 2133-2141) */
-    uint64_t V = 0;
-    for (uint64_t a = 0; a < A; ++a) {
+    /* step 5: vertex counts and offsets (dmc.cu:1382-1424, 2133-2141): the
+     * counts in parallel, then the same blocked exclusive scan */
+    #pragma omp parallel for schedule(static)
+    for (int64_t a = 0; a < (int64_t)A; ++a) {
         cell_rec *r = &rec[a];
         uint8_t n = (r->info & 0x80) ? DMC_NVERT_LUT2[r->config] : DMC_NVERT_LUT1[r->config];
-        n = (uint8_t)(n + (r->info & 1u) + ((r->info >> 1) & 1u) + ((r->info >> 2) & 1u));
-        r->nv = n;
-        r->vertex_begin = (uint32_t)V;
-        V += n;
-        if (V > INVALID32) { free(map); free(cfg); free(rec); return 3; }
+        r->nv = (uint8_t)(n + (r->info & 1u) + ((r->info >> 1) & 1u) + ((r->info >> 2) & 1u));
+    }
+    const uint64_t nblk_a = (A + SCAN_BLOCK - 1) / SCAN_BLOCK;
+    uint64_t *aoff = (uint64_t *)calloc(nblk_a + 1, sizeof(uint64_t));
+    if (!aoff) { free(map); free(cfg); free(rec); return 2; }
+    #pragma omp parallel for schedule(static)
+    for (int64_t b = 0; b < (int64_t)nblk_a; ++b) {
+        const uint64_t a0 = (uint64_t)b * SCAN_BLOCK, a1 = a0 + SCAN_BLOCK < A ? a0 + SCAN_BLOCK : A;
+        uint64_t n = 0;
+        for (uint64_t a = a0; a < a1; ++a) n += rec[a].nv;
+        aoff[b + 1] = n;
+    }
+    for (uint64_t b = 0; b < nblk_a; ++b) aoff[b + 1] += aoff[b];
+    const uint64_t V = aoff[nblk_a];
+    if (V > INVALID32) { free(aoff); free(map); free(cfg); free(rec); return 3; }
+    #pragma omp parallel for schedule(static)
+    for (int64_t b = 0; b < (int64_t)nblk_a; ++b) {
+        const uint64_t a0 = (uint64_t)b * SCAN_BLOCK, a1 = a0 + SCAN_BLOCK < A ? a0 + SCAN_BLOCK : A;
+        uint64_t v = aoff[b];
+        for (uint64_t a = a0; a < a1; ++a) { rec[a].vertex_begin = (uint32_t)v; v += rec[a].nv; }
     }
     out->n_vertices = V;
 
@@ -451,7 +489,7 @@ int oracle_dmc_ex(const void *vol, int dtype, const uint32_t dims[3], const floa
     const uint64_t csz[3] = {g.cx, g.cy, g.cz};
     if (precision == 0) {
         float *vt = (float *)malloc((V ? V : 1) * 3 * sizeof(float));
-        if (!vt) { free(map); free(cfg); free(rec); return 2; }
+        if (!vt) { free(aoff); free(map); free(cfg); free(rec); return 2; }
         out->vertices = vt;
         /* edge crossings on owned edges (dmc.cu:1468-1514) */
         #pragma omp parallel for schedule(static)
@@ -517,7 +555,7 @@ int oracle_dmc_ex(const void *vol, int dtype, const uint32_t dims[3], const floa
         }
     } else {
         double *vt = (double *)malloc((V ? V : 1) * 3 * sizeof(double));
-        if (!vt) { free(map); free(cfg); free(rec); return 2; }
+        if (!vt) { free(aoff); free(map); free(cfg); free(rec); return 2; }
         out->vertices64 = vt;
         const double rng64[3] = {(double)xyz_max[0] - xyz_min[0], (double)xyz_max[1] - xyz_min[1], (double)xyz_max[2] - xyz_min[2]};
         #pragma omp parallel for schedule(static)
@@ -580,14 +618,16 @@ int oracle_dmc_ex(const void *vol, int dtype, const uint32_t dims[3], const floa
 
     /* step 7: quads (dmc.cu:1983-2047).  Count per cell, exclusive scan, fill. */
     uint32_t *qoff = (uint32_t *)malloc((A ? A : 1) * sizeof(uint32_t));
-    if (!qoff) { free(map); free(cfg); free(rec); return 2; }
-    uint64_t Q = 0, dropped = 0;
-    for (uint64_t a = 0; a < A; ++a) {
+    if (!qoff) { free(aoff); free(map); free(cfg); free(rec); return 2; }
+    /* quads per owner cell (into qoff for now), then the blocked scan */
+    uint64_t dropped = 0;
+    #pragma omp parallel for reduction(+:dropped) schedule(static)
+    for (int64_t a = 0; a < (int64_t)A; ++a) {
         const cell_rec *r = &rec[a];
         uint64_t i1 = r->index1d;
         uint64_t x = i1 % g.cx, y = (i1 / g.cx) % g.cy, z = i1 / (g.cx * g.cy);
-        qoff[a] = (uint32_t)Q;
         static const int P0[3] = {2, 5, 7};
+        uint32_t nq = 0;
         for (int s = 0; s < 3; ++s) {
             if (!((r->info >> s) & 1u)) continue;
             int exceed = s == 0 ? (x + 1 >= g.cx || y + 1 >= g.cy)
@@ -595,11 +635,29 @@ int oracle_dmc_ex(const void *vol, int dtype, const uint32_t dims[3], const floa
                                 : (y + 1 >= g.cy || z + 1 >= g.cz);
             if (exceed) continue;
             if (((r->config >> P0[s]) & 1u) == ((r->config >> 6) & 1u)) { dropped++; continue; }
-            Q++;
+            nq++;
         }
+        qoff[a] = nq;
     }
+    #pragma omp parallel for schedule(static)
+    for (int64_t b = 0; b < (int64_t)nblk_a; ++b) {
+        const uint64_t a0 = (uint64_t)b * SCAN_BLOCK, a1 = a0 + SCAN_BLOCK < A ? a0 + SCAN_BLOCK : A;
+        uint64_t n = 0;
+        for (uint64_t a = a0; a < a1; ++a) n += qoff[a];
+        aoff[b + 1] = n;
+    }
+    aoff[0] = 0;
+    for (uint64_t b = 0; b < nblk_a; ++b) aoff[b + 1] += aoff[b];
+    const uint64_t Q = aoff[nblk_a];
     out->n_dropped_quads = dropped;
-    if (Q >= INVALID32) { free(map); free(cfg); free(rec); free(qoff); return 3; }
+    if (Q >= INVALID32) { free(aoff); free(map); free(cfg); free(rec); free(qoff); return 3; }
+    #pragma omp parallel for schedule(static)
+    for (int64_t b = 0; b < (int64_t)nblk_a; ++b) {
+        const uint64_t a0 = (uint64_t)b * SCAN_BLOCK, a1 = a0 + SCAN_BLOCK < A ? a0 + SCAN_BLOCK : A;
+        uint64_t q = aoff[b];
+        for (uint64_t a = a0; a < a1; ++a) { const uint32_t n = qoff[a]; qoff[a] = (uint32_t)q; q += n; }
+    }
+    free(aoff);
     out->n_quads = Q;
     uint32_t *qd = (uint32_t *)malloc((Q ? Q : 1) * 4 * sizeof(uint32_t));
     if (!qd) { free(map); free(cfg); free(rec); free(qoff); return 2; }
