@@ -57,7 +57,10 @@ def test_reference_arm_under_torchrun_two_ranks():
     assert len(lines) == 1, r.stdout
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
-    assert d["cpu_baseline"]["kind"] == "port"
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cpu_model"]
+    assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
+    for key in ("metric", "unit", "steps", "warmup", "ms_per_step", "higher_is_better", "config"):
+        assert key in d
 
 
 def _shard_exchange_worker(rank, world, port, out):
