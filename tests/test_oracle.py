@@ -173,3 +173,25 @@ def test_smoothing_keeps_topology_and_moves_vertices():
     # smoothed vertices stay near the surface (radius 4.1, cell size 0.5)
     r = np.linalg.norm(b["vertices"], axis=1)
     assert np.all(np.abs(r - 4.1) < 0.5)
+
+
+def test_oracle_independent_of_thread_count():
+    """The oracle's parallel passes, including the blocked scans that number
+    the active cells and place vertices and quads, give the same mesh bit
+    for bit on 1, 3 and 8 threads.  The volume spans many 64 Ki-cell scan
+    blocks, and its active cells several."""
+    from framework_gb300 import fields
+    vol = fields.gyroid((150, 120, 90), 0.35, seed=11).numpy()
+    ref = None
+    try:
+        for threads in (1, 3, 8):
+            oracle.set_threads(threads)
+            r = oracle.extract(vol, iso=0.05)
+            got = (r["vertices"].view(np.uint32), r["quads"], r["n_active"], r["n_dropped_quads"])
+            if ref is None:
+                ref = got
+                assert r["n_active"] > 3 * 65536
+            else:
+                assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1]) and got[2:] == ref[2:]
+    finally:
+        oracle.set_threads(os.cpu_count() or 1)
