@@ -60,3 +60,20 @@ def test_create_without_gpu_fails_cleanly():
     assert L.dmc_create(ctypes.byref(h), 0) == 1  # DMC_ERR_INVALID_ARG: no such device
     with pytest.raises(fg.DMCError):
         fg.Extractor(0)
+
+
+def test_python_constants_match_the_header():
+    """The Python binding's status, dtype, algorithm and option numbers are
+    the header's enum values."""
+    import re
+    import framework_gb300 as fg
+    text = open(os.path.join(ROOT, "include", "dmc_gb300.h")).read()
+    enum = {m.group(1): int(m.group(2)) for m in re.finditer(r"\b(DMC_[A-Z0-9_]+)\s*=\s*(\d+)", text)}
+    assert {v: k for k, v in fg.STATUS.items()} == {k: v for k, v in enum.items()
+                                                    if k == "DMC_OK" or k.startswith("DMC_ERR_")}
+    assert fg.DTYPE == {"float32": enum["DMC_F32"], "uint16": enum["DMC_U16"]}
+    assert fg.ALGO == {"auto": enum["DMC_ALGO_AUTO"], "simple": enum["DMC_ALGO_SIMPLE"], "brick": enum["DMC_ALGO_BRICK"]}
+    for name in ("BRICK_PLANES", "STREAM_SLABS", "FAIL_ALLOCS"):
+        assert getattr(fg, "OPT_" + name) == enum["DMC_OPT_" + name]
+    cells = re.search(r"#define\s+DMC_NOALLOC_MAX_CELLS\s+(\d+)u?", text)
+    assert cells and fg.NOALLOC_MAX_CELLS == int(cells.group(1))
