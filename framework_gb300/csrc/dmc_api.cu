@@ -110,9 +110,8 @@ static dmc_status make_args(const dmc_volume *vol, const float mn[3], const floa
     c.y = vol->dims[1] > 0 ? vol->dims[1] - 1 : 0;
     c.z = vol->dims[2] > 0 ? vol->dims[2] - 1 : 0;
     a.cells = c;
-    a.n_cells = (uint64_t)c.x * c.y * c.z;
     // 32-bit cell indices inside the kernels' per-axis math; the totals are 64-bit
-    if (a.n_cells >= (1ull << 40)) return DMC_ERR_UNSUPPORTED;
+    if (!cell_count(c, &a.n_cells) || a.n_cells >= (1ull << 40)) return DMC_ERR_UNSUPPORTED;
     a.iso = iso;
     a.mn = make_float3(mn[0], mn[1], mn[2]);
     // utils.hpp / dmc.cu:2149: xyz_range = xyz_max - xyz_min

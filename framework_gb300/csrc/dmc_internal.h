@@ -64,6 +64,14 @@ struct Ctx {
     dmc_stats stats{};
 };
 
+// Cells of a volume, (nx-1)(ny-1)(nz-1) from its cell counts per axis; false
+// when the product does not fit 64 bits.
+inline bool cell_count(uint3 c, uint64_t *n)
+{
+    uint64_t xy;
+    return !__builtin_mul_overflow((uint64_t)c.x, (uint64_t)c.y, &xy) && !__builtin_mul_overflow(xy, (uint64_t)c.z, n);
+}
+
 struct ExtractArgs {
     const void *vol;
     dmc_dtype dtype;

@@ -471,9 +471,11 @@ dmc_status simple_run(Ctx *ctx, const ExtractArgs &a, cudaStream_t st)
 // synchronise the device and stall them.  Everything the pipeline needs --
 // lookup tables, control block, per-cell arrays and scan tile states -- lives
 // in one fixed array in the module's global memory, sized for at most
-// kNoAllocMaxCells cells.  Its address is taken once per device with
-// cudaGetSymbolAddress on the first call, which also uploads the tables; make
-// that first call before any stream capture.  Per call, only the control
+// kNoAllocMaxCells cells.  Every call takes its address with
+// cudaGetSymbolAddress (host code must not pass the array's name itself to a
+// kernel); the first call on a device, and the first after its context was
+// replaced, also uploads the tables and synchronises the device, so make that
+// first call before any stream capture.  Per call, only the control
 // block and the scan tile states must start at zero (cleared with
 // cudaMemsetAsync on the caller's stream); the per-cell arrays are fully
 // rewritten.  There is one array per device, so calls on the same device must
@@ -494,19 +496,58 @@ constexpr size_t kNoAllocBytes = kNaTiles + na_align(sizeof(TileState) * kNoAllo
 static __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocBytes];
 
 static std::mutex g_noalloc_setup_mu;
-static uint8_t *g_noalloc_base[256];          // per device, set by the first call
+static uint8_t *g_noalloc_base[256];          // per device, set by the set-up
+static unsigned long long g_noalloc_ctx[256]; // id of the CUDA context that set-up ran in (0: none yet)
 
+// Unique id of the calling thread's current CUDA context (cuCtxGetId, which
+// never repeats within a process), taken through the runtime's driver entry
+// points so the library needs no link against libcuda.  0 when unavailable.
+static unsigned long long current_context_id()
+{
+    typedef int (*GetCurrent)(void **);
+    typedef int (*GetId)(void *, unsigned long long *);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaDriverEntryPointQueryResult q;
+        void *f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = (GetCurrent)f;
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = (GetId)f;
+    });
+    void *c = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&c) != 0 || !c || get_id(c, &id) != 0) return 0;
+    return id;
+}
+
+// Set-up, once per device and CUDA context: the array's device address
+// (cudaGetSymbolAddress with the device current) and the lookup tables.  The
+// upload is followed by a device synchronisation, so the tables are complete
+// before any kernel on any stream (including non-blocking ones) reads them.
+// A context that replaced an earlier one on the device (after
+// cudaDeviceReset) gets a fresh set-up: its array is a new allocation.
 static dmc_status noalloc_setup(int device, uint8_t **base)
 {
     if (device < 0 || device >= 256) return DMC_ERR_INVALID_ARG;
+    // Looked up on every call: it also makes the device's primary context
+    // current, which the context id below needs.
+    void *p = nullptr;
+    CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    const unsigned long long ctx = current_context_id();
     std::lock_guard<std::mutex> lk(g_noalloc_setup_mu);
-    if (!g_noalloc_base[device]) {
-        void *p = nullptr;
-        CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    if (g_noalloc_base[device] != (uint8_t *)p || ctx == 0 || ctx != g_noalloc_ctx[device]) {
         DeviceTables h;
         fill_tables(h);
         CUDA_TRY(cudaMemcpy((uint8_t *)p + kNaTab, &h, sizeof(DeviceTables), cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaDeviceSynchronize());
         g_noalloc_base[device] = (uint8_t *)p;
+        g_noalloc_ctx[device] = ctx;
     }
     *base = g_noalloc_base[device];
     return DMC_OK;
@@ -569,8 +610,7 @@ extern "C" dmc_status dmc_extract_device_noalloc(const dmc_volume *vol, const fl
     a.pts = make_uint3(vol->dims[0], vol->dims[1], vol->dims[2]);
     a.cells = make_uint3(vol->dims[0] ? vol->dims[0] - 1 : 0, vol->dims[1] ? vol->dims[1] - 1 : 0,
                          vol->dims[2] ? vol->dims[2] - 1 : 0);
-    a.n_cells = (uint64_t)a.cells.x * a.cells.y * a.cells.z;
-    if (a.n_cells > kNoAllocMaxCells) return DMC_ERR_TOO_LARGE;
+    if (!cell_count(a.cells, &a.n_cells) || a.n_cells > kNoAllocMaxCells) return DMC_ERR_TOO_LARGE;
     a.iso = iso;
     a.mn = make_float3(xyz_min[0], xyz_min[1], xyz_min[2]);
     a.rng = make_float3(xyz_max[0] - xyz_min[0], xyz_max[1] - xyz_min[1], xyz_max[2] - xyz_min[2]);

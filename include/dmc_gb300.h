@@ -352,8 +352,9 @@ dmc_status dmc_server_replay(dmc_server *server, uint32_t n, const uint32_t *vol
  *
  * No context: it runs on the calling thread's current device, on `stream`
  * (NULL: the legacy default stream), and returns when the mesh is complete.
- * The first call on a device looks up the array's address and uploads the
- * lookup tables; make it before any stream capture.  The array is one per
+ * The first call on a device (and the first after cudaDeviceReset) uploads
+ * the lookup tables into the array and synchronises the device; make it
+ * before any stream capture.  The array is one per
  * device: calls on the same device must not overlap (concurrent calls from
  * several host threads race on it).  Outputs and errors as in
  * dmc_extract_device (all output pointers NULL: count only). */
