@@ -1,12 +1,15 @@
-"""Parity at the benchmark sizes: the 512^3 float32 blobs and the 1024^3
-uint16 value noise, extracted on the GPU and by the CPU oracle (all host
-threads), must agree bit for bit; the brick and simple kernel families must
-agree with each other on the device as well."""
+"""Parity at the benchmark sizes: the 64^3 sphere, the 512^3 float32 blobs
+and the 1024^3 uint16 value noise, extracted on the GPU and by the CPU oracle
+(all host threads), must agree bit for bit; the brick and simple kernel
+families must agree with each other on the device as well.  Against the FP64
+oracle the topology must be identical and the vertices within the bound of
+tests/fp64bound.py (4 ulp of the extent's largest coordinate)."""
 import os
 
 import numpy as np
 import pytest
 
+import fp64bound
 import oracle
 
 pytestmark = pytest.mark.gpu
@@ -30,7 +33,10 @@ def _device_mesh(ex, vol, iso, algo):
 def _full_case(extractor, name):
     import torch
     from framework_gb300 import fields
-    if name == "blobs512":
+    if name == "sphere64":
+        vol, iso = fields.sphere_sdf(64, radius=20.0, noise=0.01, seed=1).cuda(), 0.0
+        host = vol.cpu().numpy()
+    elif name == "blobs512":
         vol, iso = fields.gaussian_blobs((512, 512, 512), device="cuda"), 0.5
         host = vol.cpu().numpy()
     else:
@@ -52,7 +58,18 @@ def _full_case(extractor, name):
     assert np.array_equal(gv.view(np.uint32), ref["vertices"].view(np.uint32))
     del gv
     assert np.array_equal(qb.cpu().numpy().view(np.uint32), ref["quads"])
-    return len(ref["vertices"]), len(ref["quads"])
+    V, Q = len(ref["vertices"]), len(ref["quads"])
+    del ref
+    ref64 = oracle.extract(host, iso=iso, precision=1)
+    assert np.array_equal(qb.cpu().numpy().view(np.uint32), ref64["quads"])      # same topology
+    worst, ulps, vox = fp64bound.check(vb.cpu().numpy(), ref64["vertices"], host.shape[::-1])
+    print("%s: FP32 vs FP64 max |d| %.3g = %.2f ulp(M) = %.3g voxel" % (name, worst, ulps, vox))
+    return V, Q
+
+
+def test_sphere64_full_size(extractor):
+    V, Q = _full_case(extractor, "sphere64")
+    assert V > 10000 and Q > 5000
 
 
 def test_blobs512_full_size(extractor):

@@ -101,13 +101,25 @@ def test_sphere_is_closed_oriented_manifold():
     assert len(np.unique(q)) - len(und) + len(q) == 2  # Euler characteristic of a sphere
 
 
-def test_fp64_oracle_close_to_fp32():
+@pytest.mark.parametrize("case", ["blobs", "offset_extent", "u16_noise"])
+def test_fp64_oracle_within_stated_bound(case):
+    """FP32 replica against FP64: same topology, vertices within 4 ulp of the
+    extent's largest coordinate (tests/fp64bound.py states and derives it)."""
+    import fp64bound
     from framework_gb300 import fields
-    vol = fields.gaussian_blobs((40, 36, 30), count=5, sigma=(4.0, 8.0), seed=3).numpy()
-    a = oracle.extract(vol, iso=0.5)
-    b = oracle.extract(vol, iso=0.5, precision=1)
+    mn = mx = None
+    if case == "blobs":
+        vol, iso = fields.gaussian_blobs((40, 36, 30), count=5, sigma=(4.0, 8.0), seed=3).numpy(), 0.5
+    elif case == "offset_extent":
+        vol, iso = fields.gaussian_blobs((48, 40, 33), count=6, sigma=(4.0, 9.0), seed=7).numpy(), 0.4
+        mn, mx = (-300.25, 17.5, 1000.0), (-100.0, 80.0, 1090.5)
+    else:
+        vol, iso = fields.as_u16_numpy(fields.value_noise_u16((70, 64, 50), base_period=16, seed=5)), 32768.0
+    a = oracle.extract(vol, mn, mx, iso=iso)
+    b = oracle.extract(vol, mn, mx, iso=iso, precision=1)
     assert np.array_equal(a["quads"], b["quads"])
-    assert np.abs(a["vertices"] - b["vertices"]).max() < 1e-4
+    assert len(a["vertices"]) > 100
+    fp64bound.check(a["vertices"], b["vertices"], vol.shape[::-1], mn, mx)
 
 
 @pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))), ids=os.path.basename)
