@@ -133,13 +133,35 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic(workload):
-    """DRAM bytes per launch of the emit kernel from the committed ncu summary."""
+# the sources of the brick kernels: a DRAM-traffic figure holds only for the
+# build it was captured on
+TRAFFIC_SOURCES = ("dmc_brick.cu", "dmc_device.cuh", "dmc_scan.cuh", "dmc_tables.inc", "dmc_internal.h")
+
+
+def kernel_sources_sha256():
+    import hashlib
+    h = hashlib.sha256()
+    for name in TRAFFIC_SOURCES:
+        with open(os.path.join(ROOT, "framework_gb300", "csrc", name), "rb") as f:
+            h.update(name.encode() + b"\0" + f.read())
+    return h.hexdigest()
+
+
+def profile_traffic(workload, kernel="emit"):
+    """DRAM bytes per launch of a brick kernel on a workload, from the ncu
+    capture recorded in profiles/traffic.json.  The record carries the
+    sha256 of the kernel sources it was captured on; when the sources have
+    changed since, the figure no longer describes this build: a warning goes
+    to stderr and the traffic is reported as null."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if not os.path.exists(p):
         return None
     d = json.load(open(p))
-    return d.get(workload)
+    if d.get("sources_sha256") != kernel_sources_sha256():
+        print("warning: profiles/traffic.json was captured on other kernel sources; traffic reported as null",
+              file=sys.stderr, flush=True)
+        return None
+    return d.get("%s:%s" % (workload, kernel))
 
 
 def cpu_model():
@@ -206,9 +228,10 @@ def run_reference(args, rank):
     import torch
     if rank != 0:
         return
-    dims, dtype, iso, desc = WORKLOADS[args.workload]
+    wl = "noise1024" if args.workload == "shard1024" else args.workload   # the sharded volume is the same field
+    dims, dtype, iso, desc = WORKLOADS[wl]
     dev = "cuda" if torch.cuda.is_available() else "cpu"
-    vol, iso = make_volume(args.workload, dev)
+    vol, iso = make_volume(wl, dev)
     from framework_gb300 import fields
     host = fields.as_u16_numpy(vol) if dtype == "uint16" else vol.cpu().numpy()
     import oracle
@@ -473,9 +496,10 @@ def run_batch_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
-SERVED_DESC = ("device-resident pool of 64 volumes, per-axis dims log-uniform 32-512, f32 blobs / u16 lattice "
-               "noise / f32 gyroid; requests (volume, iso uniform in that field's 5th-95th percentile) with "
-               "seeded Poisson arrivals; admission by worst-case output bound")
+SERVED_DESC = ("device-resident pool of 64 volumes, per-axis dims log-uniform 32-512 with the upper tail "
+               "weighted to a ~6 GB pool (each draw kept with probability (points/512^3)^1.4), f32 blobs / u16 "
+               "lattice noise / f32 gyroid; requests (volume, iso uniform in that field's 5th-95th percentile) "
+               "with seeded Poisson arrivals; admission by worst-case output bound")
 
 
 # output arenas of the served bench: 4.0 G vertices (48 GB) and 2.1 G quads (34 GB)
@@ -614,27 +638,18 @@ def run_served_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
-def run_served(args, rank, world, dist=None):
-    import numpy as np
+def served_e2e(vols, local, plain=False, n=128):
+    """End to end: a burst of n requests, each mesh copied into page-locked
+    host buffers (a ring of reused ones, sized from the warm-up meshes, grown
+    if ever short) and released once its copy is done.  The copies run on a
+    copy stream, so the next result's copy is queued while one is in flight.
+    With plain=True the same burst goes to the plain per-request server."""
     import torch
     import framework_gb300 as fg
-    local = int(os.environ.get("LOCAL_RANK", "0"))   # this rank's GPU (the current device)
-    vols = make_pool("cuda")
-    N = sum(d["volume"].numel() for d in vols)
-    nbytes = sum(d["volume"].numel() * d["volume"].element_size() for d in vols)
-    clocks = ClockSampler(local)
-    clocks.start()
-    m = served_measure(vols, n_req=max(200, 60 * args.steps), device=local)
-    clk = clocks.stop()
-    # every rank serves its own request stream: whole-job capacity is the sum
-    _, total_rps = combine_ranks(0.0, m["served"]["capacity_rps"], dist, "cuda")
-    # end to end: a burst of requests, each mesh copied into page-locked host
-    # buffers (a ring of reused ones, sized from the warm-up meshes, grown if
-    # ever short) and released once its copy is done.  The copies run on a
-    # copy stream, so the next result's copy is queued while one is in flight.
-    vid, iso, _ = request_trace(vols, 128, 0, seed=4)
+    vid, iso, _ = request_trace(vols, n, 0, seed=4)
     d2h = 0
-    with fg.Server(local, vertex_arena=SERVED_VERTEX_ARENA, quad_arena=SERVED_QUAD_ARENA) as srv:
+    kw = dict(plain=True) if plain else {}
+    with fg.Server(local, vertex_arena=SERVED_VERTEX_ARENA, quad_arena=SERVED_QUAD_ARENA, **kw) as srv:
         idmap = [srv.add_volume(d["volume"]) for d in vols]
         vmax = qmax = 1
         for v in range(len(vols)):                     # warm up: each volume once
@@ -670,6 +685,25 @@ def run_served(args, rank, world, dist=None):
         for s in range(nslot):
             retire(s)
         e2e_s = time.perf_counter() - t0
+    return {"rps": round(len(rids) / e2e_s, 2), "d2h_per_request": int(d2h / len(rids)), "requests": len(rids)}
+
+
+def run_served(args, rank, world, dist=None):
+    import numpy as np
+    import torch
+    import framework_gb300 as fg
+    local = int(os.environ.get("LOCAL_RANK", "0"))   # this rank's GPU (the current device)
+    vols = make_pool("cuda")
+    N = sum(d["volume"].numel() for d in vols)
+    nbytes = sum(d["volume"].numel() * d["volume"].element_size() for d in vols)
+    clocks = ClockSampler(local)
+    clocks.start()
+    m = served_measure(vols, n_req=max(200, 60 * args.steps), device=local)
+    clk = clocks.stop()
+    # every rank serves its own request stream: whole-job capacity is the sum
+    _, total_rps = combine_ranks(0.0, m["served"]["capacity_rps"], dist, "cuda")
+    e2e = served_e2e(vols, local, plain=False)
+    e2e_plain = served_e2e(vols, local, plain=True)
     if rank != 0:
         return None
     cpu = None
@@ -687,14 +721,112 @@ def run_served(args, rank, world, dist=None):
                    "p99_ms_at_0.8_served_capacity": m["sweep"]["served@0.8served"]["p99_ms"],
                    "l2": "pool %.2f GB > L2" % (nbytes / 1e9)},
         "cpu_baseline": cpu,
-        "e2e": {"value": round(len(rids) / e2e_s, 2), "unit": "requests/s", "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": int(d2h / len(rids)),
+        "e2e": {"value": e2e["rps"], "unit": "requests/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": e2e["d2h_per_request"], "requests": e2e["requests"],
+                "plain_value": e2e_plain["rps"],
                 "note": "pool resident on the device; per request the mesh is copied into page-locked host buffers "
-                        "(Server.fetch_into on a copy stream, three buffers in turn)"},
+                        "(Server.fetch_into on a copy stream, three buffers in turn); plain_value: the plain "
+                        "per-request server on the same burst, same copies"},
         "gpu_launches": 7 * m["served"]["stats"]["batches"],
         "clocks": clk,
     }
     return line
+
+
+def run_shard(args, rank, world, dist=None):
+    """One 1024^3 uint16 noise volume split in z across the ranks (strong
+    scaling): each rank holds its cell planes plus halo, counts its part,
+    all-gathers the (vertices, quads) totals (NCCL under torchrun, the path's
+    one collective) and writes its part with global indices.  A step is
+    count + exchange + emit; value = the whole volume's points / the slowest
+    rank's step time.  e2e adds, per step, the upload of the rank's planes
+    from page-locked host memory and the download of its part."""
+    import torch
+    import framework_gb300 as fg
+    from framework_gb300 import fields, shard
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dims, dtype, iso, desc = WORKLOADS["noise1024"]
+    nz = dims[2]
+    full = fields.value_noise_u16(dims, device="cuda")
+    zb, ze = shard.shard_ranges(nz - 1, world)[rank]
+    p0, p1 = shard.point_planes(nz, zb, ze)
+    part_in = full[p0:p1].clone()
+    del full
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    N = dims[0] * dims[1] * dims[2]
+    ex = fg.Extractor(local, algo="brick")
+    res = shard.extract_sharded(ex, part_in, nz, zb, ze, iso=iso, dist=dist)
+    V, Q = res["vertices"].shape[0], res["quads"].shape[0]
+    vbuf = torch.empty((max(V, 1), 3), device="cuda")
+    qbuf = torch.empty((max(Q, 1), 4), dtype=torch.int32, device="cuda")
+
+    def step():
+        nv, nq = ex.shard_count(part_in, nz, zb, ze, None, None, iso)
+        totals = shard.exchange_totals(nv, nq, dist)
+        voff, _ = shard.exclusive_offsets(totals, rank)
+        ex.shard_emit(voff, vbuf, qbuf)
+        return totals
+    for _ in range(args.warmup):
+        step()
+    clocks = ClockSampler(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        totals = step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    ms, _ = combine_ranks(ev0.elapsed_time(ev1) / args.steps, 0, dist, "cuda")
+    # end to end: planes in from page-locked host memory, the part out
+    host_in = torch.empty(part_in.shape, dtype=part_in.dtype, pin_memory=True)
+    host_in.copy_(part_in)
+    hv = torch.empty((max(V, 1), 3), dtype=torch.float32, pin_memory=True)
+    hq = torch.empty((max(Q, 1), 4), dtype=torch.int32, pin_memory=True)
+    e2e_steps = max(1, min(args.e2e_steps, args.steps))
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        part_in.copy_(host_in, non_blocking=True)
+        step()
+        hv.copy_(vbuf[:max(V, 1)], non_blocking=True)
+        hq.copy_(qbuf[:max(Q, 1)], non_blocking=True)
+        torch.cuda.synchronize()
+    e2e_ms, _ = combine_ranks((time.perf_counter() - t0) * 1e3 / e2e_steps, 0, dist, "cuda")
+    ex.close()
+    if rank != 0:
+        return None
+    Vt, Qt = sum(t[0] for t in totals), sum(t[1] for t in totals)
+    hbm, peak_kind = peaks()
+    alg_bytes = 2 * N + 12 * Vt + 16 * Qt
+    return {
+        "metric": "GVoxels/s", "value": round(N / (ms * 1e-3) / 1e9, 3), "unit": "GVoxels/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
+        "scaling": "strong", "vs_baseline": None, "dtype": "u16", "data": "synthetic",
+        "config": {"workload": "shard1024", "desc": desc + "; one volume split in z across ranks",
+                   "dims": list(dims), "iso": iso, "vertices": Vt, "quads": Qt,
+                   "parallelism": "z-slab shards, all-gather of (V, Q) per rank" if world > 1 else "single GPU",
+                   "l2": "input larger than L2 (no flush needed)"},
+        "roofline": {"bound": "hbm", "achieved": round(alg_bytes / (ms * 1e-3) / 1e9 / max(world, 1), 1),
+                     "peak": hbm, "unit": "GB/s",
+                     "frac": round(alg_bytes / (ms * 1e-3) / 1e9 / max(world, 1) / hbm, 4), "traffic": None,
+                     "kernel": "whole step per GPU", "peak_kind": peak_kind, "algorithmic_bytes": alg_bytes},
+        "cpu_baseline": None,
+        "e2e": {"value": round(N / (e2e_ms * 1e-3) / 1e9, 3), "unit": "GVoxels/s",
+                "h2d_bytes_per_step": 2 * dims[0] * dims[1] * (p1 - p0), "d2h_bytes_per_step": 12 * V + 16 * Q,
+                "steps": e2e_steps, "note": "per rank: its planes in, its part out (rank 0's bytes shown)"},
+        "gpu_launches": 6 * args.steps,
+        "clocks": clk,
+    }
 
 
 def main():
@@ -703,7 +835,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="noise1024", choices=sorted(WORKLOADS) + ["batch256", "served64"])
+    ap.add_argument("--workload", default="noise1024", choices=sorted(WORKLOADS) + ["batch256", "served64", "shard1024"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-extras", action="store_true",
@@ -732,6 +864,14 @@ def main():
         return
 
     torch.cuda.set_device(local)
+    if args.workload == "shard1024":
+        line = run_shard(args, rank, world, dist)
+        if line:
+            print(json.dumps(line), flush=True)
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
     if args.workload == "served64":
         line = run_served(args, rank, world, dist)
         if line:

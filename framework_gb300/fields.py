@@ -166,18 +166,28 @@ def uneven_batch_specs(count=256, lo=16, hi=256, seed=5):
     return specs
 
 
-def served_pool_specs(count=64, lo=32, hi=512, seed=9):
+def served_pool_specs(count=64, lo=32, hi=512, seed=9, size_tilt=1.4):
     """Per-volume recipe of the serving pool: dims log-uniform in [lo, hi] per
     axis; field kind uniform over blobs (float32), lattice noise (uint16) and
     gyroid (float32).  Blobs keep 32 centres, sigma 8-32, amplitude 0.5-1.5;
     noise keeps 4 octaves and persistence 0.5 with a base period of 32 voxels
     (most pool volumes are far smaller than 1024); gyroid frequency uniform in
-    [0.05, 0.4] rad/voxel."""
+    [0.05, 0.4] rad/voxel.
+
+    Size tilt: a plain log-uniform draw gives a pool of about 1.1 GB on
+    average, while the served configuration asks for about 6 GB.  Each drawn
+    dims triple is therefore kept with probability (points / hi^3)^size_tilt
+    and redrawn otherwise: the dims stay log-uniform in shape, with the upper
+    tail weighted.  size_tilt = 1.4 puts the expected pool at about 6 GB
+    (0: the plain draw)."""
     rng = np.random.default_rng(seed)
     specs = []
     for i in range(count):
-        d = np.floor(np.exp(rng.uniform(math.log(lo), math.log(hi), 3))).astype(int)
-        d = np.clip(d, lo, hi)
+        while True:
+            d = np.floor(np.exp(rng.uniform(math.log(lo), math.log(hi), 3))).astype(int)
+            d = np.clip(d, lo, hi)
+            if size_tilt <= 0 or rng.uniform() < (float(np.prod(d)) / float(hi) ** 3) ** size_tilt:
+                break
         kind = ("blobs", "noise", "gyroid")[int(rng.integers(0, 3))]
         specs.append(dict(dims=(int(d[0]), int(d[1]), int(d[2])), kind=kind,
                           freq=float(rng.uniform(0.05, 0.4)), seed=2000 + i))
