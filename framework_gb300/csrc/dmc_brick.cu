@@ -607,11 +607,58 @@ __device__ __forceinline__ const DeviceTables &stage_tables(const DeviceTables *
     return *s;
 }
 
-__device__ __forceinline__ uint32_t claim_brick(uint32_t *ticket, int lane)
+// Volume of launch brick bg: the last one whose first brick is <= bg.
+__device__ __forceinline__ uint32_t volume_of(const Geom *vols, uint32_t nvols, uint64_t bg)
 {
-    uint32_t b = 0;
-    if (lane == 0) b = atomicAdd(ticket, 1u);
-    return __shfl_sync(0xffffffffu, b, 0);
+    uint32_t lo = 0, hi = nvols - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (vols[mid].brick_base <= bg) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+constexpr uint32_t kMaxRun = 16;   // most bricks one claim of a sweep takes
+
+// Sweep work claim (guided self-scheduling): a run of consecutive units
+// sized to about half of what remains per warp, between 1 and kMaxRun, so
+// early claims are long (few halo planes) and the last ones short (even
+// finish).  [lo, hi) is empty once every unit is taken.
+__device__ __forceinline__ void claim_run(uint32_t *ticket, uint32_t n_units, uint32_t n_warps, int lane,
+                                          uint32_t &lo, uint32_t &hi)
+{
+    uint32_t t = 0, r = 0;
+    if (lane == 0) {
+        const uint32_t seen = *reinterpret_cast<volatile uint32_t *>(ticket);
+        const uint32_t want = n_units > seen ? (n_units - seen) / (2u * n_warps) : 0u;
+        r = want < 1u ? 1u : (want > kMaxRun ? kMaxRun : want);
+        t = atomicAdd(ticket, r);
+    }
+    t = __shfl_sync(0xffffffffu, t, 0);
+    r = __shfl_sync(0xffffffffu, r, 0);
+    lo = t;
+    hi = t < n_units ? (n_units - t < r ? n_units : t + r) : t;
+}
+
+// Sweep unit u of a launch, numbered z fastest within each column of
+// bricks so that consecutive units are z neighbours: its column (xs + nxs *
+// yb), z brick, and the units left in the column from it.  All bricks of a
+// launch (u is the launch brick number; volumes keep their brick ranges), or
+// a range of whole brick planes of one volume (u counts from its start).
+__device__ __forceinline__ uint32_t count_unit(const Geom &g, const BrickRange &range, uint32_t u, uint32_t &zb,
+                                               uint32_t &limit)
+{
+    const uint32_t ncol = g.nxs * g.nyb;
+    if (range.cnt == kAllBricks) {
+        const uint32_t b = (uint32_t)(u - g.brick_base);
+        zb = b % g.nzb;
+        limit = g.nzb - zb;
+        return b / g.nzb;
+    }
+    const uint32_t zb_lo = (uint32_t)(((uint64_t)range.lo - g.brick_base) / ncol), nzr = range.cnt / ncol;
+    zb = zb_lo + u % nzr;
+    limit = nzr - u % nzr;
+    return u / nzr;
 }
 
 // Corner samples 2, 5, 6, 7 (the cell's own edges) or all eight.
@@ -692,23 +739,28 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 3) brick_sweep(cons
     const uint64_t nbricks = head->nbricks[group];
     const Geom *__restrict__ vols = batch_geoms(head) + (group ? head->nvol[0] : 0u);
 
+    // The claimed bricks not yet swept, [span, span_end) in the z-fastest
+    // numbering of count_unit.  A warp sweeps a run of bricks along z of one
+    // column as one tall brick: the masks of a plane carry from one brick to
+    // the next, so each run loads (count) or fetches and ranks (emit) one
+    // plane more than it owns, instead of one per brick.
+    uint32_t span = 0, span_end = 0;
+    const uint32_t n_units = range.cnt == kAllBricks ? (uint32_t)nbricks : range.cnt;
     for (;;) {
-        const uint32_t t = claim_brick(ticket, lane);
-        if (t >= range.cnt) break;
-        const uint64_t bg = (uint64_t)range.lo + t;
-        if (bg >= nbricks) break;
-        // volume of this brick: last one whose first brick is <= bg
-        uint32_t lo = 0, hi = nvols - 1;
-        while (lo < hi) {
-            const uint32_t mid = (lo + hi + 1) >> 1;
-            if (vols[mid].brick_base <= bg) lo = mid; else hi = mid - 1;
+        if (span >= span_end) {
+            claim_run(ticket, n_units, gridDim.x * nwb(EMIT), lane, span, span_end);
+            if (span >= span_end) break;
         }
-        const Geom g = vols[lo];
+        const uint32_t vi = volume_of(vols, nvols, range.cnt == kAllBricks ? (uint64_t)span : (uint64_t)range.lo);
+        uint32_t zb, limit;
+        const uint32_t col = count_unit(vols[vi], range, span, zb, limit);
+        const uint32_t zrun = min(limit, span_end - span);
+        span += zrun;
+        const uint32_t xs = col % vols[vi].nxs, yb = col / vols[vi].nxs;
+        const Geom g = vols[vi];
+        const uint32_t z0 = zb * g.zc, z1 = min((zb + zrun) * g.zc, g.cells.z);
         const T *__restrict__ vol = reinterpret_cast<const T *>(g.data);
-        const uint32_t b = (uint32_t)(bg - g.brick_base);
-        const uint32_t xs = b % g.nxs, yb = (b / g.nxs) % g.nyb, zb = b / (g.nxs * g.nyb);
-        const uint32_t x0 = xs * W, y0 = yb * ROWS, z0 = zb * g.zc;
-        const uint32_t z1 = min(z0 + g.zc, g.cells.z);
+        const uint32_t x0 = xs * W, y0 = yb * ROWS;
         const uint64_t rowmask = ((1ull << min(NR, g.cells.y - y0)) - 1ull);
         // the emit sweep also visits plane z1: quads of plane z1-1 reference it
         const uint32_t kend = EMIT ? z1 : min(z1, range.zlim) - 1;

@@ -26,6 +26,7 @@ class _Mesh(ctypes.Structure):
         ("n_lut2", ctypes.c_uint64),
         ("n_dropped_quads", ctypes.c_uint64),
         ("n_iso_samples", ctypes.c_uint64),
+        ("ownerless", ctypes.POINTER(ctypes.c_uint8)),
     ]
 
 
@@ -95,6 +96,11 @@ def extract(volume, xyz_min=None, xyz_max=None, iso=0.0, precision=0, num_smooth
         quads = np.ctypeslib.as_array(m.quads, shape=(Q * 4,)).copy().reshape(Q, 4) if Q else np.zeros((0, 4), np.uint32)
         out = dict(vertices=verts, quads=quads, n_active=int(m.n_active), n_lut2=int(m.n_lut2),
                    n_dropped_quads=int(m.n_dropped_quads), n_iso_samples=int(m.n_iso_samples))
+        if precision == 0:
+            # dual vertices of patches without an in-volume owner edge (the
+            # reference leaves them uninitialised): a boolean per vertex
+            out["ownerless"] = (np.ctypeslib.as_array(m.ownerless, shape=(V,)).astype(bool)
+                                if V else np.zeros(0, bool))
     finally:
         lib().oracle_free(ctypes.byref(m))
     out["triangles"] = quads_to_triangles(out["quads"])

@@ -59,6 +59,9 @@ typedef struct {
     uint64_t n_lut2;
     uint64_t n_dropped_quads;
     uint64_t n_iso_samples;
+    uint8_t *ownerless;   /* per vertex (precision 0): 1 for a dual vertex whose patch has no
+                             edge with an owner cell inside the volume (the reference leaves
+                             those uninitialised, dmc.cu:1584-1592), else 0 */
 } oracle_mesh;
 
 /* per active cell record, after _VoxelInfo (dmc.cu:814-1006) */
@@ -213,8 +216,8 @@ static inline uint8_t lut_m(const cell_rec *r, int e)
 void oracle_free(oracle_mesh *m)
 {
     if (!m) return;
-    free(m->vertices); free(m->vertices64); free(m->quads);
-    m->vertices = NULL; m->vertices64 = NULL; m->quads = NULL;
+    free(m->vertices); free(m->vertices64); free(m->quads); free(m->ownerless);
+    m->vertices = NULL; m->vertices64 = NULL; m->quads = NULL; m->ownerless = NULL;
 }
 
 const char *oracle_tables_sha256(void) { return DMC_TABLES_SHA256; }
@@ -489,8 +492,10 @@ int oracle_dmc_ex(const void *vol, int dtype, const uint32_t dims[3], const floa
     const uint64_t csz[3] = {g.cx, g.cy, g.cz};
     if (precision == 0) {
         float *vt = (float *)malloc((V ? V : 1) * 3 * sizeof(float));
-        if (!vt) { free(aoff); free(map); free(cfg); free(rec); return 2; }
+        uint8_t *own = (uint8_t *)calloc(V ? V : 1, 1);
+        if (!vt || !own) { free(vt); free(own); free(aoff); free(map); free(cfg); free(rec); return 2; }
         out->vertices = vt;
+        out->ownerless = own;
         /* edge crossings on owned edges (dmc.cu:1468-1514) */
         #pragma omp parallel for schedule(static)
         for (int64_t a = 0; a < (int64_t)A; ++a) {
@@ -540,6 +545,7 @@ int oracle_dmc_ex(const void *vol, int dtype, const uint32_t dims[3], const floa
             for (uint8_t m = 0; m < niso; ++m) {
                 float *dst = &vt[3 * ((uint64_t)r->vertex_begin + m)];
                 if (!cnt[m]) {
+                    own[(uint64_t)r->vertex_begin + m] = 1;
                     for (int e = 0; e < 12; ++e) {
                         if (lut_m(r, e) != m) continue;
                         float c3[3];
