@@ -1,31 +1,34 @@
 // Brick path: persistent warps sweep bricks of the volume along z.
 //
 // A brick is 128 cell columns x 32 cell rows x a run of z planes and belongs
-// to one warp.  For every point plane the warp keeps two bits per sample,
-// "below" and "at or below the isovalue", in 64-bit masks per column (rows
-// 0..33).  The count sweep builds them from the samples: each lane loads four
-// adjacent samples of a row at a time, 8 rows in flight, and compares them (two
-// uint16 samples per word at once).  It also keeps them in a global mask
-// store, from which the emit sweep copies them back with cp.async.bulk
-// instead of reading the samples again.  A cell's configuration is a few
-// shifts on the masks of two columns in two planes, and activity for all
-// rows of a column takes ~12 bitwise operations, so only active cells (a few
-// percent) take the per-cell path.  A 32x32 bit transpose turns the column
-// masks into each row's active cells in x order.  Warps never wait for each
-// other: there is no block-level barrier in the sweep.
+// to one warp.  The count sweep keeps two bits per sample of every point
+// plane, "below" and "at or below the isovalue", in 64-bit masks per column
+// (rows 0..33), built from the samples: each lane loads four adjacent samples
+// of a row at a time, 8 rows in flight, and compares them (two uint16 samples
+// per word at once).  A cell's configuration is a few shifts on the masks of
+// two columns in two planes, and activity for all rows of a column takes ~12
+// bitwise operations, so only active cells (a few percent) take the per-cell
+// path.  A 32x32 bit transpose turns the column masks into each row's active
+// cells in x order.  The count sweep classifies them (configuration, 2B/3B
+// test, own-edge bits) and keeps the result in a cell store, one record per
+// active cell and a header of row starts per brick plane; the emit sweep
+// reads the store back instead of classifying the cells again, so it never
+// touches the masks.  Warps never wait for each other: there is no
+// block-level barrier in the sweep.
 //
 // Output order is the reference's (ascending cell index, x fastest,
 // utils.hpp:72), so the active cells of one plane, row and 128-column
 // segment form one contiguous output range, a "segment" (k, j, xs).
-//   count sweep : per segment (vertices, quads)
+//   count sweep : per segment (vertices, quads); the cell store
 //   scan        : decoupled look-back over segments -> offsets
-//   emit sweep  : ranks the active cells of each row, writes vertex positions
-//                 and quads at their final places.
+//   emit sweep  : lists each plane's cells from the store, writes vertex
+//                 positions and quads at their final places.
 // Quads reference the dual vertices of the +x, +y, +z neighbours
-// (dmc.cu:1636-1664): the emit sweep also ranks the first cell column of the
+// (dmc.cu:1636-1664): the emit sweep also lists the first cell column of the
 // next segment (its vertices start at that segment's offset) and the first
-// row of the next brick (ranked inside its own segment), and writes the quads
-// of plane k once plane k+1 has been ranked.
+// row of the next brick (ranked inside its own segment), both from their own
+// bricks' store slots, and writes the quads of plane k once plane k+1 has
+// been listed.
 #include "dmc_device.cuh"
 #include "dmc_scan.cuh"
 #include "dmc_internal.h"
@@ -47,7 +50,7 @@ constexpr int CAP = 256;                  // entries kept in shared memory per p
 constexpr int OVF = MAXL - CAP;           // entries per plane that spill to global scratch
 constexpr int NWB_COUNT = 8;              // warps per block of the count sweep (independent): 3 blocks per SM at 80
                                           // registers (4 blocks at 64 spilled and ran 10% slower)
-constexpr int NWB_EMIT = 8;               // of the emit sweep: 2 blocks per SM
+constexpr int NWB_EMIT = 8;               // of the emit sweep: 3 blocks per SM
 constexpr int nwb(bool emit) { return emit ? NWB_EMIT : NWB_COUNT; }
 constexpr int kMaxSlabs = 32;             // z slabs of a streamed host extraction
 constexpr int kTickets = 4 + 3 * kMaxSlabs; // work tickets: 4 for a batch, 3 per streamed slab
@@ -62,8 +65,7 @@ struct Geom {
     uint64_t brick_base;   // first brick of this volume in the launch's brick numbering
     uint64_t seg_base;     // first segment of this volume in the shared segment arrays
     uint64_t nseg;
-    uint64_t mask_base;    // first word of this volume's plane masks in the mask store
-    uint32_t mask_tw;      // words of one mask over a row of tiles: 130 per tile, the last one rounded to even
+    uint64_t cell_base;    // first word of this volume's slots in the cell store
     float iso;
     uint32_t iso_u16;      // uint16 samples: v < iso  <=>  v < iso_u16 (65536: always)
     uint32_t isole_u16;    // uint16 samples: v <= iso <=>  v < isole_u16
@@ -78,46 +80,76 @@ struct alignas(16) PlaneMasks {
     uint64_t le[W + 2];                // bit r: sample <= iso
 };
 
-// Mask store (global scratch): the count sweep keeps the masks of every
-// point plane of every tile (128 + 2 columns x 34 rows) and the emit sweep
-// copies them back instead of reading and comparing the samples again.
-// Chunk of tile (xs, yb), plane p: lt of its columns, then le of them, each
-// mask_cols() words; tiles of one row lie side by side.
-__device__ __forceinline__ uint32_t mask_cols(const Geom &g, uint32_t x0)
+// Cell store (global scratch).  For every cell plane of every brick (a
+// "slot": 128 columns x 32 rows of one plane) the count sweep writes what it
+// found, and the emit sweep reads it back instead of classifying the cells
+// again:
+//   header (kHdrWords words): the first list entry of each row, rowstart[0..33]
+//     as 16-bit pairs (rowstart[32] = entries of the slot), then the rows whose
+//     cell in column 0 is active (bit r);
+//   records (kRecWords words, one per active cell, row-major, x ascending):
+//     column | row << 7 | config << 12 | LUT2 << 20 | own-edge info << 21.
+// Slot s = (k * nyb + yb) * nxs + xs of a volume; its headers come first, then
+// its records, 4 bytes per cell of the volume's bricks.
+constexpr uint32_t kHdrWords = 20;
+constexpr uint32_t kRecWords = W * ROWS;
+__device__ __forceinline__ uint64_t cell_slot(const Geom &g, uint32_t k, uint32_t yb, uint32_t xs)
 {
-    return min((uint32_t)W + 2u, (g.pts.x - x0 + 1u) & ~1u);   // columns in the volume, rounded to even
+    return ((uint64_t)k * g.nyb + yb) * g.nxs + xs;
 }
-__device__ __forceinline__ uint64_t *mask_chunk(uint64_t *masks, const Geom &g, uint32_t xs, uint32_t yb, uint32_t p)
+__device__ __forceinline__ uint32_t *slot_hdr(uint32_t *cells, const Geom &g, uint64_t s)
 {
-    return masks + g.mask_base + ((uint64_t)p * g.nyb + yb) * 2ull * g.mask_tw + 2ull * (W + 2) * xs;
+    return cells + g.cell_base + s * kHdrWords;
 }
+__device__ __forceinline__ uint32_t *slot_rec(uint32_t *cells, const Geom &g, uint64_t s)
+{
+    return cells + g.cell_base + (uint64_t)g.cells.z * g.nyb * g.nxs * kHdrWords + s * kRecWords;
+}
+// 16-bit entry i of a slot header
+__device__ __forceinline__ uint32_t hdr_u16(const uint32_t *h, uint32_t i)
+{
+    return (__ldg(h + (i >> 1)) >> (16 * (i & 1))) & 0xffffu;
+}
+__device__ __forceinline__ uint32_t rec_pack(uint32_t c, uint32_t r, uint32_t cfg, bool l2, uint32_t info)
+{
+    return c | (r << 7) | (cfg << 12) | ((l2 ? 1u : 0u) << 20) | (info << 21);
+}
+__device__ __forceinline__ uint32_t rec_col(uint32_t w) { return w & 0x7fu; }
+__device__ __forceinline__ uint32_t rec_row(uint32_t w) { return (w >> 7) & 0x1fu; }
+__device__ __forceinline__ uint32_t rec_cfg(uint32_t w) { return (w >> 12) & 0xffu; }
+__device__ __forceinline__ bool rec_l2(uint32_t w) { return (w >> 20) & 1u; }
+__device__ __forceinline__ uint32_t rec_info(uint32_t w) { return (w >> 21) & 0x3fu; }
 
-// Per-warp state used by both sweeps (the count sweep allocates only this).
-struct alignas(16) SweepSmem {
-    PlaneMasks mask[2];                // point planes by parity
+// Per-warp ranking state of both sweeps: each plane's active cells in list
+// (output) order and per row.
+struct alignas(16) RankSmem {
     uint32_t xrow[2][HROWS][GROUPS];   // per row: active cells in x order, word q = columns 32q..32q+31
     uint64_t hact[2];                  // halo column activity (bit = row)
     uint16_t rowstart[2][HROWS + 1];   // first list entry of each row
     uint32_t rowbase[HROWS];           // running (v | q << 16) prefix at each row start
-    uint32_t rowtot[ROWS];             // count sweep: per-row (v | q << 16)
     uint16_t lst0[CAP];                // list of plane slot 0: row << 8 | col (the count sweep uses only this)
 };
 
-// Per-warp state of the emit sweep.
-struct alignas(16) WarpSmem : SweepSmem {
+// Per-warp state of the count sweep: the two point planes as bit masks.
+struct alignas(16) CountSmem : RankSmem {
+    PlaneMasks mask[2];                // point planes by parity
+    uint32_t rowtot[ROWS];             // per-row (v | q << 16)
+};
+
+// Per-warp state of the emit sweep (no masks: it reads the cell store).
+struct alignas(16) EmitSmem : RankSmem {
     uint16_t lst1[CAP];                // list of plane slot 1
     uint32_t segv[2][HROWS][2];        // vertex offset of (row, own / next segment)
     uint32_t segq[2][HROWS];           // quad offset of (row, own segment)
     uint32_t qwork[QBUF];              // quads of one round of owner cells: owner lane | edge << 5 | wanted edges << 7
     uint4 orec[32];                    // owners of the round, by lane: (entry | rank r1 << 16, r2 | r3 << 16, first quad, cell | info << 16)
-    uint32_t ent[2][CAP];              // packed cell: vrel 11 | qrel 10 | cfg 8 | lut2 1
+    uint32_t ent[2][CAP];              // a cell's record, then (once classified) its packed cell: vrel 11 | qrel 10 | cfg 8 | lut2 1
     uint8_t info[2][CAP];              // own-edge bipolar/ccw bits
-    uint64_t mbar[2];                  // completion of the bulk copies into mask[0] / mask[1]
 };
 
-static_assert(sizeof(WarpSmem) % 16 == 0 && sizeof(SweepSmem) % 16 == 0, "per-warp shared memory must keep 16-byte alignment");
+static_assert(sizeof(EmitSmem) % 16 == 0 && sizeof(CountSmem) % 16 == 0, "per-warp shared memory must keep 16-byte alignment");
 
-// shared memory layout of a sweep block: tables, then one WarpSmem per warp
+// shared memory layout of a sweep block: tables, then one per-warp state per warp
 constexpr size_t kTablesBytes = (sizeof(DeviceTables) + 127) & ~(size_t)127;
 
 struct Spill {                          // per warp slot, global memory
@@ -129,10 +161,16 @@ struct Spill {                          // per warp slot, global memory
 // A plane's entries: the first CAP in shared memory, the rest in the warp's
 // global spill slot.  Separate shared and global accesses (rather than one
 // reference that may point to either) keep the common case on shared-memory
-// instructions.
+// instructions.  The count sweep has one list slot and no entry words.
+template <class SM>
 struct WarpMem {
-    WarpSmem *s;
+    SM *s;
     Spill *g;
+    __device__ __forceinline__ uint16_t *lst_s(int p) const
+    {
+        if constexpr (std::is_same<SM, EmitSmem>::value) return p ? s->lst1 : s->lst0;
+        else return s->lst0;
+    }
     __device__ __forceinline__ uint32_t ent(int p, uint32_t i) const
     {
         uint32_t v;
@@ -146,12 +184,12 @@ struct WarpMem {
     __device__ __forceinline__ uint32_t lst(int p, uint32_t i) const
     {
         uint32_t v;
-        if (i < CAP) v = (p ? s->lst1 : s->lst0)[i]; else v = g->lst[p][i - CAP];
+        if (i < CAP) v = lst_s(p)[i]; else v = g->lst[p][i - CAP];
         return v;
     }
     __device__ __forceinline__ void set_lst(int p, uint32_t i, uint32_t v)
     {
-        if (i < CAP) (p ? s->lst1 : s->lst0)[i] = (uint16_t)v; else g->lst[p][i - CAP] = (uint16_t)v;
+        if (i < CAP) lst_s(p)[i] = (uint16_t)v; else g->lst[p][i - CAP] = (uint16_t)v;
     }
     __device__ __forceinline__ uint32_t info(int p, uint32_t i) const
     {
@@ -219,11 +257,10 @@ __device__ __forceinline__ uint32_t le_u16x2(uint32_t v, uint32_t m, uint32_t mh
 // active).  Loads go out 8 rows per lane before their results are used; the
 // next plane is not prefetched into L2 (all resident warps' planes together
 // outrun the L2, and prefetched lines were evicted before their use, which
-// read the volume 1.9 times instead of 1.35).  With gm set, the masks also go
-// to the mask store chunk gm (ncolr columns per mask).
+// read the volume 1.9 times instead of 1.35).
 template <class T>
 __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint32_t thr, uint32_t thr_le, uint32_t x0,
-                                        uint32_t y0, uint32_t p, PlaneMasks &m, int lane, uint64_t *gm, uint32_t ncolr)
+                                        uint32_t y0, uint32_t p, PlaneMasks &m, int lane)
 {
     uint32_t lo[GROUPS] = {0, 0, 0, 0}, hi[GROUPS] = {0, 0, 0, 0};
     uint32_t elo[GROUPS] = {0, 0, 0, 0}, ehi[GROUPS] = {0, 0, 0, 0};
@@ -325,10 +362,6 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
         const uint4 e1 = make_uint4(elo[2] & rmask_le, ehi[2] & hmask_le, elo[3] & rmask_le, ehi[3] & hmask_le);
         uint4 *lt4 = reinterpret_cast<uint4 *>(&m.lt[4 * lane]), *le4 = reinterpret_cast<uint4 *>(&m.le[4 * lane]);
         lt4[0] = t0; lt4[1] = t1; le4[0] = e0; le4[1] = e1;
-        if (gm) {   // all 128 columns are in the volume here, so ncolr >= 128
-            uint4 *g4 = reinterpret_cast<uint4 *>(gm + 4 * lane), *ge4 = reinterpret_cast<uint4 *>(gm + ncolr + 4 * lane);
-            g4[0] = t0; g4[1] = t1; ge4[0] = e0; ge4[1] = e1;
-        }
     } else {
         const T *base = vol + (plane0 + y0) * sx + x0 + lane;
         bool cok[GROUPS];
@@ -369,7 +402,6 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
             const uint64_t e = (uint64_t)(elo[j] & rmask & cm) | ((uint64_t)(ehi[j] & hmask & cm) << 32);
             m.lt[c] = t;
             m.le[c] = e;
-            if (gm && c < ncolr) { gm[c] = t; gm[ncolr + c] = e; }
         }
     }
 #pragma unroll 1
@@ -388,55 +420,7 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
             const uint64_t t = (uint64_t)l32 | ((uint64_t)h2 << 32), e = (uint64_t)e32 | ((uint64_t)eh2 << 32);
             m.lt[W + hc] = t;
             m.le[W + hc] = e;
-            if (gm && W + hc < ncolr) { gm[W + hc] = t; gm[ncolr + W + hc] = e; }
         }
-    }
-}
-
-// mbarrier and bulk-copy (TMA) primitives for the mask fetches.  Waits are
-// bounded: a wait that gives up returns false and the caller reports
-// DEV_ERR_TIMEOUT.
-__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void mbar_init(uint64_t *bar)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
-}
-__device__ __forceinline__ void mbar_expect(uint64_t *bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
-{
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar))
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
-{
-    const uint32_t a = smem_addr(bar);
-    for (uint32_t it = 0; it < (1u << 20); ++it) {
-        uint32_t done;
-        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}"
-                     : "=r"(done) : "r"(a), "r"(parity) : "memory");
-        if (done) return true;
-    }
-    return false;
-}
-
-// Bulk copy of plane p's masks from the mask store into slot m (lane 0
-// issues; the slot's mbarrier counts the bytes).  The warp must be done
-// reading the slot's previous plane.
-__device__ __forceinline__ void fetch_masks(uint64_t *masks, const Geom &g, uint32_t xs, uint32_t yb, uint32_t x0,
-                                            uint32_t p, PlaneMasks &m, uint64_t *bar, int lane)
-{
-    __syncwarp();
-    if (lane == 0) {
-        const uint32_t n = mask_cols(g, x0);
-        const uint64_t *src = mask_chunk(masks, g, xs, yb, p);
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        mbar_expect(bar, 16u * n);
-        bulk_g2s(m.lt, src, 8u * n, bar);
-        bulk_g2s(m.le, src + n, 8u * n, bar);
     }
 }
 
@@ -687,53 +671,129 @@ __device__ __forceinline__ uint32_t ring_edge(int s, int kk)
     return (uint32_t)((E >> (4 * (4 * s + kk))) & 0xfull);
 }
 
+// Emit sweep: plane k of brick (xs, yb) as a list, read from the cell store.
+// Besides the slot's own cells, the quads need the halo: column W (column 0
+// of the next x brick) and row 32 (row 0 of the next y brick).  List order is
+// output order: rows 0..31, each followed by its column-W cell, then row 32
+// and its column-W cell.  Each entry's record goes to ent[p]; xrow[p], hact[p]
+// and rowstart[p][0..33] index the list.  Returns its length.
+template <class T, class SM>
+__device__ __forceinline__ uint32_t load_slot_list(uint32_t *cells, const Geom &g, uint32_t k, uint32_t xs, uint32_t yb,
+                                                    int p, int lane, SM &S, WarpMem<SM> &M, const T *vol, bool pf)
+{
+    const uint64_t s0 = cell_slot(g, k, yb, xs);
+    const bool hx = xs + 1 < g.nxs, hy = yb + 1 < g.nyb;
+    const uint32_t *h0 = slot_hdr(cells, g, s0);
+    const uint32_t *r0 = slot_rec(cells, g, s0);
+    // own rows: lane r holds the first entry of row r and of row r+1
+    const uint32_t st = hdr_u16(h0, lane), en = hdr_u16(h0, lane + 1);
+    const uint32_t lown = __shfl_sync(0xffffffffu, en, 31);
+    if (lown == 0) {
+        // No own cell: no quad of plane k-1 has a ring cell in this plane
+        // (each ring around an owned edge 9 or 10 holds the cell above the
+        // owner, in an own column and row), so the halo is not needed.
+        S.rowstart[p][lane] = 0;
+        *reinterpret_cast<uint4 *>(S.xrow[p][lane]) = make_uint4(0u, 0u, 0u, 0u);
+        if (lane == 0) {
+            S.rowstart[p][32] = 0;
+            S.rowstart[p][33] = 0;
+            S.hact[p] = 0;
+            *reinterpret_cast<uint4 *>(S.xrow[p][32]) = make_uint4(0u, 0u, 0u, 0u);
+        }
+        __syncwarp();
+        return 0;
+    }
+    // halo column (the next x brick's rows with an active column-0 cell) and
+    // the corner cell of row 32
+    uint32_t col0 = 0, hxrec = 0, n32 = 0, corner = 0, crec = 0;
+    if (hx) {
+        const uint32_t *hX = slot_hdr(cells, g, s0 + 1);
+        col0 = __ldg(hX + 17);
+        if ((col0 >> lane) & 1u) hxrec = __ldg(slot_rec(cells, g, s0 + 1) + hdr_u16(hX, lane));
+    }
+    if (hy) {
+        n32 = hdr_u16(slot_hdr(cells, g, s0 + g.nxs), 1);   // entries of row 0 of the next y brick
+        if (hx && (__ldg(slot_hdr(cells, g, s0 + g.nxs + 1) + 17) & 1u)) {
+            corner = 1;
+            crec = __ldg(slot_rec(cells, g, s0 + g.nxs + 1));
+        }
+    }
+    const uint32_t hcp = __popc(col0 & ((1u << lane) - 1u));   // halo entries in the rows before row lane
+    const uint32_t start32 = lown + __popc(col0);
+    const uint32_t L = start32 + n32 + corner;
+    S.rowstart[p][lane] = (uint16_t)(st + hcp);
+    *reinterpret_cast<uint4 *>(S.xrow[p][lane]) = make_uint4(0u, 0u, 0u, 0u);
+    if (lane == 0) {
+        S.rowstart[p][32] = (uint16_t)start32;
+        S.rowstart[p][33] = (uint16_t)L;
+        S.hact[p] = (uint64_t)col0 | ((uint64_t)corner << 32);
+        *reinterpret_cast<uint4 *>(S.xrow[p][32]) = make_uint4(0u, 0u, 0u, 0u);
+        if (corner) {
+            M.set_lst(p, start32 + n32, (32u << 8) | W);
+            M.set_ent(p, start32 + n32, crec);
+        }
+    }
+    if ((col0 >> lane) & 1u) {   // last entry of row lane
+        M.set_lst(p, en + hcp, ((uint32_t)lane << 8) | W);
+        M.set_ent(p, en + hcp, hxrec);
+    }
+    __syncwarp();
+    for (uint32_t b = 0; b < lown; b += 32) {
+        const uint32_t i = b + lane;
+        const uint32_t rec = i < lown ? __ldg(r0 + i) : 0u;
+        const uint32_t r = rec_row(rec), c = rec_col(rec);
+        const uint32_t shift = __shfl_sync(0xffffffffu, hcp, (int)r);
+        if (i < lown) {
+            if (pf) {
+                const uint64_t sy = g.pts.x, sz = (uint64_t)g.pts.x * g.pts.y;
+                const T *q = vol + (uint64_t)k * sz + (uint64_t)(yb * ROWS + r) * sy + xs * W + c;
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(q));
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(q + sy));
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(q + sz));
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(q + sz + sy));
+            }
+            M.set_lst(p, i + shift, (r << 8) | c);
+            M.set_ent(p, i + shift, rec);
+            atomicOr(&S.xrow[p][r][c >> 5], 1u << (c & 31));
+        }
+    }
+    if (n32) {
+        const uint32_t *rY = slot_rec(cells, g, s0 + g.nxs);
+        for (uint32_t j = lane; j < n32; j += 32) {
+            const uint32_t rec = __ldg(rY + j), c = rec_col(rec);
+            M.set_lst(p, start32 + j, (32u << 8) | c);
+            M.set_ent(p, start32 + j, rec);
+            atomicOr(&S.xrow[p][32][c >> 5], 1u << (c & 31));
+        }
+    }
+    __syncwarp();
+    return L;
+}
+
 // One sweep kernel for both passes.
-//   EMIT = false (count): ranks the active cells of the brick's own 32 rows
-//     and writes per-segment (vertices, quads) totals.
-//   EMIT = true: also ranks the halo row and column, writes the vertices of
-//     plane k at their final offsets and the quads of plane k-1.
+//   EMIT = false (count): ranks and classifies the active cells of the
+//     brick's own 32 rows, writes per-segment (vertices, quads) totals and
+//     each plane's slot of the cell store.
+//   EMIT = true: reads each plane's slot (with the halo row and column from
+//     the neighbouring slots), writes the vertices of plane k at their final
+//     offsets and the quads of plane k-1.
 // Active cells are compacted per plane in output order and processed 32 at a
 // time, one per lane; quads are compacted the same way.
 template <class T, bool EMIT>
-__global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 3) brick_sweep(const BatchHead *__restrict__ head, uint32_t group,
-                                                        BrickRange range, const DeviceTables *__restrict__ tabp,
-                                                        uint2 *__restrict__ seg_cnt, EmitOut out,
-                                                        Spill *__restrict__ spill, uint64_t *masks, uint32_t *ticket,
-                                                        unsigned long long *counters, uint32_t *err)
+__global__ void __launch_bounds__(32 * nwb(EMIT), 3) brick_sweep(const BatchHead *__restrict__ head, uint32_t group,
+                                                                 BrickRange range, const DeviceTables *__restrict__ tabp,
+                                                                 uint2 *__restrict__ seg_cnt, EmitOut out,
+                                                                 Spill *__restrict__ spill, uint32_t *__restrict__ cells,
+                                                                 uint32_t *ticket, unsigned long long *counters,
+                                                                 uint32_t *err)
 {
+    using SM = typename std::conditional<EMIT, EmitSmem, CountSmem>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     if (head->nbricks[group] == 0) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const DeviceTables &tab = stage_tables(tabp, reinterpret_cast<DeviceTables *>(smem_raw));
-    // the count sweep gives each warp only the SweepSmem part
-    WarpSmem &S = *reinterpret_cast<WarpSmem *>(smem_raw + kTablesBytes + (size_t)warp * (EMIT ? sizeof(WarpSmem) : sizeof(SweepSmem)));
-    WarpMem M{&S, spill + (uint64_t)blockIdx.x * nwb(EMIT) + warp};
-    // emit: parity of the next completion of each mask slot's mbarrier, and
-    // the slots with a copy in flight
-    uint32_t phase = 0, pend = 0;
-    if (EMIT) {
-        if (lane == 0) {
-            mbar_init(&S.mbar[0]);
-            mbar_init(&S.mbar[1]);
-            asm volatile("fence.mbarrier_init.release.cluster;\n\tfence.proxy.async.shared::cta;" ::: "memory");
-        }
-        __syncwarp();
-    }
-    // emit: waits for the masks of slot s.  If the copy never completes the
-    // error is reported, the copies in flight get another bounded wait (so
-    // none lands after the warp has left) and the warp stops.
-    auto wait_slot = [&](int s) -> bool {
-        if (__all_sync(0xffffffffu, mbar_wait(&S.mbar[s], (phase >> s) & 1u))) {
-            phase ^= 1u << s;
-            pend &= ~(1u << s);
-            return true;
-        }
-        if (lane == 0) atomicOr(err, DEV_ERR_TIMEOUT);
-        for (int q = 0; q < 2; ++q)
-            if ((pend >> q) & 1u) mbar_wait(&S.mbar[q], (phase >> q) & 1u);
-        return false;
-    };
-    constexpr uint32_t NR = EMIT ? HROWS : ROWS;   // ranked rows
+    SM &S = *reinterpret_cast<SM *>(smem_raw + kTablesBytes + (size_t)warp * sizeof(SM));
+    WarpMem<SM> M{&S, spill + (uint64_t)blockIdx.x * nwb(EMIT) + warp};
     uint32_t n_act = 0, n_l2 = 0, n_drop = 0;
     const uint32_t nvols = head->nvol[group];
     const uint64_t nbricks = head->nbricks[group];
@@ -750,7 +810,7 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 3) brick_sweep(cons
     const uint32_t n_units = range.cnt == kAllBricks ? (uint32_t)nbricks : range.cnt;
     for (;;) {
         uint32_t vi, xs, yb, zb, zrun;
-        if (EMIT) {
+        if constexpr (EMIT) {
             uint32_t t = 0;
             if (lane == 0) t = atomicAdd(ticket, 1u);
             t = __shfl_sync(0xffffffffu, t, 0);
@@ -778,50 +838,36 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 3) brick_sweep(cons
         const uint32_t z0 = zb * g.zc, z1 = min((zb + zrun) * g.zc, g.cells.z);
         const T *__restrict__ vol = reinterpret_cast<const T *>(g.data);
         const uint32_t x0 = xs * W, y0 = yb * ROWS;
-        const uint64_t rowmask = ((1ull << min(NR, g.cells.y - y0)) - 1ull);
         // the emit sweep also visits plane z1: quads of plane z1-1 reference it
         const uint32_t kend = EMIT ? z1 : min(z1, range.zlim) - 1;
 
-        // Point planes z0..z1 of the brick.  The count sweep computes their
-        // masks from the samples and keeps them in the mask store (each
-        // plane once: a brick's last plane only when it is the volume's
-        // last).  The emit sweep copies them back, one plane ahead, and reads
-        // samples only for its corner gathers (demand loads: an L2 prefetch
-        // of whole planes read 1.9 times the bytes the gathers need).
-        const uint32_t ncolr = mask_cols(g, x0);
-        if (EMIT) {
-            fetch_masks(masks, g, xs, yb, x0, z0, S.mask[z0 & 1], &S.mbar[z0 & 1], lane);
-            fetch_masks(masks, g, xs, yb, x0, z0 + 1, S.mask[(z0 + 1) & 1], &S.mbar[(z0 + 1) & 1], lane);
-            pend = 3u;
-            if (!wait_slot(z0 & 1)) return;
-        } else {
-            load_plane<T>(vol, g.pts, g.iso, g.iso_u16, g.isole_u16, x0, y0, z0, S.mask[z0 & 1], lane,
-                          mask_chunk(masks, g, xs, yb, z0), ncolr);
-        }
+        // Count sweep: point planes z0..z1 as bit masks, computed from the
+        // samples (the masks of plane k+1 are loaded while plane k is ranked).
+        if constexpr (!EMIT)
+            load_plane<T>(vol, g.pts, g.iso, g.iso_u16, g.isole_u16, x0, y0, z0, S.mask[z0 & 1], lane);
         for (uint32_t k = z0; k <= kend; ++k) {
             const int cur = k & 1, prv = cur ^ 1;
             const int lp = EMIT ? cur : 0;                 // list slot of this plane
             const bool have_plane = k < g.cells.z;
             uint32_t L = 0;
-            if (have_plane) {
-                if (EMIT) {
-                    for (uint32_t r = lane; r < HROWS; r += 32) {
-                        const uint32_t yy = y0 + r;
-                        uint2 own = make_uint2(0, 0), nxt = make_uint2(0, 0);
-                        if (yy < g.cells.y) {
-                            own = out.seg_off[seg_index(g, k, yy, xs)];
-                            if (xs + 1 < g.nxs) nxt = out.seg_off[seg_index(g, k, yy, xs + 1)];
+            if constexpr (EMIT) {
+                if (have_plane) {
+                    L = load_slot_list<T>(cells, g, k, xs, yb, cur, lane, S, M, vol, k < z1);
+                    // the segment offsets of the rows (read only where cells are)
+                    if (L)
+                        for (uint32_t r = lane; r < HROWS; r += 32) {
+                            const uint32_t yy = y0 + r;
+                            uint2 own = make_uint2(0, 0), nxt = make_uint2(0, 0);
+                            if (yy < g.cells.y) {
+                                own = out.seg_off[seg_index(g, k, yy, xs)];
+                                if (xs + 1 < g.nxs) nxt = out.seg_off[seg_index(g, k, yy, xs + 1)];
+                            }
+                            S.segv[cur][r][0] = own.x; S.segv[cur][r][1] = nxt.x; S.segq[cur][r] = own.y;
                         }
-                        S.segv[cur][r][0] = own.x; S.segv[cur][r][1] = nxt.x; S.segq[cur][r] = own.y;
-                    }
-                    if (!wait_slot((k + 1) & 1)) return;
-                } else {
-                    // (a plane-limited count also keeps its last plane: the emit
-                    // sweep of the shard below reads it)
-                    const bool keep = k + 1 < z1 || z1 == g.cells.z || k + 1 >= range.zlim;
-                    load_plane<T>(vol, g.pts, g.iso, g.iso_u16, g.isole_u16, x0, y0, k + 1, S.mask[(k + 1) & 1], lane,
-                                  keep ? mask_chunk(masks, g, xs, yb, k + 1) : nullptr, ncolr);
                 }
+            } else {
+                const uint64_t rowmask = ((1ull << min((uint32_t)ROWS, g.cells.y - y0)) - 1ull);
+                load_plane<T>(vol, g.pts, g.iso, g.iso_u16, g.isole_u16, x0, y0, k + 1, S.mask[(k + 1) & 1], lane);
                 __syncwarp();
                 const uint64_t *mk = S.mask[cur].lt, *mk1 = S.mask[(k + 1) & 1].lt;
                 uint64_t act[GROUPS];
@@ -830,79 +876,47 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 3) brick_sweep(cons
                     const int c = lane + 32 * j;
                     act[j] = (x0 + c < g.cells.x) ? active_rows(mk[c], mk[c + 1], mk1[c], mk1[c + 1]) & rowmask : 0ull;
                 }
-                uint64_t hact = 0;
-                if (EMIT && lane == 0 && x0 + W < g.cells.x) hact = active_rows(mk[W], mk[W + 1], mk1[W], mk1[W + 1]) & rowmask;
-                // emit sweep: a plane without active cells (common on sparse
-                // surfaces) skips the transposes, the scan and the list (in
-                // the count sweep the extra branch cost more than it saved)
-                const bool any_act = !EMIT || __any_sync(0xffffffffu, (act[0] | act[1] | act[2] | act[3] | hact) != 0ull);
-                if (!any_act) {
-                    *reinterpret_cast<uint4 *>(S.xrow[cur][lane]) = make_uint4(0u, 0u, 0u, 0u);
-                    S.rowstart[cur][lane] = 0;
-                    if (lane == 0) {
-                        if (EMIT) *reinterpret_cast<uint4 *>(S.xrow[cur][32]) = make_uint4(0u, 0u, 0u, 0u);
-                        S.rowstart[cur][32] = 0;
-                        S.rowstart[cur][33] = 0;
-                        S.hact[cur] = 0;
-                    }
-                } else {
-                    // bit transpose: lane r gets row r's active cells in x order
-                    uint32_t xr[GROUPS], x32[GROUPS];
-                    uint32_t cnt = 0, cnt32 = 0;
-    #pragma unroll
+                // bit transpose: lane r gets row r's active cells in x order
+                uint32_t xr[GROUPS];
+                uint32_t cnt = 0;
+#pragma unroll
+                for (int j = 0; j < GROUPS; ++j) {
+                    xr[j] = warp_transpose32((uint32_t)act[j], lane);
+                    cnt += __popc(xr[j]);
+                }
+                const uint32_t inc = warp_incl_scan(cnt, lane);
+                L = __shfl_sync(0xffffffffu, inc, 31);
+                const uint32_t start = inc - cnt;
+                S.rowstart[cur][lane] = (uint16_t)start;
+                if (lane == 0) { S.rowstart[cur][32] = (uint16_t)L; S.rowstart[cur][33] = (uint16_t)L; }
+                // the slot header for the emit sweep: row starts, and the rows
+                // whose first cell (column 0) is active
+                const uint32_t col0 = __ballot_sync(0xffffffffu, xr[0] & 1u);
+                {
+                    uint32_t *h = slot_hdr(cells, g, cell_slot(g, k, yb, xs));
+                    const uint32_t lo = __shfl_sync(0xffffffffu, start, (2 * lane) & 31);
+                    const uint32_t hi = __shfl_sync(0xffffffffu, start, (2 * lane + 1) & 31);
+                    if (lane < 16) h[lane] = lo | (hi << 16);
+                    if (lane == 16) { h[16] = L | (L << 16); h[17] = col0; }
+                }
+                // lane r lists row r in x order
+                {
+                    uint32_t pos = start;
+#pragma unroll
                     for (int j = 0; j < GROUPS; ++j) {
-                        xr[j] = warp_transpose32((uint32_t)act[j], lane);
-                        cnt += __popc(xr[j]);
-                        x32[j] = EMIT ? __ballot_sync(0xffffffffu, (act[j] >> 32) & 1ull) : 0u;
-                        cnt32 += __popc(x32[j]);
-                    }
-                    if (EMIT) {
-                        hact = __shfl_sync(0xffffffffu, hact, 0);
-                        cnt += (uint32_t)((hact >> lane) & 1ull);
-                        cnt32 += (uint32_t)((hact >> 32) & 1ull);
-                    }
-                    *reinterpret_cast<uint4 *>(S.xrow[cur][lane]) = make_uint4(xr[0], xr[1], xr[2], xr[3]);
-                    if (EMIT && lane == 0) *reinterpret_cast<uint4 *>(S.xrow[cur][32]) = make_uint4(x32[0], x32[1], x32[2], x32[3]);
-                    const uint32_t inc = warp_incl_scan(cnt, lane);
-                    const uint32_t tot32 = __shfl_sync(0xffffffffu, inc, 31);
-                    const uint32_t start = inc - cnt;
-                    S.rowstart[cur][lane] = (uint16_t)start;
-                    if (lane == 0) { S.rowstart[cur][32] = (uint16_t)tot32; S.rowstart[cur][33] = (uint16_t)(tot32 + cnt32); S.hact[cur] = hact; }
-                    L = tot32 + cnt32;
-                    // lane r lists row r in x order (lane 0 also row 32)
-                    {
-                        uint32_t pos = start;
-    #pragma unroll
-                        for (int j = 0; j < GROUPS; ++j) {
-                            uint32_t w = xr[j];
-                            while (w) {
-                                const int l = __ffs(w) - 1;
-                                w &= w - 1;
-                                M.set_lst(lp, pos++, (lane << 8) | (32 * j + l));
-                            }
-                        }
-                        if (EMIT && ((hact >> lane) & 1ull)) M.set_lst(lp, pos++, (lane << 8) | W);
-                        if (EMIT && lane == 0) {
-                            pos = tot32;
-    #pragma unroll
-                            for (int j = 0; j < GROUPS; ++j) {
-                                uint32_t w = x32[j];
-                                while (w) {
-                                    const int l = __ffs(w) - 1;
-                                    w &= w - 1;
-                                    M.set_lst(lp, pos++, (32 << 8) | (32 * j + l));
-                                }
-                            }
-                            if ((hact >> 32) & 1ull) M.set_lst(lp, pos++, (32 << 8) | W);
+                        uint32_t w = xr[j];
+                        while (w) {
+                            const int l = __ffs(w) - 1;
+                            w &= w - 1;
+                            M.set_lst(lp, pos++, (lane << 8) | (32 * j + l));
                         }
                     }
                 }
                 __syncwarp();
             }
             // ranked active cells, 32 at a time
-            const uint64_t *mk = S.mask[cur].lt, *mk1 = S.mask[(k + 1) & 1].lt;
-            const uint64_t *ek = S.mask[cur].le, *ek1 = S.mask[(k + 1) & 1].le;
             uint32_t run = 0;
+            uint32_t *const recs = EMIT ? nullptr : slot_rec(cells, g, cell_slot(g, k, yb, xs));
             for (uint32_t base = 0; base < L; base += 32) {
                 const uint32_t i = base + lane;
                 const bool valid = i < L;
@@ -916,22 +930,31 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 3) brick_sweep(cons
                     r = e >> 8; c = e & 0xff;
                     x = x0 + c; y = y0 + r;
                     own = r < ROWS && c < W;
-                    cfg = cfg_from_masks(mk[c], mk[c + 1], mk1[c], mk1[c + 1], r);
-                    if (EMIT && own && k < z1) load_cell(vol, g, x, y, k, v, true);
-                    l2 = needs_lut2(vol, g, tab, cfg, mk, mk1, c, r, x, y, k);
-                    info = info_from_bits(cfg, le4_from_masks(ek[c + 1], ek1[c], ek1[c + 1], r));
+                    if constexpr (EMIT) {
+                        // classified by the count sweep: the cell's record
+                        const uint32_t rec = M.ent(lp, i);
+                        cfg = rec_cfg(rec); l2 = rec_l2(rec); info = rec_info(rec);
+                        if (own && k < z1) load_cell(vol, g, x, y, k, v, true);
+                    } else {
+                        const uint64_t *mk = S.mask[cur].lt, *mk1 = S.mask[(k + 1) & 1].lt;
+                        const uint64_t *ek = S.mask[cur].le, *ek1 = S.mask[(k + 1) & 1].le;
+                        cfg = cfg_from_masks(mk[c], mk[c + 1], mk1[c], mk1[c + 1], r);
+                        l2 = needs_lut2(vol, g, tab, cfg, mk, mk1, c, r, x, y, k);
+                        info = info_from_bits(cfg, le4_from_masks(ek[c + 1], ek1[c], ek1[c + 1], r));
+                        recs[i] = rec_pack((uint32_t)c, (uint32_t)r, cfg, l2, info);
+                        n_l2 += l2;
+                    }
                     nv = nvert_of(tab, cfg, l2) + __popc(info & 7u);
                     uint32_t nq = 0;
                     if (own) nq = quad_count(info, cfg, x, y, k, g.cells, n_drop);
                     packed = nv | (nq << 16);
-                    n_l2 += l2;
                 }
                 const uint32_t incl = warp_incl_scan(packed, lane);
                 const uint32_t ex = run + incl - packed;
                 run += __shfl_sync(0xffffffffu, incl, 31);
                 if (valid && i == S.rowstart[cur][r]) S.rowbase[r] = ex;
                 __syncwarp();
-                if (!EMIT) {
+                if constexpr (!EMIT) {
                     if (valid && i + 1 == S.rowstart[cur][r + 1]) S.rowtot[r] = ex + packed - S.rowbase[r];
                 } else if (valid) {
                     const uint32_t rb = S.rowbase[r];
@@ -955,12 +978,7 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 3) brick_sweep(cons
                 }
                 __syncwarp();
             }
-            // plane k's masks are done with: its slot takes plane k+2
-            if (EMIT && k + 1 < g.cells.z && k + 1 <= kend) {
-                fetch_masks(masks, g, xs, yb, x0, k + 2, S.mask[cur], &S.mbar[cur], lane);
-                pend |= 1u << cur;
-            }
-            if (!EMIT) {
+            if constexpr (!EMIT) {
                 if (y0 + lane < g.cells.y) {
                     const uint32_t t = S.rowstart[cur][lane] == S.rowstart[cur][lane + 1] ? 0u : S.rowtot[lane];
                     seg_cnt[seg_index(g, k, y0 + lane, xs)] = make_uint2(t & 0xffffu, t >> 16);
@@ -970,7 +988,7 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 3) brick_sweep(cons
             // quads of own cells of plane k-1: their +z ring cells are in plane
             // k.  Owners are taken 32 at a time; their quads are compacted into
             // qwork and written one per lane.
-            if (EMIT && k > z0) {
+            if constexpr (EMIT) if (k > z0) {
                 const uint32_t kp = k - 1;
                 const uint32_t Lp = S.rowstart[prv][HROWS];
                 for (uint32_t base = 0; base < Lp; base += 32) {
@@ -1068,7 +1086,7 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), EMIT ? 2 : 3) brick_sweep(cons
             __syncwarp();
         }
     }
-    if (!EMIT && !(range.flags & kNoStats)) {
+    if constexpr (!EMIT) if (!(range.flags & kNoStats)) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             n_l2 += __shfl_xor_sync(0xffffffffu, n_l2, o);
@@ -1189,13 +1207,13 @@ bool brick_supports(const ExtractArgs &a)
     return a.cells.x >= 1 && a.cells.y >= 1 && a.cells.z >= 1;
 }
 
-constexpr size_t kEmitSmem = brick::kTablesBytes + sizeof(brick::WarpSmem) * brick::NWB_EMIT;
-constexpr size_t kCountSmem = brick::kTablesBytes + sizeof(brick::SweepSmem) * brick::NWB_COUNT;
+constexpr size_t kEmitSmem = brick::kTablesBytes + sizeof(brick::EmitSmem) * brick::NWB_EMIT;
+constexpr size_t kCountSmem = brick::kTablesBytes + sizeof(brick::CountSmem) * brick::NWB_COUNT;
 // two emit blocks and three count blocks per SM (228 KB of shared memory,
 // 1 KB of it reserved per block); what is left of the 256 KB is L1, which the
 // emit sweep's corner gathers use: 12 KB more shared memory per emit block
 // made it 4% slower
-static_assert(2 * (kEmitSmem + 1024) <= 228 * 1024, "emit sweep: two blocks per SM must fit");
+static_assert(3 * (kEmitSmem + 1024) <= 228 * 1024, "emit sweep: three blocks per SM must fit");
 static_assert(3 * (kCountSmem + 1024) <= 228 * 1024, "count sweep: three blocks per SM must fit");
 
 template <class T, bool EMIT>
@@ -1221,24 +1239,14 @@ static void iso_thresholds(float f, uint32_t &lt, uint32_t &le)
     else le = (uint32_t)f + 1;
 }
 
-// Mask store of one volume: for every point plane and row of tiles, the lt
-// and le words of each tile's columns (130 per tile; the last tile holds the
-// columns left in the volume, rounded up to even so that every chunk starts
-// and ends on a 16-byte boundary).
-static uint32_t mask_row_words(const BrickItem &it)
-{
-    using namespace brick;
-    const uint32_t nxs = (it.cells.x + W - 1) / W;
-    if (nxs == 0) return 0;
-    const uint32_t last = std::min<uint32_t>(W + 2, (it.pts.x - (nxs - 1) * W + 1) & ~1u);
-    return (W + 2) * (nxs - 1) + last;
-}
-static uint64_t mask_words(const BrickItem &it)
+// Cell store of one volume: a header and a record area per slot (cell plane
+// of a brick), 4 bytes per cell of its bricks plus 80 bytes per slot.
+static uint64_t cell_words(const BrickItem &it)
 {
     using namespace brick;
     if (it.cells.x == 0 || it.cells.y == 0 || it.cells.z == 0) return 0;
-    const uint64_t nyb = (it.cells.y + ROWS - 1) / ROWS;
-    return (uint64_t)it.pts.z * nyb * 2ull * mask_row_words(it);
+    const uint64_t nslots = (uint64_t)it.cells.z * ((it.cells.y + ROWS - 1) / ROWS) * ((it.cells.x + W - 1) / W);
+    return nslots * (kHdrWords + kRecWords);
 }
 
 // Per-context pipeline state.  Scratch (device) and staging (pinned host) are
@@ -1248,7 +1256,7 @@ static uint64_t mask_words(const BrickItem &it)
 struct BatchState {
     // capacities of the layout
     uint32_t cap_items = 0;
-    uint64_t cap_seg = 0, cap_coord = 0, cap_mask = 0;
+    uint64_t cap_seg = 0, cap_coord = 0, cap_cell = 0;
     uint64_t layout_gen = 0;           // scratch_gen the layout was carved for (0: none)
     uint64_t layout_id = 0;            // bumped on every re-carve: captured graphs hold the addresses
     // device layout (inside ctx->scratch)
@@ -1256,7 +1264,7 @@ struct BatchState {
     uint2 *seg_cnt = nullptr, *seg_off = nullptr;
     TileState *tiles = nullptr;
     brick::Spill *spill = nullptr;
-    uint64_t *masks = nullptr;          // mask store, cap_mask words
+    uint32_t *cells = nullptr;          // cell store, cap_cell words
     float *coord = nullptr;
     dmc_batch_result *d_res = nullptr;
     uint32_t *tickets = nullptr;
@@ -1346,17 +1354,17 @@ static dmc_status batch_state(Ctx *ctx, BatchState **out)
 }
 
 // Carves the scratch and staging for at least the given capacities.
-static dmc_status batch_layout(Ctx *ctx, BatchState &b, uint32_t items, uint64_t seg, uint64_t ncoord, uint64_t nmask)
+static dmc_status batch_layout(Ctx *ctx, BatchState &b, uint32_t items, uint64_t seg, uint64_t ncoord, uint64_t ncell)
 {
     using namespace brick;
     const bool fits = b.layout_gen == ctx->scratch_gen && items <= b.cap_items && seg <= b.cap_seg &&
-                      ncoord <= b.cap_coord && nmask <= b.cap_mask;
+                      ncoord <= b.cap_coord && ncell <= b.cap_cell;
     if (fits) return DMC_OK;
     // grow with headroom so that a stream of similar batches settles on one layout
     b.cap_items = std::max<uint32_t>(b.cap_items, items + items / 4 + 1);
     b.cap_seg = std::max<uint64_t>(b.cap_seg, seg + seg / 4 + SCAN_TILE);
     b.cap_coord = std::max<uint64_t>(b.cap_coord, ncoord + ncoord / 4 + 64);
-    b.cap_mask = std::max<uint64_t>(b.cap_mask, nmask + nmask / 4 + 64);
+    b.cap_cell = std::max<uint64_t>(b.cap_cell, ncell + ncell / 4 + 64);
     const uint64_t cap_tiles = (b.cap_seg + SCAN_TILE - 1) / SCAN_TILE;
     b.plan_bytes = sizeof(BatchHead) + sizeof(Geom) * (size_t)b.cap_items;
     size_t off = 0;
@@ -1365,7 +1373,7 @@ static dmc_status batch_layout(Ctx *ctx, BatchState &b, uint32_t items, uint64_t
     const size_t o_cnt = carve(8 * b.cap_seg), o_off = carve(8 * b.cap_seg);
     const size_t o_tiles = carve(sizeof(TileState) * (cap_tiles + kMaxSlabs));   // slabs: one partial tile each
     const size_t o_spill = carve(sizeof(Spill) * (size_t)sweep_warps(b));
-    const size_t o_mask = carve(8 * b.cap_mask);
+    const size_t o_cell = carve(4 * b.cap_cell);
     const size_t o_coord = carve(4 * b.cap_coord);
     const size_t o_res = carve(sizeof(dmc_batch_result) * (size_t)b.cap_items);
     const size_t o_tk = carve(4 * kTickets);
@@ -1378,7 +1386,7 @@ static dmc_status batch_layout(Ctx *ctx, BatchState &b, uint32_t items, uint64_t
     b.seg_off = (uint2 *)(base + o_off);
     b.tiles = (TileState *)(base + o_tiles);
     b.spill = (Spill *)(base + o_spill);
-    b.masks = (uint64_t *)(base + o_mask);
+    b.cells = (uint32_t *)(base + o_cell);
     b.coord = (float *)(base + o_coord);
     b.d_res = (dmc_batch_result *)(base + o_res);
     b.tickets = (uint32_t *)(base + o_tk);
@@ -1426,12 +1434,12 @@ static dmc_status enqueue_front(Ctx *ctx, BatchState &b, dmc_batch_result *d_res
     if (timed) CUDA_TRY(cudaEventRecord(ctx->evk[0], st));
     if (all || nb[0]) {
         brick_sweep<float, false><<<sweep_blocks(b, 0, false, nb[0], all), 32 * NWB_COUNT, kCountSmem, st>>>(
-            b.d_plan, 0, BrickRange{0, kAllBricks}, ctx->d_tab, b.seg_cnt, EmitOut{}, b.spill, b.masks, &b.tickets[0], ctx->d_ctl->counters, &ctx->d_ctl->err);
+            b.d_plan, 0, BrickRange{0, kAllBricks}, ctx->d_tab, b.seg_cnt, EmitOut{}, b.spill, b.cells, &b.tickets[0], ctx->d_ctl->counters, &ctx->d_ctl->err);
         CUDA_TRY(cudaGetLastError());
     }
     if (all || nb[1]) {
         brick_sweep<uint16_t, false><<<sweep_blocks(b, 1, false, nb[1], all), 32 * NWB_COUNT, kCountSmem, st>>>(
-            b.d_plan, 1, BrickRange{0, kAllBricks}, ctx->d_tab, b.seg_cnt, EmitOut{}, b.spill, b.masks, &b.tickets[1], ctx->d_ctl->counters, &ctx->d_ctl->err);
+            b.d_plan, 1, BrickRange{0, kAllBricks}, ctx->d_tab, b.seg_cnt, EmitOut{}, b.spill, b.cells, &b.tickets[1], ctx->d_ctl->counters, &ctx->d_ctl->err);
         CUDA_TRY(cudaGetLastError());
     }
     if (timed) CUDA_TRY(cudaEventRecord(ctx->evk[1], st));
@@ -1457,12 +1465,12 @@ static dmc_status enqueue_back(Ctx *ctx, BatchState &b, const brick::EmitOut &eo
     if (timed) CUDA_TRY(cudaEventRecord(ctx->evk[3], st));
     if (all || nb[0]) {
         brick_sweep<float, true><<<sweep_blocks(b, 0, true, nb[0], all), 32 * NWB_EMIT, kEmitSmem, st>>>(
-            b.d_plan, 0, BrickRange{0, kAllBricks}, ctx->d_tab, nullptr, eo, b.spill, b.masks, &b.tickets[2], ctx->d_ctl->counters, &ctx->d_ctl->err);
+            b.d_plan, 0, BrickRange{0, kAllBricks}, ctx->d_tab, nullptr, eo, b.spill, b.cells, &b.tickets[2], ctx->d_ctl->counters, &ctx->d_ctl->err);
         CUDA_TRY(cudaGetLastError());
     }
     if (all || nb[1]) {
         brick_sweep<uint16_t, true><<<sweep_blocks(b, 1, true, nb[1], all), 32 * NWB_EMIT, kEmitSmem, st>>>(
-            b.d_plan, 1, BrickRange{0, kAllBricks}, ctx->d_tab, nullptr, eo, b.spill, b.masks, &b.tickets[3], ctx->d_ctl->counters, &ctx->d_ctl->err);
+            b.d_plan, 1, BrickRange{0, kAllBricks}, ctx->d_tab, nullptr, eo, b.spill, b.cells, &b.tickets[3], ctx->d_ctl->counters, &ctx->d_ctl->err);
         CUDA_TRY(cudaGetLastError());
     }
     if (timed) CUDA_TRY(cudaEventRecord(ctx->evk[4], st));
@@ -1587,11 +1595,11 @@ static dmc_status retarget_graph(Ctx *ctx, BatchState &b, const brick::EmitOut &
         uint2 *a_cnt = nullptr;
         EmitOut a_out = eo;
         Spill *a_spill = b.spill;
-        uint64_t *a_masks = b.masks;
+        uint32_t *a_cells = b.cells;
         uint32_t *a_ticket = &b.tickets[2 + g];
         unsigned long long *a_counters = ctx->d_ctl->counters;
         uint32_t *a_err = &ctx->d_ctl->err;
-        void *args[] = {&a_head, &a_group, &a_range, &a_tab, &a_cnt, &a_out, &a_spill, &a_masks, &a_ticket, &a_counters, &a_err};
+        void *args[] = {&a_head, &a_group, &a_range, &a_tab, &a_cnt, &a_out, &a_spill, &a_cells, &a_ticket, &a_counters, &a_err};
         cudaKernelNodeParams kp = b.emit_params[g];
         kp.kernelParams = args;
         kp.extra = nullptr;
@@ -1634,24 +1642,24 @@ static dmc_status stage_plan(Ctx *ctx, BatchState &b, const BrickItem *items, ui
     using namespace brick;
     const uint32_t zc = zc_force ? zc_force : pick_zc(ctx, b, items, n);
     // descriptors: the f32 volumes, then the u16 ones (one launch per type)
-    uint64_t nseg = 0, ncoord = 0, nmask = 0;
+    uint64_t nseg = 0, ncoord = 0, ncell = 0;
     nb[0] = nb[1] = 0;
     uint32_t nvol[2] = {0, 0};
     for (uint32_t i = 0; i < n; ++i) {
         const BrickItem &it = items[i];
         nseg += (uint64_t)it.cells.z * it.cells.y * ((it.cells.x + W - 1) / W);
         ncoord += (uint64_t)it.pts.x + it.pts.y + it.pts.z;
-        nmask += mask_words(it);
+        ncell += cell_words(it);
         nvol[it.dtype == DMC_F32 ? 0 : 1]++;
     }
     const uint64_t n_tiles = (nseg + SCAN_TILE - 1) / SCAN_TILE;
     if (n_tiles >= (1ull << 31)) return DMC_ERR_UNSUPPORTED;
-    dmc_status s = batch_layout(ctx, b, n, nseg, ncoord, nmask);
+    dmc_status s = batch_layout(ctx, b, n, nseg, ncoord, ncell);
     if (s != DMC_OK) return s;
     BatchHead *head = (BatchHead *)b.h_stage;
     Geom *geoms = (Geom *)(head + 1);
     uint32_t pos[2] = {0, nvol[0]};
-    uint64_t seg_base = 0, coord_base = 0, mask_base = 0;
+    uint64_t seg_base = 0, coord_base = 0, cell_base = 0;
     for (uint32_t i = 0; i < n; ++i) {
         const BrickItem &it = items[i];
         const int grp = it.dtype == DMC_F32 ? 0 : 1;
@@ -1669,9 +1677,8 @@ static dmc_status stage_plan(Ctx *ctx, BatchState &b, const BrickItem *items, ui
         g.nseg = (uint64_t)it.cells.z * it.cells.y * g.nxs;
         seg_base += g.nseg;
         g.coord = b.coord + coord_base;
-        g.mask_tw = mask_row_words(it);
-        g.mask_base = mask_base;
-        mask_base += mask_words(it);
+        g.cell_base = cell_base;
+        cell_base += cell_words(it);
         coord_base += (uint64_t)it.pts.x + it.pts.y + it.pts.z;
         g.item = i;
     }
@@ -1780,10 +1787,10 @@ static void launch_sweep(Ctx *ctx, BatchState &b, bool emit, brick::BrickRange r
     const uint32_t grp = std::is_same<T, float>::value ? 0 : 1;
     if (emit)
         brick_sweep<T, true><<<sweep_blocks(b, grp, true, r.cnt, false), 32 * NWB_EMIT, kEmitSmem, st>>>(
-            b.d_plan, grp, r, ctx->d_tab, nullptr, eo, b.spill, b.masks, ticket, ctx->d_ctl->counters, &ctx->d_ctl->err);
+            b.d_plan, grp, r, ctx->d_tab, nullptr, eo, b.spill, b.cells, ticket, ctx->d_ctl->counters, &ctx->d_ctl->err);
     else
         brick_sweep<T, false><<<sweep_blocks(b, grp, false, r.cnt, false), 32 * NWB_COUNT, kCountSmem, st>>>(
-            b.d_plan, grp, r, ctx->d_tab, b.seg_cnt, EmitOut{}, b.spill, b.masks, ticket, ctx->d_ctl->counters, &ctx->d_ctl->err);
+            b.d_plan, grp, r, ctx->d_tab, b.seg_cnt, EmitOut{}, b.spill, b.cells, ticket, ctx->d_ctl->counters, &ctx->d_ctl->err);
 }
 
 // Host volume to host mesh in z slabs, so that the upload of later slabs,
