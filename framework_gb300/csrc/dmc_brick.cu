@@ -77,7 +77,6 @@ struct Geom {
 
 struct alignas(16) PlaneMasks {
     uint64_t lt[W + 2];                // bit r: sample (x0+c, y0+r) < iso
-    uint64_t le[W + 2];                // bit r: sample <= iso
 };
 
 // Cell store (global scratch).  For every cell plane of every brick (a
@@ -257,13 +256,14 @@ __device__ __forceinline__ uint32_t le_u16x2(uint32_t v, uint32_t m, uint32_t mh
 // active).  Loads go out 8 rows per lane before their results are used; the
 // next plane is not prefetched into L2 (all resident warps' planes together
 // outrun the L2, and prefetched lines were evicted before their use, which
-// read the volume 1.9 times instead of 1.35).
+// read the volume 1.9 times instead of 1.35).  Only "below" is kept: where a
+// sample equals the isovalue the active cells' corners are tested one by one
+// (corner_eq4).
 template <class T>
-__device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint32_t thr, uint32_t thr_le, uint32_t x0,
+__device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint32_t thr, uint32_t x0,
                                         uint32_t y0, uint32_t p, PlaneMasks &m, int lane)
 {
     uint32_t lo[GROUPS] = {0, 0, 0, 0}, hi[GROUPS] = {0, 0, 0, 0};
-    uint32_t elo[GROUPS] = {0, 0, 0, 0}, ehi[GROUPS] = {0, 0, 0, 0};
     const bool pz = p < pts.z;
     const uint32_t nrow = pz ? min(34u, pts.y - y0) : 0u;
     const uint64_t sx = pts.x;
@@ -273,7 +273,7 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
     // batched path (8 rows of loads in flight) whatever its position.
     const uint32_t rmask = nrow >= 32 ? 0xffffffffu : ((1u << nrow) - 1u);
     const uint32_t hmask = nrow > 32 ? ((1u << (nrow - 32)) - 1u) : 0u;
-    uint32_t rmask_lt = rmask, hmask_lt = hmask, rmask_le = rmask, hmask_le = hmask;
+    uint32_t rmask_lt = rmask, hmask_lt = hmask;
     // All 128 columns in range and rows aligned for 4-sample loads
     // (warp-uniform): lane l takes the adjacent columns 4l..4l+3 of a row in
     // one load.  Otherwise lane l takes columns l, l+32, l+64, l+96.
@@ -288,14 +288,13 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
             // result bits (15 and 31) enter the accumulators from the top,
             // which shift right by one per row: after 16 rows, row j of the
             // half sits at bit j (even column) and 16+j (odd column).
-            const uint32_t m_lt = (thr - 1u) & 0xffffu, m_le = (thr_le - 1u) & 0xffffu;
-            const uint32_t M_lt = m_lt * 0x10001u, M_le = m_le * 0x10001u;
-            const uint32_t MH_lt = M_lt | 0x80008000u, MH_le = M_le | 0x80008000u;
+            const uint32_t m_lt = (thr - 1u) & 0xffffu;
+            const uint32_t M_lt = m_lt * 0x10001u;
+            const uint32_t MH_lt = M_lt | 0x80008000u;
             if (thr == 0) rmask_lt = hmask_lt = 0;
-            if (thr_le == 0) rmask_le = hmask_le = 0;
 #pragma unroll 1
             for (uint32_t h = 0; h < 2; ++h) {
-                uint32_t ax = 0, ay = 0, bx = 0, by = 0;   // lt of columns (0,1) and (2,3); le of the same
+                uint32_t ax = 0, ay = 0;   // columns (0,1) and (2,3)
 #pragma unroll
                 for (uint32_t r0 = 0; r0 < 16; r0 += 8) {
                     V v[8];
@@ -308,27 +307,20 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
                     for (int i = 0; i < 8; ++i) {
                         ax = (ax >> 1) | (le_u16x2(v[i].x, M_lt, MH_lt) & 0x80008000u);
                         ay = (ay >> 1) | (le_u16x2(v[i].y, M_lt, MH_lt) & 0x80008000u);
-                        bx = (bx >> 1) | (le_u16x2(v[i].x, M_le, MH_le) & 0x80008000u);
-                        by = (by >> 1) | (le_u16x2(v[i].y, M_le, MH_le) & 0x80008000u);
                     }
                 }
                 const uint32_t sh = 16 * h;
                 lo[0] |= (ax & 0xffffu) << sh; lo[1] |= (ax >> 16) << sh;
                 lo[2] |= (ay & 0xffffu) << sh; lo[3] |= (ay >> 16) << sh;
-                elo[0] |= (bx & 0xffffu) << sh; elo[1] |= (bx >> 16) << sh;
-                elo[2] |= (by & 0xffffu) << sh; elo[3] |= (by >> 16) << sh;
             }
-            uint32_t ax = 0, ay = 0, bx = 0, by = 0;      // rows 32, 33 end at bits 14, 15 (30, 31)
+            uint32_t ax = 0, ay = 0;      // rows 32, 33 end at bits 14, 15 (30, 31)
 #pragma unroll
             for (int i = 0; i < 2; ++i) {
                 const V v = 32u + i < nrow ? load4(vb + (uint64_t)(32 + i) * sx) : V{};
                 ax = (ax >> 1) | (le_u16x2(v.x, M_lt, MH_lt) & 0x80008000u);
                 ay = (ay >> 1) | (le_u16x2(v.y, M_lt, MH_lt) & 0x80008000u);
-                bx = (bx >> 1) | (le_u16x2(v.x, M_le, MH_le) & 0x80008000u);
-                by = (by >> 1) | (le_u16x2(v.y, M_le, MH_le) & 0x80008000u);
             }
             hi[0] = (ax >> 14) & 3u; hi[1] = ax >> 30; hi[2] = (ay >> 14) & 3u; hi[3] = ay >> 30;
-            ehi[0] = (bx >> 14) & 3u; ehi[1] = bx >> 30; ehi[2] = (by >> 14) & 3u; ehi[3] = by >> 30;
         } else {
 #pragma unroll 1
             for (uint32_t r0 = 0; r0 < 32; r0 += 8) {
@@ -338,30 +330,20 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
 #pragma unroll
                 for (int i = 0; i < 8; ++i)
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const T t = elem4(v[i], q);
-                        lo[q] |= below(t, iso, thr) << (r0 + i);
-                        elo[q] |= at_or_below(t, iso, thr_le) << (r0 + i);
-                    }
+                    for (int q = 0; q < 4; ++q) lo[q] |= below(elem4(v[i], q), iso, thr) << (r0 + i);
             }
 #pragma unroll
             for (int i = 0; i < 2; ++i) {
                 const V v = 32u + i < nrow ? load4(vb + (uint64_t)(32 + i) * sx) : V{};
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const T t = elem4(v, q);
-                    hi[q] |= below(t, iso, thr) << i;
-                    ehi[q] |= at_or_below(t, iso, thr_le) << i;
-                }
+                for (int q = 0; q < 4; ++q) hi[q] |= below(elem4(v, q), iso, thr) << i;
             }
         }
-        // columns 4l..4l+3: two 16-byte stores per mask
+        // columns 4l..4l+3: two 16-byte stores
         const uint4 t0 = make_uint4(lo[0] & rmask_lt, hi[0] & hmask_lt, lo[1] & rmask_lt, hi[1] & hmask_lt);
         const uint4 t1 = make_uint4(lo[2] & rmask_lt, hi[2] & hmask_lt, lo[3] & rmask_lt, hi[3] & hmask_lt);
-        const uint4 e0 = make_uint4(elo[0] & rmask_le, ehi[0] & hmask_le, elo[1] & rmask_le, ehi[1] & hmask_le);
-        const uint4 e1 = make_uint4(elo[2] & rmask_le, ehi[2] & hmask_le, elo[3] & rmask_le, ehi[3] & hmask_le);
-        uint4 *lt4 = reinterpret_cast<uint4 *>(&m.lt[4 * lane]), *le4 = reinterpret_cast<uint4 *>(&m.le[4 * lane]);
-        lt4[0] = t0; lt4[1] = t1; le4[0] = e0; le4[1] = e1;
+        uint4 *lt4 = reinterpret_cast<uint4 *>(&m.lt[4 * lane]);
+        lt4[0] = t0; lt4[1] = t1;
     } else {
         const T *base = vol + (plane0 + y0) * sx + x0 + lane;
         bool cok[GROUPS];
@@ -379,10 +361,7 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
 #pragma unroll
             for (int i = 0; i < 8; ++i)
 #pragma unroll
-                for (int j = 0; j < GROUPS; ++j) {
-                    lo[j] |= below(v[i][j], iso, thr) << (r0 + i);
-                    elo[j] |= at_or_below(v[i][j], iso, thr_le) << (r0 + i);
-                }
+                for (int j = 0; j < GROUPS; ++j) lo[j] |= below(v[i][j], iso, thr) << (r0 + i);
         }
 #pragma unroll
         for (int i = 0; i < 2; ++i) {
@@ -391,17 +370,12 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
             for (int j = 0; j < GROUPS; ++j) {
                 const T v = (32u + i < nrow && cok[j]) ? raw_load(row + 32 * j) : T(0);
                 hi[j] |= below(v, iso, thr) << i;
-                ehi[j] |= at_or_below(v, iso, thr_le) << i;
             }
         }
 #pragma unroll
         for (int j = 0; j < GROUPS; ++j) {
             const uint32_t cm = cok[j] ? 0xffffffffu : 0u;
-            const uint32_t c = lane + 32 * j;
-            const uint64_t t = (uint64_t)(lo[j] & rmask & cm) | ((uint64_t)(hi[j] & hmask & cm) << 32);
-            const uint64_t e = (uint64_t)(elo[j] & rmask & cm) | ((uint64_t)(ehi[j] & hmask & cm) << 32);
-            m.lt[c] = t;
-            m.le[c] = e;
+            m.lt[lane + 32 * j] = (uint64_t)(lo[j] & rmask & cm) | ((uint64_t)(hi[j] & hmask & cm) << 32);
         }
     }
 #pragma unroll 1
@@ -414,14 +388,23 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
         const float v2 = in2 ? sample_p(vol, pts, x, y2, p) : 0.f;
         const uint32_t l32 = __ballot_sync(0xffffffffu, in1 && v < iso);
         const uint32_t h2 = __ballot_sync(0xffffffffu, in2 && v2 < iso) & 3u;
-        const uint32_t e32 = __ballot_sync(0xffffffffu, in1 && v <= iso);
-        const uint32_t eh2 = __ballot_sync(0xffffffffu, in2 && v2 <= iso) & 3u;
-        if (lane == 0) {
-            const uint64_t t = (uint64_t)l32 | ((uint64_t)h2 << 32), e = (uint64_t)e32 | ((uint64_t)eh2 << 32);
-            m.lt[W + hc] = t;
-            m.le[W + hc] = e;
-        }
+        if (lane == 0) m.lt[W + hc] = (uint64_t)l32 | ((uint64_t)h2 << 32);
     }
+}
+
+// At-the-isovalue bits of corners 2, 5, 6, 7 of cell (x, y, z) (bit 0 corner
+// 2, bit 1 corner 5, bit 2 corner 6, bit 3 corner 7): sample == iso, the
+// cases where "at or below" differs from "below".  Read from the samples
+// (a few active cells per brick plane) instead of keeping a second mask per
+// sample.
+template <class T>
+__device__ __forceinline__ uint32_t corner_eq4(const T *vol, const Geom &g, uint32_t x, uint32_t y, uint32_t z)
+{
+    const uint64_t sy = g.pts.x, sz = (uint64_t)g.pts.x * g.pts.y;
+    const T *p = vol + (uint64_t)z * sz + (uint64_t)y * sy + x;
+    const float s2 = load_sample(p, sy + 1), s5 = load_sample(p, sz + 1);
+    const float s6 = load_sample(p, sz + sy + 1), s7 = load_sample(p, sz + sy);
+    return (s2 == g.iso ? 1u : 0u) | (s5 == g.iso ? 2u : 0u) | (s6 == g.iso ? 4u : 0u) | (s7 == g.iso ? 8u : 0u);
 }
 
 // Reference bipolarity and ccw bits of the cell's own edges (dmc.cu:1199-1216)
@@ -498,6 +481,17 @@ __device__ __forceinline__ bool needs_lut2(const T *vol, const Geom &g, const De
     else
         ncfg = cfg_global(vol, g, (uint32_t)nx, (uint32_t)ny, (uint32_t)nz);
     return tab.amb_face[ncfg] != 0xffu;
+}
+
+// Owned edges (bit s: edge 6, 9, 10) whose quad the cell writes: bipolar by
+// the reference's test, quad inside the volume, sign change in the config.
+__device__ __forceinline__ uint32_t quad_want(uint32_t info, uint32_t cfg, uint32_t x, uint32_t y, uint32_t z, uint3 cells)
+{
+    uint32_t want = 0;
+#pragma unroll
+    for (int s = 0; s < 3; ++s)
+        if ((info & (1u << s)) && owned_quad_in_volume(s, x, y, z, cells) && owned_sign_change(cfg, s)) want |= 1u << s;
+    return want;
 }
 
 __device__ __forceinline__ uint32_t quad_count(uint32_t info, uint32_t cfg, uint32_t x, uint32_t y, uint32_t z,
@@ -671,17 +665,23 @@ __device__ __forceinline__ uint32_t ring_edge(int s, int kk)
     return (uint32_t)((E >> (4 * (4 * s + kk))) & 0xfull);
 }
 
-// Emit sweep: plane k of brick (xs, yb) as a list, read from the cell store.
-// Besides the slot's own cells, the quads need the halo: column W (column 0
-// of the next x brick) and row 32 (row 0 of the next y brick).  List order is
-// output order: rows 0..31, each followed by its column-W cell, then row 32
-// and its column-W cell.  Each entry's record goes to ent[p]; xrow[p], hact[p]
-// and rowstart[p][0..33] index the list.  Returns its length.
+// Emit sweep, plane k of brick (xs, yb), from the cell store: lists the
+// plane's cells in output order, with their packed cell words and own-edge
+// bits, and writes the vertices of its own cells (for k < zv).  Besides the
+// slot's own cells, the quads need the halo: column W (column 0 of the next x
+// brick) and row 32 (row 0 of the next y brick).  List order is rows 0..31,
+// each followed by its column-W cell, then row 32 and its column-W cell;
+// xrow[p], hact[p] and rowstart[p][0..33] index the list, segv[p] / segq[p]
+// hold the rows' segment offsets.  Each record is read and classified once:
+// its counts, its place in its row (a segmented scan: records come row by
+// row) and its vertices are taken in the same pass.  Returns the list length.
 template <class T, class SM>
-__device__ __forceinline__ uint32_t load_slot_list(uint32_t *cells, const Geom &g, uint32_t k, uint32_t xs, uint32_t yb,
-                                                    int p, int lane, SM &S, WarpMem<SM> &M, const T *vol, bool pf)
+__device__ __forceinline__ uint32_t emit_plane(uint32_t *cells, const Geom &g, const T *vol, const DeviceTables &tab,
+                                               const EmitOut &out, uint32_t *err, uint32_t k, uint32_t zv,
+                                               uint32_t xs, uint32_t yb, int p, int lane, SM &S, WarpMem<SM> &M)
 {
     const uint64_t s0 = cell_slot(g, k, yb, xs);
+    const uint32_t x0 = xs * W, y0 = yb * ROWS;
     const bool hx = xs + 1 < g.nxs, hy = yb + 1 < g.nyb;
     const uint32_t *h0 = slot_hdr(cells, g, s0);
     const uint32_t *r0 = slot_rec(cells, g, s0);
@@ -703,6 +703,16 @@ __device__ __forceinline__ uint32_t load_slot_list(uint32_t *cells, const Geom &
         __syncwarp();
         return 0;
     }
+    // segment offsets of the rows
+    for (uint32_t r = lane; r < HROWS; r += 32) {
+        const uint32_t yy = y0 + r;
+        uint2 own = make_uint2(0, 0), nxt = make_uint2(0, 0);
+        if (yy < g.cells.y) {
+            own = out.seg_off[seg_index(g, k, yy, xs)];
+            if (hx) nxt = out.seg_off[seg_index(g, k, yy, xs + 1)];
+        }
+        S.segv[p][r][0] = own.x; S.segv[p][r][1] = nxt.x; S.segq[p][r] = own.y;
+    }
     // halo column (the next x brick's rows with an active column-0 cell) and
     // the corner cell of row 32
     uint32_t col0 = 0, hxrec = 0, n32 = 0, corner = 0, crec = 0;
@@ -723,6 +733,7 @@ __device__ __forceinline__ uint32_t load_slot_list(uint32_t *cells, const Geom &
     const uint32_t L = start32 + n32 + corner;
     S.rowstart[p][lane] = (uint16_t)(st + hcp);
     *reinterpret_cast<uint4 *>(S.xrow[p][lane]) = make_uint4(0u, 0u, 0u, 0u);
+    // column-W cells are the first of their segment (vertex offset 0)
     if (lane == 0) {
         S.rowstart[p][32] = (uint16_t)start32;
         S.rowstart[p][33] = (uint16_t)L;
@@ -730,40 +741,96 @@ __device__ __forceinline__ uint32_t load_slot_list(uint32_t *cells, const Geom &
         *reinterpret_cast<uint4 *>(S.xrow[p][32]) = make_uint4(0u, 0u, 0u, 0u);
         if (corner) {
             M.set_lst(p, start32 + n32, (32u << 8) | W);
-            M.set_ent(p, start32 + n32, crec);
+            M.set_ent(p, start32 + n32, pack_cell(0u, 0u, rec_cfg(crec), rec_l2(crec)));
+            M.set_info(p, start32 + n32, rec_info(crec) & 0x38u);
         }
     }
     if ((col0 >> lane) & 1u) {   // last entry of row lane
         M.set_lst(p, en + hcp, ((uint32_t)lane << 8) | W);
-        M.set_ent(p, en + hcp, hxrec);
+        M.set_ent(p, en + hcp, pack_cell(0u, 0u, rec_cfg(hxrec), rec_l2(hxrec)));
+        M.set_info(p, en + hcp, rec_info(hxrec) & 0x38u);
     }
     __syncwarp();
+    // own cells, 32 at a time; each round's records are read one round ahead
+    // and their corner lines prefetched into L2
+    const uint64_t sy = g.pts.x, sz = (uint64_t)g.pts.x * g.pts.y;
+    auto prefetch = [&](uint32_t w) {
+        const T *q = vol + (uint64_t)k * sz + (uint64_t)(y0 + rec_row(w)) * sy + x0 + rec_col(w);
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(q));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(q + sy));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(q + sz));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(q + sz + sy));
+    };
+    uint32_t run = 0;
+    uint32_t nrec = (uint32_t)lane < lown ? __ldg(r0 + lane) : 0u;
+    if ((uint32_t)lane < lown && k < zv) prefetch(nrec);
     for (uint32_t b = 0; b < lown; b += 32) {
         const uint32_t i = b + lane;
-        const uint32_t rec = i < lown ? __ldg(r0 + i) : 0u;
+        const bool valid = i < lown;
+        const uint32_t rec = nrec;
+        nrec = i + 32 < lown ? __ldg(r0 + i + 32) : 0u;
+        if (i + 32 < lown && k < zv) prefetch(nrec);
         const uint32_t r = rec_row(rec), c = rec_col(rec);
         const uint32_t shift = __shfl_sync(0xffffffffu, hcp, (int)r);
-        if (i < lown) {
-            if (pf) {
-                const uint64_t sy = g.pts.x, sz = (uint64_t)g.pts.x * g.pts.y;
-                const T *q = vol + (uint64_t)k * sz + (uint64_t)(yb * ROWS + r) * sy + xs * W + c;
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(q));
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(q + sy));
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(q + sz));
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(q + sz + sy));
-            }
-            M.set_lst(p, i + shift, (r << 8) | c);
-            M.set_ent(p, i + shift, rec);
-            atomicOr(&S.xrow[p][r][c >> 5], 1u << (c & 31));
+        const uint32_t first = __shfl_sync(0xffffffffu, st, (int)r);
+        const uint32_t cfg = rec_cfg(rec), info = rec_info(rec);
+        const bool l2 = rec_l2(rec);
+        const uint32_t x = x0 + c, y = y0 + r;
+        float v[8];
+        if (valid && k < zv) load_cell(vol, g, x, y, k, v, true);
+        uint32_t packed = 0, want = 0;
+        if (valid) {
+            want = quad_want(info, cfg, x, y, k, g.cells);
+            packed = (nvert_of(tab, cfg, l2) + __popc(info & 7u)) | (__popc(want) << 16);
         }
+        const uint32_t incl = warp_incl_scan(packed, lane);
+        const uint32_t ex = run + incl - packed;
+        run += __shfl_sync(0xffffffffu, incl, 31);
+        if (valid && i == first) S.rowbase[r] = ex;
+        __syncwarp();
+        if (valid) {
+            const uint32_t rb = S.rowbase[r];
+            const uint32_t vrel = (ex & 0xffffu) - (rb & 0xffffu);
+            const uint32_t qrel = (ex >> 16) - (rb >> 16);
+            M.set_lst(p, i + shift, (r << 8) | c);
+            M.set_ent(p, i + shift, pack_cell(vrel, qrel, cfg, l2));
+            M.set_info(p, i + shift, want | (info & 0x38u));   // the quads need only these: wanted edges, ccw bits
+            atomicOr(&S.xrow[p][r][c >> 5], 1u << (c & 31));
+            if (k < zv) {
+                const uint32_t nv = packed & 0xffffu;
+                const uint64_t vb = (uint64_t)S.segv[p][r][0] + vrel;
+                if (vb + nv > out.vcap) {
+                    atomicOr(err, DEV_ERR_OVERFLOW);
+                } else {
+                    Geo geo;
+                    geo.x0 = g.coord[x]; geo.x1 = g.coord[x + 1];
+                    geo.y0 = g.coord[g.pts.x + y]; geo.y1 = g.coord[g.pts.x + y + 1];
+                    geo.z0 = g.coord[g.pts.x + g.pts.y + k]; geo.z1 = g.coord[g.pts.x + g.pts.y + k + 1];
+                    cell_vertices(tab, v, geo, g.iso, cfg, l2, nvert_of(tab, cfg, l2), info, x, y, k,
+                                  out.verts + 3 * vb);
+                }
+            }
+        }
+        __syncwarp();
     }
+    // halo row (row 0 of the next y brick): its place in its own segment
     if (n32) {
         const uint32_t *rY = slot_rec(cells, g, s0 + g.nxs);
-        for (uint32_t j = lane; j < n32; j += 32) {
-            const uint32_t rec = __ldg(rY + j), c = rec_col(rec);
-            M.set_lst(p, start32 + j, (32u << 8) | c);
-            M.set_ent(p, start32 + j, rec);
-            atomicOr(&S.xrow[p][32][c >> 5], 1u << (c & 31));
+        uint32_t hrun = 0;
+        for (uint32_t b = 0; b < n32; b += 32) {
+            const uint32_t j = b + lane;
+            const uint32_t rec = j < n32 ? __ldg(rY + j) : 0u;
+            const uint32_t cfg = rec_cfg(rec), info = rec_info(rec), c = rec_col(rec);
+            const bool l2 = rec_l2(rec);
+            const uint32_t nv = j < n32 ? nvert_of(tab, cfg, l2) + __popc(info & 7u) : 0u;
+            const uint32_t incl = warp_incl_scan(nv, lane);
+            if (j < n32) {
+                M.set_lst(p, start32 + j, (32u << 8) | c);
+                M.set_ent(p, start32 + j, pack_cell(hrun + incl - nv, 0u, cfg, l2));
+                M.set_info(p, start32 + j, info & 0x38u);
+                atomicOr(&S.xrow[p][32][c >> 5], 1u << (c & 31));
+            }
+            hrun += __shfl_sync(0xffffffffu, incl, 31);
         }
     }
     __syncwarp();
@@ -844,30 +911,17 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), 3) brick_sweep(const BatchHead
         // Count sweep: point planes z0..z1 as bit masks, computed from the
         // samples (the masks of plane k+1 are loaded while plane k is ranked).
         if constexpr (!EMIT)
-            load_plane<T>(vol, g.pts, g.iso, g.iso_u16, g.isole_u16, x0, y0, z0, S.mask[z0 & 1], lane);
+            load_plane<T>(vol, g.pts, g.iso, g.iso_u16, x0, y0, z0, S.mask[z0 & 1], lane);
         for (uint32_t k = z0; k <= kend; ++k) {
             const int cur = k & 1, prv = cur ^ 1;
             const int lp = EMIT ? cur : 0;                 // list slot of this plane
             const bool have_plane = k < g.cells.z;
             uint32_t L = 0;
             if constexpr (EMIT) {
-                if (have_plane) {
-                    L = load_slot_list<T>(cells, g, k, xs, yb, cur, lane, S, M, vol, k < z1);
-                    // the segment offsets of the rows (read only where cells are)
-                    if (L)
-                        for (uint32_t r = lane; r < HROWS; r += 32) {
-                            const uint32_t yy = y0 + r;
-                            uint2 own = make_uint2(0, 0), nxt = make_uint2(0, 0);
-                            if (yy < g.cells.y) {
-                                own = out.seg_off[seg_index(g, k, yy, xs)];
-                                if (xs + 1 < g.nxs) nxt = out.seg_off[seg_index(g, k, yy, xs + 1)];
-                            }
-                            S.segv[cur][r][0] = own.x; S.segv[cur][r][1] = nxt.x; S.segq[cur][r] = own.y;
-                        }
-                }
+                if (have_plane) L = emit_plane<T>(cells, g, vol, tab, out, err, k, z1, xs, yb, cur, lane, S, M);
             } else {
                 const uint64_t rowmask = ((1ull << min((uint32_t)ROWS, g.cells.y - y0)) - 1ull);
-                load_plane<T>(vol, g.pts, g.iso, g.iso_u16, g.isole_u16, x0, y0, k + 1, S.mask[(k + 1) & 1], lane);
+                load_plane<T>(vol, g.pts, g.iso, g.iso_u16, x0, y0, k + 1, S.mask[(k + 1) & 1], lane);
                 __syncwarp();
                 const uint64_t *mk = S.mask[cur].lt, *mk1 = S.mask[(k + 1) & 1].lt;
                 uint64_t act[GROUPS];
@@ -914,71 +968,42 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), 3) brick_sweep(const BatchHead
                 }
                 __syncwarp();
             }
-            // ranked active cells, 32 at a time
-            uint32_t run = 0;
-            uint32_t *const recs = EMIT ? nullptr : slot_rec(cells, g, cell_slot(g, k, yb, xs));
-            for (uint32_t base = 0; base < L; base += 32) {
-                const uint32_t i = base + lane;
-                const bool valid = i < L;
-                uint32_t packed = 0, cfg = 0, info = 0, nv = 0;
-                int r = 0, c = 0;
-                bool l2 = false, own = false;
-                uint32_t x = 0, y = 0;
-                float v[8];
-                if (valid) {
-                    const uint32_t e = M.lst(lp, i);
-                    r = e >> 8; c = e & 0xff;
-                    x = x0 + c; y = y0 + r;
-                    own = r < ROWS && c < W;
-                    if constexpr (EMIT) {
-                        // classified by the count sweep: the cell's record
-                        const uint32_t rec = M.ent(lp, i);
-                        cfg = rec_cfg(rec); l2 = rec_l2(rec); info = rec_info(rec);
-                        if (own && k < z1) load_cell(vol, g, x, y, k, v, true);
-                    } else {
-                        const uint64_t *mk = S.mask[cur].lt, *mk1 = S.mask[(k + 1) & 1].lt;
-                        const uint64_t *ek = S.mask[cur].le, *ek1 = S.mask[(k + 1) & 1].le;
-                        cfg = cfg_from_masks(mk[c], mk[c + 1], mk1[c], mk1[c + 1], r);
-                        l2 = needs_lut2(vol, g, tab, cfg, mk, mk1, c, r, x, y, k);
-                        info = info_from_bits(cfg, le4_from_masks(ek[c + 1], ek1[c], ek1[c + 1], r));
+            // count sweep: the ranked active cells, 32 at a time, classified
+            // and recorded in the cell store
+            if constexpr (!EMIT) {
+                uint32_t run = 0;
+                uint32_t *const recs = slot_rec(cells, g, cell_slot(g, k, yb, xs));
+                const uint64_t *mk = S.mask[cur].lt, *mk1 = S.mask[(k + 1) & 1].lt;
+                // can a sample equal the isovalue (uint16: only an integer isovalue)?
+                const bool can_eq = std::is_same<T, float>::value || g.isole_u16 == g.iso_u16 + 1u;
+                for (uint32_t base = 0; base < L; base += 32) {
+                    const uint32_t i = base + lane;
+                    const bool valid = i < L;
+                    uint32_t packed = 0;
+                    int r = 0;
+                    if (valid) {
+                        const uint32_t e = M.lst(lp, i);
+                        r = e >> 8;
+                        const int c = e & 0xff;
+                        const uint32_t x = x0 + c, y = y0 + r;
+                        const uint32_t cfg = cfg_from_masks(mk[c], mk[c + 1], mk1[c], mk1[c + 1], r);
+                        const bool l2 = needs_lut2(vol, g, tab, cfg, mk, mk1, c, r, x, y, k);
+                        uint32_t le4 = le4_from_masks(mk[c + 1], mk1[c], mk1[c + 1], r);   // below
+                        if (can_eq) le4 |= corner_eq4(vol, g, x, y, k);                      // or at
+                        const uint32_t info = info_from_bits(cfg, le4);
                         recs[i] = rec_pack((uint32_t)c, (uint32_t)r, cfg, l2, info);
                         n_l2 += l2;
+                        packed = (nvert_of(tab, cfg, l2) + __popc(info & 7u)) |
+                                 (quad_count(info, cfg, x, y, k, g.cells, n_drop) << 16);
                     }
-                    nv = nvert_of(tab, cfg, l2) + __popc(info & 7u);
-                    uint32_t nq = 0;
-                    if (own) nq = quad_count(info, cfg, x, y, k, g.cells, n_drop);
-                    packed = nv | (nq << 16);
-                }
-                const uint32_t incl = warp_incl_scan(packed, lane);
-                const uint32_t ex = run + incl - packed;
-                run += __shfl_sync(0xffffffffu, incl, 31);
-                if (valid && i == S.rowstart[cur][r]) S.rowbase[r] = ex;
-                __syncwarp();
-                if constexpr (!EMIT) {
+                    const uint32_t incl = warp_incl_scan(packed, lane);
+                    const uint32_t ex = run + incl - packed;
+                    run += __shfl_sync(0xffffffffu, incl, 31);
+                    if (valid && i == S.rowstart[cur][r]) S.rowbase[r] = ex;
+                    __syncwarp();
                     if (valid && i + 1 == S.rowstart[cur][r + 1]) S.rowtot[r] = ex + packed - S.rowbase[r];
-                } else if (valid) {
-                    const uint32_t rb = S.rowbase[r];
-                    const uint32_t vrel = c == W ? 0u : (ex & 0xffffu) - (rb & 0xffffu);
-                    const uint32_t qrel = (ex >> 16) - (rb >> 16);
-                    M.set_ent(cur, i, pack_cell(vrel, qrel, cfg, l2));
-                    M.set_info(cur, i, info);
-                    if (own && k < z1) {
-                        const uint64_t vb = (uint64_t)S.segv[cur][r][0] + vrel;
-                        if (vb + nv > out.vcap) {
-                            atomicOr(err, DEV_ERR_OVERFLOW);
-                        } else {
-                            Geo geo;
-                            geo.x0 = g.coord[x]; geo.x1 = g.coord[x + 1];
-                            geo.y0 = g.coord[g.pts.x + y]; geo.y1 = g.coord[g.pts.x + y + 1];
-                            geo.z0 = g.coord[g.pts.x + g.pts.y + k]; geo.z1 = g.coord[g.pts.x + g.pts.y + k + 1];
-                            cell_vertices(tab, v, geo, g.iso, cfg, l2, nvert_of(tab, cfg, l2), info, x, y, k,
-                                          out.verts + 3 * vb);
-                        }
-                    }
+                    __syncwarp();
                 }
-                __syncwarp();
-            }
-            if constexpr (!EMIT) {
                 if (y0 + lane < g.cells.y) {
                     const uint32_t t = S.rowstart[cur][lane] == S.rowstart[cur][lane + 1] ? 0u : S.rowtot[lane];
                     seg_cnt[seg_index(g, k, y0 + lane, xs)] = make_uint2(t & 0xffffu, t >> 16);
@@ -989,7 +1014,6 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), 3) brick_sweep(const BatchHead
             // k.  Owners are taken 32 at a time; their quads are compacted into
             // qwork and written one per lane.
             if constexpr (EMIT) if (k > z0) {
-                const uint32_t kp = k - 1;
                 const uint32_t Lp = S.rowstart[prv][HROWS];
                 for (uint32_t base = 0; base < Lp; base += 32) {
                     const uint32_t i = base + lane;
@@ -998,15 +1022,10 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), 3) brick_sweep(const BatchHead
                         const uint32_t e = M.lst(prv, i);
                         const int r = e >> 8, c = e & 0xff;
                         if (r < ROWS && c < W) {
-                            const uint32_t x = x0 + c, y = y0 + r;
-                            const uint32_t d = M.ent(prv, i);
-                            const uint32_t cfg = cell_cfg(d);
-                            const uint32_t info = M.info(prv, i);
-#pragma unroll
-                            for (int s = 0; s < 3; ++s)
-                                if ((info & (1u << s)) && owned_quad_in_volume(s, x, y, kp, g.cells) && owned_sign_change(cfg, s))
-                                    want |= 1u << s;
+                            const uint32_t info = M.info(prv, i);   // wanted edges (bits 0-2), ccw bits (3-5)
+                            want = info & 7u;
                             if (want) {
+                                const uint32_t d = M.ent(prv, i);
                                 // The ring cells of the owner's quads, by list index: the
                                 // owner (c, r) of plane k-1, (c, r+1) of plane k-1, (c, r)
                                 // and (c, r+1) of plane k, each possibly followed by its
