@@ -54,7 +54,8 @@ constexpr int NWB_EMIT = 8;               // of the emit sweep: 3 blocks per SM
 constexpr int nwb(bool emit) { return emit ? NWB_EMIT : NWB_COUNT; }
 constexpr int kMaxSlabs = 32;             // z slabs of a streamed host extraction
 constexpr int kTickets = 4 + 3 * kMaxSlabs; // work tickets: 4 for a batch, 3 per streamed slab
-constexpr int QBUF = 96;                  // quads of one round of owner cells (3 per cell)
+constexpr int QCAP = 256;                 // quad items of a plane kept in shared memory
+constexpr int QOVF = 3 * W * ROWS - QCAP; // quad items of a plane that spill to global scratch
 constexpr int SCAN_NT = 512, SCAN_ITEMS = 8, SCAN_TILE = SCAN_NT * SCAN_ITEMS;   // 4096 segments per tile: half the look-back chain of 2048
 
 // One volume of an extraction (a plain call has one, a batch many).
@@ -140,8 +141,8 @@ struct alignas(16) EmitSmem : RankSmem {
     uint16_t lst1[CAP];                // list of plane slot 1
     uint32_t segv[2][HROWS][2];        // vertex offset of (row, own / next segment)
     uint32_t segq[2][HROWS];           // quad offset of (row, own segment)
-    uint32_t qwork[QBUF];              // quads of one round of owner cells: owner lane | edge << 5 | wanted edges << 7
-    uint4 orec[32];                    // owners of the round, by lane: (entry | rank r1 << 16, r2 | r3 << 16, first quad, cell | info << 16)
+    uint16_t qitem[2][QCAP];           // the plane's quads in order: owner's list entry | owned edge << 13
+    uint32_t qn[2];                    // quads of the plane
     uint32_t ent[2][CAP];              // a cell's record, then (once classified) its packed cell: vrel 11 | qrel 10 | cfg 8 | lut2 1
     uint8_t info[2][CAP];              // own-edge bipolar/ccw bits
 };
@@ -155,6 +156,7 @@ struct Spill {                          // per warp slot, global memory
     uint32_t ent[2][OVF];
     uint16_t lst[2][OVF];
     uint8_t info[2][OVF];
+    uint16_t qitem[2][QOVF];
 };
 
 // A plane's entries: the first CAP in shared memory, the rest in the warp's
@@ -199,6 +201,16 @@ struct WarpMem {
     __device__ __forceinline__ void set_info(int p, uint32_t i, uint32_t v)
     {
         if (i < CAP) s->info[p][i] = (uint8_t)v; else g->info[p][i - CAP] = (uint8_t)v;
+    }
+    __device__ __forceinline__ uint32_t qitem(int p, uint32_t t) const
+    {
+        uint32_t v;
+        if (t < QCAP) v = s->qitem[p][t]; else v = g->qitem[p][t - QCAP];
+        return v;
+    }
+    __device__ __forceinline__ void set_qitem(int p, uint32_t t, uint32_t v)
+    {
+        if (t < QCAP) s->qitem[p][t] = (uint16_t)v; else g->qitem[p][t - QCAP] = (uint16_t)v;
     }
 };
 
@@ -698,6 +710,7 @@ __device__ __forceinline__ uint32_t emit_plane(uint32_t *cells, const Geom &g, c
             S.rowstart[p][32] = 0;
             S.rowstart[p][33] = 0;
             S.hact[p] = 0;
+            S.qn[p] = 0;
             *reinterpret_cast<uint4 *>(S.xrow[p][32]) = make_uint4(0u, 0u, 0u, 0u);
         }
         __syncwarp();
@@ -795,6 +808,9 @@ __device__ __forceinline__ uint32_t emit_plane(uint32_t *cells, const Geom &g, c
             M.set_lst(p, i + shift, (r << 8) | c);
             M.set_ent(p, i + shift, pack_cell(vrel, qrel, cfg, l2));
             M.set_info(p, i + shift, want | (info & 0x38u));   // the quads need only these: wanted edges, ccw bits
+            // the cell's quads, at their place among the plane's quads
+            for (uint32_t w = want, t = ex >> 16; w; w &= w - 1, ++t)
+                M.set_qitem(p, t, (i + shift) | ((uint32_t)(__ffs(w) - 1) << 13));
             atomicOr(&S.xrow[p][r][c >> 5], 1u << (c & 31));
             if (k < zv) {
                 const uint32_t nv = packed & 0xffffu;
@@ -813,6 +829,7 @@ __device__ __forceinline__ uint32_t emit_plane(uint32_t *cells, const Geom &g, c
         }
         __syncwarp();
     }
+    if (lane == 0) S.qn[p] = run >> 16;
     // halo row (row 0 of the next y brick): its place in its own segment
     if (n32) {
         const uint32_t *rY = slot_rec(cells, g, s0 + g.nxs);
@@ -1011,95 +1028,64 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), 3) brick_sweep(const BatchHead
                 n_act += L;
             }
             // quads of own cells of plane k-1: their +z ring cells are in plane
-            // k.  Owners are taken 32 at a time; their quads are compacted into
-            // qwork and written one per lane.
+            // k.  The plane's quads were listed in order as its cells were
+            // classified; each lane writes one.
             if constexpr (EMIT) if (k > z0) {
-                const uint32_t Lp = S.rowstart[prv][HROWS];
-                for (uint32_t base = 0; base < Lp; base += 32) {
-                    const uint32_t i = base + lane;
-                    uint32_t want = 0;
-                    if (i < Lp) {
-                        const uint32_t e = M.lst(prv, i);
-                        const int r = e >> 8, c = e & 0xff;
-                        if (r < ROWS && c < W) {
-                            const uint32_t info = M.info(prv, i);   // wanted edges (bits 0-2), ccw bits (3-5)
-                            want = info & 7u;
-                            if (want) {
-                                const uint32_t d = M.ent(prv, i);
-                                // The ring cells of the owner's quads, by list index: the
-                                // owner (c, r) of plane k-1, (c, r+1) of plane k-1, (c, r)
-                                // and (c, r+1) of plane k, each possibly followed by its
-                                // +x neighbour, the next entry of its row.  The three
-                                // ranks are taken once here for all of the owner's quads.
-                                const uint32_t qc = (uint32_t)c >> 5, bm = (1u << (c & 31)) - 1u;
-                                const uint32_t m0 = qc > 0 ? ~0u : bm, m1 = qc > 1 ? ~0u : (qc == 1 ? bm : 0u);
-                                const uint32_t m2 = qc > 2 ? ~0u : (qc == 2 ? bm : 0u), m3 = qc == 3 ? bm : 0u;
-                                auto rank = [&](int pl, int rr) -> uint32_t {
-                                    const uint4 w = *reinterpret_cast<const uint4 *>(S.xrow[pl][rr]);
-                                    return S.rowstart[pl][rr] + __popc(w.x & m0) + __popc(w.y & m1) + __popc(w.z & m2) +
-                                           __popc(w.w & m3);
-                                };
-                                const uint32_t r1 = rank(prv, r + 1), r2 = rank(cur, r), r3 = rank(cur, r + 1);
-                                S.orec[lane] = make_uint4(i | (r1 << 16), r2 | (r3 << 16), S.segq[prv][r] + cell_qrel(d),
-                                                          e | (info << 16));
-                            }
-                        }
+                const uint32_t Qp = S.qn[prv];
+                for (uint32_t t = lane; t < Qp; t += 32) {
+                    const uint32_t item = M.qitem(prv, t);
+                    const uint32_t i = item & 0x1fffu;
+                    const int s = (int)(item >> 13);
+                    const uint32_t e = M.lst(prv, i);
+                    const int r = e >> 8, c = e & 0xff;
+                    const uint32_t info = M.info(prv, i);   // wanted edges (bits 0-2), ccw bits (3-5)
+                    const uint64_t q = (uint64_t)S.segq[prv][r] + cell_qrel(M.ent(prv, i)) +
+                                       __popc(info & 7u & ((1u << s) - 1u));
+                    if (q >= out.qcap) {
+                        atomicOr(err, DEV_ERR_OVERFLOW);
+                        continue;
                     }
-                    const uint32_t nq = __popc(want);
-                    const uint32_t qinc = warp_incl_scan(nq, lane);
-                    const uint32_t qtot = __shfl_sync(0xffffffffu, qinc, 31);
-                    {
-                        uint32_t pos = qinc - nq, w = want;
-                        while (w) {
-                            const int s = __ffs(w) - 1;
-                            w &= w - 1;
-                            S.qwork[pos++] = (uint32_t)lane | ((uint32_t)s << 5) | (want << 7);
-                        }
-                    }
-                    __syncwarp();
-                    for (uint32_t qb = 0; qb < qtot; qb += 32) {
-                        if (qb + lane < qtot) {
-                            const uint32_t item = S.qwork[qb + lane];
-                            const int s = (int)((item >> 5) & 3u);
-                            const uint32_t owant = item >> 7;
-                            const uint4 o = S.orec[item & 31u];
-                            const int r = (o.w >> 8) & 0xff, c = o.w & 0xff;
-                            const uint32_t info = o.w >> 16;
-                            const uint64_t q = (uint64_t)o.z + __popc(owant & ((1u << s) - 1u));
-                            if (q >= out.qcap) {
-                                atomicOr(err, DEV_ERR_OVERFLOW);
-                            } else {
-                                const uint32_t ring = s == 0 ? kRing6 : (s == 1 ? kRing9 : kRing10);
-                                const bool ccw = (info >> (s + 3)) & 1u;
-                                uint32_t idx[4];
-                                bool bad = false;
+                    // The ring cells of the quad, by list index: the owner (c, r)
+                    // of plane k-1 and the first cells at or after column c of
+                    // row r+1 of plane k-1 (r1), and of rows r (r2) and r+1 (r3)
+                    // of plane k, each possibly followed by its +x neighbour, the
+                    // next entry of its row.
+                    const uint32_t qc = (uint32_t)c >> 5, bm = (1u << (c & 31)) - 1u;
+                    const uint32_t m0 = qc > 0 ? ~0u : bm, m1 = qc > 1 ? ~0u : (qc == 1 ? bm : 0u);
+                    const uint32_t m2 = qc > 2 ? ~0u : (qc == 2 ? bm : 0u), m3 = qc == 3 ? bm : 0u;
+                    auto rank = [&](int pl, int rr) -> uint32_t {
+                        const uint4 w = *reinterpret_cast<const uint4 *>(S.xrow[pl][rr]);
+                        return S.rowstart[pl][rr] + __popc(w.x & m0) + __popc(w.y & m1) + __popc(w.z & m2) +
+                               __popc(w.w & m3);
+                    };
+                    const uint32_t ox = i | (rank(prv, r + 1) << 16), oy = rank(cur, r) | (rank(cur, r + 1) << 16);
+                    const uint32_t ring = s == 0 ? kRing6 : (s == 1 ? kRing9 : kRing10);
+                    const bool ccw = (info >> (s + 3)) & 1u;
+                    uint32_t idx[4];
+                    bool bad = false;
 #pragma unroll
-                                for (int it = 0; it < 4; ++it) {
-                                    const int kk = ccw ? it : (4 - it) & 3;    // ccw 0,1,2,3; cw 0,3,2,1 (dmc.cu:1636-1645)
-                                    const uint32_t sl = (ring >> (8 * kk)) & 0xffu;
-                                    const int pl = (sl & 1u) ? cur : prv;
-                                    const uint32_t plus = (sl >> 3) & 1u, rr = (uint32_t)r + ((sl >> 4) & 1u);
-                                    // base entry (sl bits 1-2): owner, r1, r2, r3; then its +x neighbour
-                                    const uint32_t bsel = (sl >> 1) & 3u;
-                                    const uint32_t bw = bsel < 2 ? o.x : o.y;
-                                    const uint32_t li = ((bsel & 1u) ? (bw >> 16) : (bw & 0xffffu)) + plus;
-                                    const bool ok = li < S.rowstart[pl][HROWS];
-                                    const uint32_t rd = ok ? M.ent(pl, li) : 0u;
-                                    const uint32_t m = lut_m(tab, cell_cfg(rd), cell_l2(rd), (int)ring_edge(s, kk));
-                                    bad |= !ok || m == 0xffu;
-                                    idx[it] = S.segv[pl][rr][(c + (int)plus) == W ? 1 : 0] + cell_vrel(rd) + (m == 0xffu ? 0u : m) - g.vbase;
-                                }
-                                if (bad) atomicOr(err, DEV_ERR_BOUNDS);
-                                reinterpret_cast<uint4 *>(out.quads)[q] = make_uint4(idx[0], idx[1], idx[2], idx[3]);
-                                if (out.tris) {
-                                    uint32_t *tp = out.tris + 6 * q;   // 4-byte stores: callers' buffers need only 4-byte alignment
-                                    tp[0] = idx[0]; tp[1] = idx[1]; tp[2] = idx[2];
-                                    tp[3] = idx[2]; tp[4] = idx[3]; tp[5] = idx[0];
-                                }
-                            }
-                        }
+                    for (int it = 0; it < 4; ++it) {
+                        const int kk = ccw ? it : (4 - it) & 3;    // ccw 0,1,2,3; cw 0,3,2,1 (dmc.cu:1636-1645)
+                        const uint32_t sl = (ring >> (8 * kk)) & 0xffu;
+                        const int pl = (sl & 1u) ? cur : prv;
+                        const uint32_t plus = (sl >> 3) & 1u, rr = (uint32_t)r + ((sl >> 4) & 1u);
+                        // base entry (sl bits 1-2): owner, r1, r2, r3; then its +x neighbour
+                        const uint32_t bsel = (sl >> 1) & 3u;
+                        const uint32_t bw = bsel < 2 ? ox : oy;
+                        const uint32_t li = ((bsel & 1u) ? (bw >> 16) : (bw & 0xffffu)) + plus;
+                        const bool ok = li < S.rowstart[pl][HROWS];
+                        const uint32_t rd = ok ? M.ent(pl, li) : 0u;
+                        const uint32_t m = lut_m(tab, cell_cfg(rd), cell_l2(rd), (int)ring_edge(s, kk));
+                        bad |= !ok || m == 0xffu;
+                        idx[it] = S.segv[pl][rr][(c + (int)plus) == W ? 1 : 0] + cell_vrel(rd) + (m == 0xffu ? 0u : m) - g.vbase;
                     }
-                    __syncwarp();
+                    if (bad) atomicOr(err, DEV_ERR_BOUNDS);
+                    reinterpret_cast<uint4 *>(out.quads)[q] = make_uint4(idx[0], idx[1], idx[2], idx[3]);
+                    if (out.tris) {
+                        uint32_t *tp = out.tris + 6 * q;   // 4-byte stores: callers' buffers need only 4-byte alignment
+                        tp[0] = idx[0]; tp[1] = idx[1]; tp[2] = idx[2];
+                        tp[3] = idx[2]; tp[4] = idx[3]; tp[5] = idx[0];
+                    }
                 }
             }
             __syncwarp();
