@@ -695,6 +695,16 @@ __device__ __forceinline__ uint32_t emit_plane(uint32_t *cells, const Geom &g, c
     const uint64_t s0 = cell_slot(g, k, yb, xs);
     const uint32_t x0 = xs * W, y0 = yb * ROWS;
     const bool hx = xs + 1 < g.nxs, hy = yb + 1 < g.nyb;
+    // the rows' segment offsets, issued first (their latency overlaps the header)
+    uint2 so0 = make_uint2(0, 0), sn0 = make_uint2(0, 0), so1 = make_uint2(0, 0), sn1 = make_uint2(0, 0);
+    if (y0 + lane < g.cells.y) {
+        so0 = out.seg_off[seg_index(g, k, y0 + lane, xs)];
+        if (hx) sn0 = out.seg_off[seg_index(g, k, y0 + lane, xs + 1)];
+    }
+    if (lane == 0 && y0 + 32 < g.cells.y) {
+        so1 = out.seg_off[seg_index(g, k, y0 + 32, xs)];
+        if (hx) sn1 = out.seg_off[seg_index(g, k, y0 + 32, xs + 1)];
+    }
     const uint32_t *h0 = slot_hdr(cells, g, s0);
     const uint32_t *r0 = slot_rec(cells, g, s0);
     // own rows: lane r holds the first entry of row r and of row r+1
@@ -716,16 +726,9 @@ __device__ __forceinline__ uint32_t emit_plane(uint32_t *cells, const Geom &g, c
         __syncwarp();
         return 0;
     }
-    // segment offsets of the rows
-    for (uint32_t r = lane; r < HROWS; r += 32) {
-        const uint32_t yy = y0 + r;
-        uint2 own = make_uint2(0, 0), nxt = make_uint2(0, 0);
-        if (yy < g.cells.y) {
-            own = out.seg_off[seg_index(g, k, yy, xs)];
-            if (hx) nxt = out.seg_off[seg_index(g, k, yy, xs + 1)];
-        }
-        S.segv[p][r][0] = own.x; S.segv[p][r][1] = nxt.x; S.segq[p][r] = own.y;
-    }
+    // segment offsets of the rows (loaded before the slot header was checked)
+    S.segv[p][lane][0] = so0.x; S.segv[p][lane][1] = sn0.x; S.segq[p][lane] = so0.y;
+    if (lane == 0) { S.segv[p][32][0] = so1.x; S.segv[p][32][1] = sn1.x; S.segq[p][32] = so1.y; }
     // halo column (the next x brick's rows with an active column-0 cell) and
     // the corner cell of row 32
     uint32_t col0 = 0, hxrec = 0, n32 = 0, corner = 0, crec = 0;
