@@ -278,6 +278,19 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
     uint32_t lo[GROUPS] = {0, 0, 0, 0}, hi[GROUPS] = {0, 0, 0, 0};
     const bool pz = p < pts.z;
     const uint32_t nrow = pz ? min(34u, pts.y - y0) : 0u;
+    // the two halo columns x0+W, x0+W+1 (rows lane and 32+lane), loaded first
+    // so that their latency overlaps the tile's rows
+    float hv[2], hv2[2];
+    bool hin[2], hin2[2];
+#pragma unroll
+    for (int hc = 0; hc < 2; ++hc) {
+        const uint32_t x = x0 + W + hc;
+        const bool okx = pz && x < pts.x;
+        hin[hc] = okx && y0 + lane < pts.y;
+        hin2[hc] = okx && lane < 2 && y0 + 32 + lane < pts.y;
+        hv[hc] = hin[hc] ? sample_p(vol, pts, x, y0 + lane, p) : 0.f;
+        hv2[hc] = hin2[hc] ? sample_p(vol, pts, x, y0 + 32 + lane, p) : 0.f;
+    }
     const uint64_t sx = pts.x;
     const uint64_t plane0 = (uint64_t)p * pts.y;
     // Rows past the volume (or past 34) and columns past it give 0 bits: the
@@ -390,16 +403,10 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
             m.lt[lane + 32 * j] = (uint64_t)(lo[j] & rmask & cm) | ((uint64_t)(hi[j] & hmask & cm) << 32);
         }
     }
-#pragma unroll 1
+#pragma unroll
     for (int hc = 0; hc < 2; ++hc) {
-        const uint32_t x = x0 + W + hc;
-        const bool okx = pz && x < pts.x;
-        const uint32_t y = y0 + lane, y2 = y0 + 32 + lane;
-        const bool in1 = okx && y < pts.y, in2 = okx && lane < 2 && y2 < pts.y;
-        const float v = in1 ? sample_p(vol, pts, x, y, p) : 0.f;
-        const float v2 = in2 ? sample_p(vol, pts, x, y2, p) : 0.f;
-        const uint32_t l32 = __ballot_sync(0xffffffffu, in1 && v < iso);
-        const uint32_t h2 = __ballot_sync(0xffffffffu, in2 && v2 < iso) & 3u;
+        const uint32_t l32 = __ballot_sync(0xffffffffu, hin[hc] && hv[hc] < iso);
+        const uint32_t h2 = __ballot_sync(0xffffffffu, hin2[hc] && hv2[hc] < iso) & 3u;
         if (lane == 0) m.lt[W + hc] = (uint64_t)l32 | ((uint64_t)h2 << 32);
     }
 }
