@@ -638,7 +638,7 @@ def run_served_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
-def served_e2e(vols, local, plain=False, n=128):
+def served_e2e(vols, local, plain=False, n=128, max_batch=64):
     """End to end: a burst of n requests, each mesh copied into page-locked
     host buffers (a ring of reused ones, sized from the warm-up meshes, grown
     if ever short) and released once its copy is done.  The copies run on a
@@ -648,7 +648,7 @@ def served_e2e(vols, local, plain=False, n=128):
     import framework_gb300 as fg
     vid, iso, _ = request_trace(vols, n, 0, seed=4)
     d2h = 0
-    kw = dict(plain=True) if plain else {}
+    kw = dict(plain=True) if plain else dict(max_batch=max_batch)
     with fg.Server(local, vertex_arena=SERVED_VERTEX_ARENA, quad_arena=SERVED_QUAD_ARENA, **kw) as srv:
         idmap = [srv.add_volume(d["volume"]) for d in vols]
         vmax = qmax = 1
