@@ -410,19 +410,25 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
     }
 }
 
-// At-the-isovalue bits of corners 2, 5, 6, 7 of cell (x, y, z) (bit 0 corner
-// 2, bit 1 corner 5, bit 2 corner 6, bit 3 corner 7): sample == iso, the
-// cases where "at or below" differs from "below".  Read from the samples
-// (a few active cells per brick plane) instead of keeping a second mask per
-// sample.
+// Corners 2, 5, 6, 7 of cell (x, y, z), for their at-the-isovalue bits
+// (corner_eq4): where a sample equals the isovalue "at or below" differs from
+// "below".  Read from the samples (a few active cells per brick plane)
+// instead of keeping a second mask per sample; the loads are issued before
+// the cell is classified, so that their latency overlaps that work.
+struct Corners4 { float s2, s5, s6, s7; };
+
 template <class T>
-__device__ __forceinline__ uint32_t corner_eq4(const T *vol, const Geom &g, uint32_t x, uint32_t y, uint32_t z)
+__device__ __forceinline__ Corners4 load_corners4(const T *vol, const Geom &g, uint32_t x, uint32_t y, uint32_t z)
 {
     const uint64_t sy = g.pts.x, sz = (uint64_t)g.pts.x * g.pts.y;
     const T *p = vol + (uint64_t)z * sz + (uint64_t)y * sy + x;
-    const float s2 = load_sample(p, sy + 1), s5 = load_sample(p, sz + 1);
-    const float s6 = load_sample(p, sz + sy + 1), s7 = load_sample(p, sz + sy);
-    return (s2 == g.iso ? 1u : 0u) | (s5 == g.iso ? 2u : 0u) | (s6 == g.iso ? 4u : 0u) | (s7 == g.iso ? 8u : 0u);
+    return Corners4{load_sample(p, sy + 1), load_sample(p, sz + 1), load_sample(p, sz + sy + 1), load_sample(p, sz + sy)};
+}
+
+// bit 0 corner 2, bit 1 corner 5, bit 2 corner 6, bit 3 corner 7: sample == iso
+__device__ __forceinline__ uint32_t corner_eq4(const Corners4 &s, float iso)
+{
+    return (s.s2 == iso ? 1u : 0u) | (s.s5 == iso ? 2u : 0u) | (s.s6 == iso ? 4u : 0u) | (s.s7 == iso ? 8u : 0u);
 }
 
 // Reference bipolarity and ccw bits of the cell's own edges (dmc.cu:1199-1216)
@@ -774,24 +780,15 @@ __device__ __forceinline__ uint32_t emit_plane(uint32_t *cells, const Geom &g, c
     }
     __syncwarp();
     // own cells, 32 at a time; each round's records are read one round ahead
-    // and their corner lines prefetched into L2
-    const uint64_t sy = g.pts.x, sz = (uint64_t)g.pts.x * g.pts.y;
-    auto prefetch = [&](uint32_t w) {
-        const T *q = vol + (uint64_t)k * sz + (uint64_t)(y0 + rec_row(w)) * sy + x0 + rec_col(w);
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(q));
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(q + sy));
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(q + sz));
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(q + sz + sy));
-    };
+    // (an L2 prefetch of the next round's corner lines, tried here, made the
+    // sweep 3% slower)
     uint32_t run = 0;
     uint32_t nrec = (uint32_t)lane < lown ? __ldg(r0 + lane) : 0u;
-    if ((uint32_t)lane < lown && k < zv) prefetch(nrec);
     for (uint32_t b = 0; b < lown; b += 32) {
         const uint32_t i = b + lane;
         const bool valid = i < lown;
         const uint32_t rec = nrec;
         nrec = i + 32 < lown ? __ldg(r0 + i + 32) : 0u;
-        if (i + 32 < lown && k < zv) prefetch(nrec);
         const uint32_t r = rec_row(rec), c = rec_col(rec);
         const uint32_t shift = __shfl_sync(0xffffffffu, hcp, (int)r);
         const uint32_t first = __shfl_sync(0xffffffffu, st, (int)r);
@@ -1012,10 +1009,12 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), 3) brick_sweep(const BatchHead
                         r = e >> 8;
                         const int c = e & 0xff;
                         const uint32_t x = x0 + c, y = y0 + r;
+                        Corners4 eqs{0.f, 0.f, 0.f, 0.f};
+                        if (can_eq) eqs = load_corners4(vol, g, x, y, k);
                         const uint32_t cfg = cfg_from_masks(mk[c], mk[c + 1], mk1[c], mk1[c + 1], r);
                         const bool l2 = needs_lut2(vol, g, tab, cfg, mk, mk1, c, r, x, y, k);
                         uint32_t le4 = le4_from_masks(mk[c + 1], mk1[c], mk1[c + 1], r);   // below
-                        if (can_eq) le4 |= corner_eq4(vol, g, x, y, k);                      // or at
+                        if (can_eq) le4 |= corner_eq4(eqs, g.iso);                           // or at
                         const uint32_t info = info_from_bits(cfg, le4);
                         recs[i] = rec_pack((uint32_t)c, (uint32_t)r, cfg, l2, info);
                         n_l2 += l2;
