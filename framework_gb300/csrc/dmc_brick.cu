@@ -1222,10 +1222,9 @@ bool brick_supports(const ExtractArgs &a)
 
 constexpr size_t kEmitSmem = brick::kTablesBytes + sizeof(brick::EmitSmem) * brick::NWB_EMIT;
 constexpr size_t kCountSmem = brick::kTablesBytes + sizeof(brick::CountSmem) * brick::NWB_COUNT;
-// two emit blocks and three count blocks per SM (228 KB of shared memory,
+// three emit blocks and three count blocks per SM (228 KB of shared memory,
 // 1 KB of it reserved per block); what is left of the 256 KB is L1, which the
-// emit sweep's corner gathers use: 12 KB more shared memory per emit block
-// made it 4% slower
+// emit sweep's corner gathers use
 static_assert(3 * (kEmitSmem + 1024) <= 228 * 1024, "emit sweep: three blocks per SM must fit");
 static_assert(3 * (kCountSmem + 1024) <= 228 * 1024, "count sweep: three blocks per SM must fit");
 
