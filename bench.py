@@ -358,6 +358,36 @@ def run_batch(args, rank, world, dist=None):
             ex.extract_device(d["volume"], iso=d["iso"], vertices=vbuf, quads=qbuf)
     torch.cuda.synchronize()
     plain_s = (time.perf_counter() - t0) / plain_reps
+    # the same volumes as one-volume asynchronous batches on two contexts,
+    # each with its own stream: no batching across volumes, and no host wait
+    # between launches (a context waits only for its own previous volume)
+    exa = (ex, fg.Extractor(local, algo="brick"))
+    exa[1].set_option(fg.OPT_BRICK_PLANES, int(tune["planes"]))
+    sa = [torch.cuda.Stream(device=local) for _ in range(2)]
+    vmax, qmax = int(res[:, 1].max()), int(res[:, 3].max())
+    one_v = [torch.empty((max(vmax, 1), 3), device="cuda") for _ in range(2)]
+    one_q = [torch.empty((max(qmax, 1), 4), dtype=torch.int32, device="cuda") for _ in range(2)]
+
+    def one_by_one():
+        busy = [False, False]
+        for i, d in enumerate(vols):
+            c = i & 1
+            if busy[c]:
+                exa[c].batch_wait()
+            exa[c].extract_batch([d], one_v[c], one_q[c], mode="async", stream=sa[c])
+            busy[c] = True
+        for c in (0, 1):
+            if busy[c]:
+                exa[c].batch_wait()
+    one_by_one()                                  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(plain_reps):
+        one_by_one()
+    torch.cuda.synchronize()
+    single_s = (time.perf_counter() - t0) / plain_reps
+    exa[1].close()
+    del one_v, one_q
     # end to end: pinned host volumes in, host meshes out, per step.  The
     # volumes go up, through and down in 8 groups on two contexts (asynchronous
     # batches), so that one group's upload, another's extraction and a third's
@@ -455,6 +485,8 @@ def run_batch(args, rank, world, dist=None):
                        "gvox_per_s": round(N / (ms * 1e-3) / 1e9, 3),
                        "plain_volumes_per_s": round(n / plain_s, 2),
                        "batched_over_plain": round((n / (ms * 1e-3)) / (n / plain_s), 2),
+                       "single_async_volumes_per_s": round(n / single_s, 2),
+                       "batched_over_single_async": round((n / (ms * 1e-3)) / (n / single_s), 2),
                        "kernel_ms": {"count": round(st["count_ms"], 4), "scan": round(st["scan_ms"], 4),
                                      "emit": round(st["emit_ms"], 4)},
                        "l2": "batch input %.0f MB > L2 (no flush needed)" % (4 * N / 1e6)},
@@ -1034,7 +1066,8 @@ def main():
         if line is not None:
             line["batched"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "e2e", "roofline")}
             line["batched"].update({k: b["config"][k] for k in ("volumes", "points", "plain_volumes_per_s",
-                                                               "batched_over_plain", "autotune", "kernel_ms")})
+                                                               "batched_over_plain", "single_async_volumes_per_s",
+                                                               "batched_over_single_async", "autotune", "kernel_ms")})
             line["served"] = {"value": sv["value"], "unit": sv["unit"], "e2e": sv["e2e"]}
             line["served"].update({k: sv["config"][k] for k in ("volumes", "pool_bytes", "served_over_plain",
                                                                 "p99_ms_at_0.8_served_capacity", "sweep")})
