@@ -1064,15 +1064,14 @@ def main():
         torch.cuda.empty_cache()
         sv = run_served(sub, rank, world, dist)
         if line is not None:
-            line["batched"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "e2e", "roofline")}
+            line["batched"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "e2e", "roofline", "gpu_launches")}
             line["batched"].update({k: b["config"][k] for k in ("volumes", "points", "plain_volumes_per_s",
                                                                "batched_over_plain", "single_async_volumes_per_s",
                                                                "batched_over_single_async", "autotune", "kernel_ms")})
-            line["served"] = {"value": sv["value"], "unit": sv["unit"], "e2e": sv["e2e"]}
+            line["served"] = {"value": sv["value"], "unit": sv["unit"], "e2e": sv["e2e"], "gpu_launches": sv["gpu_launches"]}
             line["served"].update({k: sv["config"][k] for k in ("volumes", "pool_bytes", "served_over_plain",
                                                                 "p99_ms_at_0.8_served_capacity", "sweep")})
             line["served"]["plain_capacity_rps"] = sv["config"]["plain"]["capacity_rps"]
-            line["gpu_launches"] += b["gpu_launches"] + sv["gpu_launches"]
     if line is not None:
         print(json.dumps(line), flush=True)
     if dist:
