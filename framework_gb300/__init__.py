@@ -34,7 +34,7 @@ ALGO = {"auto": 0, "simple": 1, "brick": 2}
 
 # exported symbols of the C ABI (include/dmc_gb300.h)
 ABI_SYMBOLS = [
-    "dmc_version", "dmc_tables_sha256", "dmc_status_string", "dmc_create", "dmc_destroy",
+    "dmc_version", "dmc_tables_sha256", "dmc_status_string", "dmc_last_cuda_error", "dmc_create", "dmc_destroy",
     "dmc_set_algo", "dmc_run", "dmc_run_into", "dmc_mesh_free", "dmc_extract_device", "dmc_get_stats",
     "dmc_extract_batch", "dmc_batch_wait", "dmc_set_option", "dmc_extract_device_noalloc",
     "dmc_server_create", "dmc_server_destroy", "dmc_server_add_volume", "dmc_server_submit", "dmc_server_wait",
@@ -50,8 +50,19 @@ OPT_FAIL_ALLOCS = 3       # test hook: the context's next n device allocations f
 class DMCError(RuntimeError):
     def __init__(self, status, what=""):
         self.status = int(status)
-        super().__init__("%s%s" % (STATUS.get(self.status, "status %d" % self.status),
-                                   (": " + what) if what else ""))
+        # for DMC_ERR_OOM / DMC_ERR_CUDA, the CUDA error behind it
+        self.cuda_error = last_cuda_error() if self.status in (2, 5) else ""
+        super().__init__("%s%s%s" % (STATUS.get(self.status, "status %d" % self.status),
+                                     (": " + what) if what else "",
+                                     (" (%s)" % self.cuda_error) if self.cuda_error else ""))
+
+
+def last_cuda_error():
+    """``dmc_last_cuda_error``: the CUDA error behind the last DMC_ERR_CUDA or
+    DMC_ERR_OOM on this thread, or ""."""
+    if _lib is None:            # nothing was called yet
+        return ""
+    return _lib.dmc_last_cuda_error().decode()
 
 
 class _Volume(ctypes.Structure):
@@ -126,6 +137,8 @@ def load_library(build_if_missing=True):
     L.dmc_tables_sha256.restype = ctypes.c_char_p
     L.dmc_status_string.restype = ctypes.c_char_p
     L.dmc_status_string.argtypes = [ctypes.c_int]
+    L.dmc_last_cuda_error.restype = ctypes.c_char_p
+    L.dmc_last_cuda_error.argtypes = []
     L.dmc_create.argtypes = [P(ctypes.c_void_p), ctypes.c_int]
     L.dmc_destroy.argtypes = [ctypes.c_void_p]
     L.dmc_set_algo.argtypes = [ctypes.c_void_p, ctypes.c_int]
@@ -171,7 +184,7 @@ def load_library(build_if_missing=True):
                                              ctypes.c_void_p, P(ctypes.c_uint64), P(ctypes.c_uint64),
                                              ctypes.c_void_p]
     for name in ABI_SYMBOLS:
-        if name not in ("dmc_version", "dmc_tables_sha256", "dmc_status_string", "dmc_mesh_free"):
+        if name not in ("dmc_version", "dmc_tables_sha256", "dmc_status_string", "dmc_last_cuda_error", "dmc_mesh_free"):
             getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L

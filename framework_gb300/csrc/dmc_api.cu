@@ -1,5 +1,6 @@
 // C ABI entry points (include/dmc_gb300.h): context, table upload, host and
 // device forms of the extraction.
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #include <unistd.h>
@@ -10,8 +11,14 @@
 
 namespace dmc {
 
-static thread_local cudaError_t g_last_cuda = cudaSuccess;
-void set_last_cuda_error(cudaError_t e) { g_last_cuda = e; }
+// The CUDA error behind the last DMC_ERR_CUDA / DMC_ERR_OOM of this thread,
+// as the reference's error check prints it before exiting
+// (cuda_includes.h:13-19): the error's name and description.
+static thread_local char g_last_cuda[256];
+void set_last_cuda_error(cudaError_t e)
+{
+    snprintf(g_last_cuda, sizeof(g_last_cuda), "%s: %s", cudaGetErrorName(e), cudaGetErrorString(e));
+}
 
 // The DMC_OPT_FAIL_ALLOCS hook: true while allocations are to fail.
 static bool fake_oom(Ctx *ctx)
@@ -163,6 +170,8 @@ const char *dmc_version(void) { return "gb300-dmc 0.1.0 (sm_103a)"; }
 
 const char *dmc_tables_sha256(void) { return DMC_TABLES_SHA256; }
 
+const char *dmc_last_cuda_error(void) { return g_last_cuda; }
+
 const char *dmc_status_string(dmc_status s)
 {
     switch (s) {
@@ -184,7 +193,9 @@ dmc_status dmc_create(dmc_ctx **out, int device)
     if (!out) return DMC_ERR_INVALID_ARG;
     *out = nullptr;
     int n = 0;
-    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return DMC_ERR_INVALID_ARG;
+    const cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) set_last_cuda_error(e);
+    if (e != cudaSuccess || device < 0 || device >= n) return DMC_ERR_INVALID_ARG;
     dmc_ctx *ctx = new (std::nothrow) dmc_ctx();
     if (!ctx) return DMC_ERR_OOM;
     Ctx *c = &ctx->c;

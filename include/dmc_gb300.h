@@ -92,6 +92,11 @@ const char *dmc_version(void);
 const char *dmc_tables_sha256(void);
 /* Human-readable name of a status. */
 const char *dmc_status_string(dmc_status s);
+/* The CUDA error behind the last DMC_ERR_CUDA or DMC_ERR_OOM returned on the
+ * calling thread ("cudaErrorName: description"), or "" if there was none;
+ * also set when dmc_create finds no usable device.  The reference prints the
+ * same before exit(1) (cuda_includes.h:13-19). */
+const char *dmc_last_cuda_error(void);
 
 /* Replaces dmc::setup_device_luts() (dmc.hpp:40, dmc.cu:713-779): creates a
  * context bound to CUDA device `device` holding its stream, lookup tables and

@@ -58,6 +58,9 @@ def test_create_without_gpu_fails_cleanly():
     L = fg.load_library()
     h = ctypes.c_void_p()
     assert L.dmc_create(ctypes.byref(h), 0) == 1  # DMC_ERR_INVALID_ARG: no such device
+    # the CUDA error behind it, as the reference would print it before exiting
+    assert L.dmc_last_cuda_error().startswith(b"cudaError")
+    assert fg.last_cuda_error().startswith("cudaError")
     with pytest.raises(fg.DMCError):
         fg.Extractor(0)
 
