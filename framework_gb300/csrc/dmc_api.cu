@@ -25,6 +25,7 @@ static bool fake_oom(Ctx *ctx)
 {
     if (!ctx->fail_allocs) return false;
     --ctx->fail_allocs;
+    set_last_cuda_error(cudaErrorMemoryAllocation);   // as the failing cudaMalloc would report
     return true;
 }
 

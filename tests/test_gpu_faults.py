@@ -56,6 +56,7 @@ def test_batch_recovers_from_allocation_failure(mode):
         with pytest.raises(fg.DMCError) as e:
             ex.extract_batch(big)                     # a larger layout: the old scratch goes, the new one fails
         assert e.value.status == OOM
+        assert e.value.cuda_error.startswith("cudaErrorMemoryAllocation")
         _check_batch(ex, big, mode)                   # carved again on a new scratch
         _check_batch(ex, small, mode)
 
