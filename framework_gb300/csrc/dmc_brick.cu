@@ -413,16 +413,20 @@ __device__ __noinline__ void load_plane(const T *vol, uint3 pts, float iso, uint
 // Corners 2, 5, 6, 7 of cell (x, y, z), for their at-the-isovalue bits
 // (corner_eq4): where a sample equals the isovalue "at or below" differs from
 // "below".  Read from the samples (a few active cells per brick plane)
-// instead of keeping a second mask per sample; the loads are issued before
-// the cell is classified, so that their latency overlaps that work.
+// instead of keeping a second mask per sample.  Only corners that are not
+// below the isovalue (their bit clear in the configuration) can equal it, so
+// only those are read; the others get a NaN, which equals nothing.
 struct Corners4 { float s2, s5, s6, s7; };
 
 template <class T>
-__device__ __forceinline__ Corners4 load_corners4(const T *vol, const Geom &g, uint32_t x, uint32_t y, uint32_t z)
+__device__ __forceinline__ Corners4 load_corners4(const T *vol, const Geom &g, uint32_t x, uint32_t y, uint32_t z,
+                                                  uint32_t cfg)
 {
     const uint64_t sy = g.pts.x, sz = (uint64_t)g.pts.x * g.pts.y;
     const T *p = vol + (uint64_t)z * sz + (uint64_t)y * sy + x;
-    return Corners4{load_sample(p, sy + 1), load_sample(p, sz + 1), load_sample(p, sz + sy + 1), load_sample(p, sz + sy)};
+    const float none = __int_as_float(0x7fc00000);
+    return Corners4{(cfg >> 2) & 1u ? none : load_sample(p, sy + 1), (cfg >> 5) & 1u ? none : load_sample(p, sz + 1),
+                    (cfg >> 6) & 1u ? none : load_sample(p, sz + sy + 1), (cfg >> 7) & 1u ? none : load_sample(p, sz + sy)};
 }
 
 // bit 0 corner 2, bit 1 corner 5, bit 2 corner 6, bit 3 corner 7: sample == iso
@@ -1009,9 +1013,9 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), 3) brick_sweep(const BatchHead
                         r = e >> 8;
                         const int c = e & 0xff;
                         const uint32_t x = x0 + c, y = y0 + r;
-                        Corners4 eqs{0.f, 0.f, 0.f, 0.f};
-                        if (can_eq) eqs = load_corners4(vol, g, x, y, k);
                         const uint32_t cfg = cfg_from_masks(mk[c], mk[c + 1], mk1[c], mk1[c + 1], r);
+                        Corners4 eqs{0.f, 0.f, 0.f, 0.f};
+                        if (can_eq) eqs = load_corners4(vol, g, x, y, k, cfg);
                         const bool l2 = needs_lut2(vol, g, tab, cfg, mk, mk1, c, r, x, y, k);
                         uint32_t le4 = le4_from_masks(mk[c + 1], mk1[c], mk1[c + 1], r);   // below
                         if (can_eq) le4 |= corner_eq4(eqs, g.iso);                           // or at
