@@ -57,6 +57,8 @@ constexpr int kTickets = 4 + 3 * kMaxSlabs; // work tickets: 4 for a batch, 3 pe
 constexpr int QCAP = 256;                 // quad items of a plane kept in shared memory
 constexpr int QOVF = 3 * W * ROWS - QCAP; // quad items of a plane that spill to global scratch
 constexpr int SCAN_NT = 512, SCAN_ITEMS = 8, SCAN_TILE = SCAN_NT * SCAN_ITEMS;   // 4096 segments per tile: half the look-back chain of 2048
+// a segment's count packs its vertices (at most 7 per cell) and quads (3) in 16 bits each; a thread's items add in place
+static_assert(SCAN_ITEMS * 7 * W < 65536 && SCAN_ITEMS * 3 * W < 65536, "packed segment counts must not carry between halves");
 
 // One volume of an extraction (a plain call has one, a batch many).
 struct Geom {
@@ -876,7 +878,7 @@ __device__ __forceinline__ uint32_t emit_plane(uint32_t *cells, const Geom &g, c
 template <class T, bool EMIT>
 __global__ void __launch_bounds__(32 * nwb(EMIT), 3) brick_sweep(const BatchHead *__restrict__ head, uint32_t group,
                                                                  BrickRange range, const DeviceTables *__restrict__ tabp,
-                                                                 uint2 *__restrict__ seg_cnt, EmitOut out,
+                                                                 uint32_t *__restrict__ seg_cnt, EmitOut out,
                                                                  Spill *__restrict__ spill, uint32_t *__restrict__ cells,
                                                                  uint32_t *ticket, unsigned long long *counters,
                                                                  uint32_t *err)
@@ -1035,7 +1037,7 @@ __global__ void __launch_bounds__(32 * nwb(EMIT), 3) brick_sweep(const BatchHead
                 }
                 if (y0 + lane < g.cells.y) {
                     const uint32_t t = S.rowstart[cur][lane] == S.rowstart[cur][lane + 1] ? 0u : S.rowtot[lane];
-                    seg_cnt[seg_index(g, k, y0 + lane, xs)] = make_uint2(t & 0xffffu, t >> 16);
+                    seg_cnt[seg_index(g, k, y0 + lane, xs)] = t;   // vertices | quads << 16
                 }
                 n_act += L;
             }
@@ -1142,7 +1144,7 @@ __global__ void batch_prep(const BatchHead *__restrict__ head, TileState *tiles,
 }
 
 // After the scan: each volume's first vertex / quad and its counts.
-__global__ void volume_results(BatchHead *head, const uint2 *seg_cnt, const uint2 *seg_off,
+__global__ void volume_results(BatchHead *head, const uint32_t *seg_cnt, const uint2 *seg_off,
                                const unsigned long long *totals, dmc_batch_result *res)
 {
     Geom *vols = const_cast<Geom *>(batch_geoms(head));
@@ -1154,9 +1156,10 @@ __global__ void volume_results(BatchHead *head, const uint2 *seg_cnt, const uint
             if (g.seg_base < head->nseg) { r.vertex_offset = seg_off[g.seg_base].x; r.quad_offset = seg_off[g.seg_base].y; }
             else { r.vertex_offset = totals[0]; r.quad_offset = totals[1]; }
         } else {
-            const uint2 f = seg_off[g.seg_base], lo = seg_off[g.seg_base + g.nseg - 1], lc = seg_cnt[g.seg_base + g.nseg - 1];
-            r.vertex_offset = f.x; r.n_vertices = (unsigned long long)lo.x + lc.x - f.x;
-            r.quad_offset = f.y; r.n_quads = (unsigned long long)lo.y + lc.y - f.y;
+            const uint2 f = seg_off[g.seg_base], lo = seg_off[g.seg_base + g.nseg - 1];
+            const uint32_t lc = seg_cnt[g.seg_base + g.nseg - 1];
+            r.vertex_offset = f.x; r.n_vertices = (unsigned long long)lo.x + (lc & 0xffffu) - f.x;
+            r.quad_offset = f.y; r.n_quads = (unsigned long long)lo.y + (lc >> 16) - f.y;
             g.vbase = f.x; g.qbase = f.y;
         }
         if (res) res[g.item] = r;
@@ -1179,7 +1182,7 @@ __global__ void snap_totals(const DevCtl *ctl, unsigned long long *dst)
 // segment scan (decoupled look-back)
 
 // Scans segments [seg_lo, seg_lo + seg_cnt) (clipped to the plan's segments).
-__global__ void __launch_bounds__(SCAN_NT) seg_scan(const BatchHead *__restrict__ head, const uint2 *__restrict__ cnt,
+__global__ void __launch_bounds__(SCAN_NT) seg_scan(const BatchHead *__restrict__ head, const uint32_t *__restrict__ cnt,
                                                     ScanCtl ctl, uint2 *__restrict__ off, uint64_t seg_lo, uint64_t seg_cnt)
 {
     __shared__ uint32_t s_slot;
@@ -1195,13 +1198,17 @@ __global__ void __launch_bounds__(SCAN_NT) seg_scan(const BatchHead *__restrict_
         const uint32_t tile = claim_tile(ctl.ticket, &s_slot);
         if (tile >= ctl.n_tiles) break;
         const uint64_t first = (uint64_t)tile * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
-        uint2 c[SCAN_ITEMS];
-        uint32_t sv = 0, sq = 0;
+        // a segment's count is vertices | quads << 16 (at most 7 and 3 per
+        // cell of a 128-cell row), so the packed words of a thread's items
+        // add without a carry between the halves
+        uint32_t c[SCAN_ITEMS];
+        uint32_t sum = 0;
 #pragma unroll
         for (int i = 0; i < SCAN_ITEMS; ++i) {
-            c[i] = first + i < n ? cnt[first + i] : make_uint2(0, 0);
-            sv += c[i].x; sq += c[i].y;
+            c[i] = first + i < n ? cnt[first + i] : 0u;
+            sum += c[i];
         }
+        const uint32_t sv = sum & 0xffffu, sq = sum >> 16;
         unsigned long long tot;
         unsigned long long ex = block_exclusive_scan<SCAN_NT>((unsigned long long)sv | ((unsigned long long)sq << 32), s_warp, &tot);
         tile_prefix(ctl, tile, (uint32_t)tot, (uint32_t)(tot >> 32), s_ex);
@@ -1209,7 +1216,7 @@ __global__ void __launch_bounds__(SCAN_NT) seg_scan(const BatchHead *__restrict_
 #pragma unroll
         for (int i = 0; i < SCAN_ITEMS; ++i) {
             if (first + i < n) off[first + i] = make_uint2((uint32_t)bv, (uint32_t)bq);
-            bv += c[i].x; bq += c[i].y;
+            bv += c[i] & 0xffffu; bq += c[i] >> 16;
         }
     }
 }
@@ -1277,7 +1284,8 @@ struct BatchState {
     uint64_t layout_id = 0;            // bumped on every re-carve: captured graphs hold the addresses
     // device layout (inside ctx->scratch)
     brick::BatchHead *d_plan = nullptr;
-    uint2 *seg_cnt = nullptr, *seg_off = nullptr;
+    uint32_t *seg_cnt = nullptr;   // per segment: vertices | quads << 16
+    uint2 *seg_off = nullptr;
     TileState *tiles = nullptr;
     brick::Spill *spill = nullptr;
     uint32_t *cells = nullptr;          // cell store, cap_cell words
@@ -1386,7 +1394,7 @@ static dmc_status batch_layout(Ctx *ctx, BatchState &b, uint32_t items, uint64_t
     size_t off = 0;
     auto carve = [&](size_t bytes) { size_t r = off; off += (bytes + 255) & ~(size_t)255; return r; };
     const size_t o_plan = carve(b.plan_bytes);
-    const size_t o_cnt = carve(8 * b.cap_seg), o_off = carve(8 * b.cap_seg);
+    const size_t o_cnt = carve(4 * b.cap_seg), o_off = carve(8 * b.cap_seg);
     const size_t o_tiles = carve(sizeof(TileState) * (cap_tiles + kMaxSlabs));   // slabs: one partial tile each
     const size_t o_spill = carve(sizeof(Spill) * (size_t)sweep_warps(b));
     const size_t o_cell = carve(4 * b.cap_cell);
@@ -1398,7 +1406,7 @@ static dmc_status batch_layout(Ctx *ctx, BatchState &b, uint32_t items, uint64_t
     if (s != DMC_OK) return s;
     uint8_t *base = (uint8_t *)ctx->scratch;
     b.d_plan = (BatchHead *)(base + o_plan);
-    b.seg_cnt = (uint2 *)(base + o_cnt);
+    b.seg_cnt = (uint32_t *)(base + o_cnt);
     b.seg_off = (uint2 *)(base + o_off);
     b.tiles = (TileState *)(base + o_tiles);
     b.spill = (Spill *)(base + o_spill);
