@@ -56,7 +56,7 @@ constexpr int kMaxSlabs = 32;             // z slabs of a streamed host extracti
 constexpr int kTickets = 4 + 3 * kMaxSlabs; // work tickets: 4 for a batch, 3 per streamed slab
 constexpr int QCAP = 256;                 // quad items of a plane kept in shared memory
 constexpr int QOVF = 3 * W * ROWS - QCAP; // quad items of a plane that spill to global scratch
-constexpr int SCAN_NT = 512, SCAN_ITEMS = 8, SCAN_TILE = SCAN_NT * SCAN_ITEMS;   // 4096 segments per tile: half the look-back chain of 2048
+constexpr int SCAN_NT = 512, SCAN_ITEMS = 16, SCAN_TILE = SCAN_NT * SCAN_ITEMS;  // 8192 segments per tile: a short look-back chain
 // a segment's count packs its vertices (at most 7 per cell) and quads (3) in 16 bits each; a thread's items add in place
 static_assert(SCAN_ITEMS * 7 * W < 65536 && SCAN_ITEMS * 3 * W < 65536, "packed segment counts must not carry between halves");
 
